@@ -1,0 +1,328 @@
+"""Benchmark: batched c32 DFT throughput on GB300 against the measured HBM roofline.
+
+Workload (the mixed-radix / prime parity set): complex c32 DFT, forward, at
+N in {1000, 1536, 2187, 30720, 127, 8191} with batch = 256 MiB / (8 N) signals each (33554, 21845, 15343,
+1092, 264208, 4096).  One step = one forward pass over all six batches (1.5 GiB in, 1.5 GiB out); every
+input is larger than L2, so no flush is needed between steps.  Inputs are seeded i.i.d. N(0,1) times a
+seeded amplitude (synthetic; the reference publishes no dataset for this path).
+
+value   = algorithmic bytes (16 N per signal: read N c32 + write N c32) / device time of the step,
+          timed with CUDA events on the launching stream, inputs resident in HBM.
+e2e     = the same bytes / wall time of the same step through the C ABI with pinned HOST buffers
+          (kfr_dft_execute_batch_f32 with a NULL stream: H2D copy, kernels, D2H copy, synchronise).
+roofline: the kernel with the largest share of the step (per-length CUDA-event timing), its algorithmic
+          GB/s against MEASURED_PEAKS.json's HBM copy bandwidth.
+cpu_baseline: the CPU oracle's single-precision port (oracle/kfr_oracle.c, same algorithm family as
+          KFR's dft_plan<float>) on all host cores over a bounded sample of each batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs the full workload on its own GPU (batch sharding, no collective on the data
+path; weak scaling); rank 0 prints one JSON line with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZES = [1000, 1536, 2187, 30720, 127, 8191]
+BYTES_PER_SIZE = 256 << 20
+METRIC = "batched c32 DFT GB/s (% of HBM roofline), chosen vs plain form at ≤1e-6 rel RMS"
+FALLBACK_HBM_GBS = 6800.0
+
+# DRAM bytes per signal measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided
+# by the signals it processed); see profiles/ for the captures.  None = not captured.
+NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float | None] = {}
+
+
+def batch_for(n: int) -> int:
+    return BYTES_PER_SIZE // (8 * n)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(ngpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_inputs(torch, n, batch, seed, device):
+    g = torch.Generator(device=device).manual_seed(seed)
+    amp = 0.5 + float(np.random.default_rng(seed).uniform(0, 1))
+    x = torch.randn(batch, n, dtype=torch.complex64, device=device, generator=g) * amp
+    return x
+
+
+def cpu_baseline_run(steps_scale: float = 1.0, threads: int | None = None):
+    """Oracle f32 port on the host cores over 1/32 of each batch; returns (GB/s, sample description)."""
+    from oracle.oracle import Oracle
+
+    orc = Oracle("orc")
+    threads = threads or os.cpu_count() or 1
+    total_bytes, total_t = 0, 0.0
+    for n in SIZES:
+        b = max(1, int(batch_for(n) // 32 * steps_scale))
+        rng = np.random.default_rng(n)
+        x = (rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))).astype(np.complex64)
+        orc.dft(x[: max(1, b // 8)], precision="f32", threads=threads)  # warm the pages and plan path
+        t0 = time.perf_counter()
+        orc.dft(x, precision="f32", threads=threads)
+        total_t += time.perf_counter() - t0
+        total_bytes += 16 * n * b
+    return total_bytes / total_t / 1e9, threads, "1/32 of each batch (8 MiB per length), forward, all host threads"
+
+
+def run_reference(args):
+    rank, world, local = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), 0
+    if rank != 0:
+        return 0
+    for _ in range(args.warmup):
+        cpu_baseline_run(0.25)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, threads, sample = cpu_baseline_run()
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_dict(),
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_dict():
+    return {"workload": "c32 forward DFT, N in {1000,1536,2187,30720,127,8191}, 256 MiB batch per N",
+            "sizes": SIZES, "batches": [batch_for(n) for n in SIZES], "bytes_per_n": BYTES_PER_SIZE,
+            "l2": "every input (256 MiB) exceeds L2; no flush needed", "form": "plain"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import kfr_gb300 as k
+    from oracle.oracle import Oracle, rel_rms
+
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    hbm, peak_kind = peaks()
+
+    plans, xs, ys = {}, {}, {}
+    for i, n in enumerate(SIZES):
+        plans[n] = k.dft_plan(n, "f32")
+        xs[n] = make_inputs(torch, n, batch_for(n), 1000 + i + 97 * rank, dev)
+        ys[n] = torch.empty_like(xs[n])
+    temps = {n: torch.empty(max(1, plans[n].temp_size_batch(batch_for(n))), dtype=torch.uint8, device=dev)
+             for n in SIZES}
+
+    def step(events=None):
+        for n in SIZES:
+            if events is not None:
+                events[n][0].record(stream)
+            plans[n].execute_batch(ys[n], xs[n], batch_for(n), temp=temps[n], stream=stream)
+            if events is not None:
+                events[n][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # accuracy on a sample of each batch (outside the timed region)
+    orc = Oracle("orc")
+    errs = {}
+    for n in SIZES:
+        s = min(8, batch_for(n))
+        ref = orc.dft(xs[n][:s].cpu().numpy().astype(np.complex128), threads=os.cpu_count() or 1)
+        errs[n] = rel_rms(ys[n][:s].cpu().numpy(), ref)
+
+    clocks = ClockSampler(local)
+    ev = {n: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)] for n in SIZES}
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    start.record(stream)
+    for s in range(args.steps):
+        step({n: ev[n][s] for n in SIZES})
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    total_ms = max_over_ranks(start.elapsed_time(stop), world)
+    ms_step = total_ms / args.steps
+    bytes_step = sum(16 * n * batch_for(n) for n in SIZES)
+    value = bytes_step * world / (ms_step * 1e-3) / 1e9
+
+    per = {}
+    for n in SIZES:
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev[n]]))
+        gbs = 16 * n * batch_for(n) / (ms * 1e-3) / 1e9
+        per[n] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / hbm, 4),
+                  "gflops": round(5 * n * np.log2(n) * batch_for(n) / (ms * 1e-3) / 1e9, 1),
+                  "rel_rms": float(f"{errs[n]:.3e}"), "plan": None}
+    dom = max(SIZES, key=lambda n: per[n]["ms"])
+    traffic = NCU_TRAFFIC_BYTES_PER_SIGNAL.get(dom)
+    roof = {"bound": "hbm", "achieved": per[dom]["gbs"], "peak": hbm, "unit": "GB/s",
+            "frac": per[dom]["frac"], "traffic": (traffic * batch_for(dom)) if traffic else None,
+            "kernel": f"N={dom} ({'four-step' if dom == 30720 else 'block FFT'})", "peak_kind": peak_kind,
+            "step_frac": round(value / world / hbm, 4)}
+    launches = args.steps * sum(plans[n].launch_count(batch_for(n)) for n in SIZES)
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        hin = {n: xs[n].cpu().pin_memory() for n in SIZES}
+        hout = {n: torch.empty_like(hin[n]).pin_memory() for n in SIZES}
+
+        def e2e_step():
+            for n in SIZES:
+                plans[n].execute_batch(hout[n], hin[n], batch_for(n))
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        wall = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": round(bytes_step * world / (wall / args.steps) / 1e9, 3), "unit": "GB/s",
+               "h2d_bytes_per_step": bytes_step // 2, "d2h_bytes_per_step": bytes_step // 2,
+               "ms_per_step": round(wall / args.steps * 1e3, 3)}
+        del hin, hout
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, threads, sample = cpu_baseline_run()
+        cpu = {"value": round(v, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded N(0,1) x amplitude, c32",
+            "config": config_dict(), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk, "per_size": {str(n): per[n] for n in SIZES},
+            "max_rel_rms": float(f"{max(errs.values()):.3e}"),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,246 @@
+/*
+ * kfr_capi.h: C ABI of the GB300 DFT library, a drop-in for KFR 7.0.1's C API (include/kfr/capi.h).
+ *
+ * Every declaration in the first part has the same name, argument types, argument meaning and error
+ * behaviour as the reference entry point cited beside it, so a program (or a cgo / ctypes / JNI binding)
+ * built against the reference header links and runs against libkfr_capi.so from this repository:
+ *   - plans are opaque heap objects owned by the caller and freed with *_delete_plan (NULL allowed);
+ *   - no exception crosses the ABI: failures return NULL / 0 and leave a message for kfr_last_error();
+ *   - inverse transforms are unscaled; real plans use the CCs or Perm packing.
+ *
+ * What is different, because the work runs on the GPU:
+ *   - `in`, `out` and `temp` may be host pointers (staged through device memory; pinned host memory from
+ *     kfr_allocate copies fastest) or device pointers (used in place).  The call returns when the result
+ *     is in `out`, as the reference's does.
+ *   - `temp` is device scratch: a device pointer of at least *_get_temp_size bytes is used as scratch; a
+ *     NULL or host pointer makes the plan use scratch of its own.
+ *
+ * The second part declares additive extensions (batched and stream-ordered execution) that have no
+ * reference counterpart.
+ */
+#ifndef KFR_GB300_CAPI_H
+#define KFR_GB300_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined __STDC_IEC_559_COMPLEX__ && !defined KFR_NO_C_COMPLEX_TYPES
+#include <complex.h>
+#endif
+
+#ifdef __cplusplus
+extern "C"
+{
+#endif
+
+#if defined(_WIN32)
+#define KFR_API_SPEC __declspec(dllexport)
+#else
+#define KFR_API_SPEC __attribute__((visibility("default")))
+#endif
+
+/* kfr_bool as in include/kfr/capi.h:79-95 */
+#if defined(__STDC_VERSION__) && __STDC_VERSION__ >= 199901L
+typedef _Bool kfr_bool;
+#elif defined(__cplusplus)
+typedef bool kfr_bool;
+#else
+typedef char kfr_bool;
+#endif
+
+/* scalar and complex element types, include/kfr/capi.h:131-143 */
+typedef float kfr_f32;
+typedef double kfr_f64;
+#if defined __STDC_IEC_559_COMPLEX__ && !defined KFR_NO_C_COMPLEX_TYPES
+typedef float _Complex kfr_c32;
+typedef double _Complex kfr_c64;
+#define KFR_COMPLEX_SIZE_MULTIPLIER 1
+#else
+typedef float kfr_c32;
+typedef double kfr_c64;
+#define KFR_COMPLEX_SIZE_MULTIPLIER 2
+#endif
+
+/* opaque plan handles, include/kfr/capi.h:145-161 */
+#define KFR_OPAQUE_STRUCT(NAME)                                                                             \
+    typedef struct NAME                                                                                     \
+    {                                                                                                       \
+        int opaque;                                                                                         \
+    } NAME;
+KFR_OPAQUE_STRUCT(KFR_DFT_PLAN_F32)
+KFR_OPAQUE_STRUCT(KFR_DFT_PLAN_F64)
+KFR_OPAQUE_STRUCT(KFR_DFT_REAL_PLAN_F32)
+KFR_OPAQUE_STRUCT(KFR_DFT_REAL_PLAN_F64)
+KFR_OPAQUE_STRUCT(KFR_DCT_PLAN_F32)
+KFR_OPAQUE_STRUCT(KFR_DCT_PLAN_F64)
+KFR_OPAQUE_STRUCT(KFR_FILTER_F32)
+KFR_OPAQUE_STRUCT(KFR_FILTER_F64)
+KFR_OPAQUE_STRUCT(KFR_FILTER_C32)
+KFR_OPAQUE_STRUCT(KFR_FILTER_C64)
+
+#define KFR_DEFAULT_ALIGNMENT 64 /* include/kfr/capi.h:165 */
+#define KFR_HEADERS_VERSION 70000
+
+/* real DFT packing, include/kfr/capi.h:196-200 (values are part of the ABI) */
+typedef enum KFR_DFT_PACK_FORMAT
+{
+    Perm = 0, /* N/2 complex values; X[N/2].re is stored in out[0].im */
+    CCs  = 1  /* N/2 + 1 complex values */
+} KFR_DFT_PACK_FORMAT;
+
+/* ---- library information and errors ------------------------------------------------------------ */
+KFR_API_SPEC const char* kfr_version_string(void); /* capi.h:116 */
+KFR_API_SPEC uint32_t kfr_version(void);           /* capi.h:119: 70001 */
+KFR_API_SPEC const char* kfr_enabled_archs(void);  /* capi.h:122: "sm_103a" */
+KFR_API_SPEC int kfr_current_arch(void);           /* capi.h:125: compute capability, e.g. 103 */
+KFR_API_SPEC const char* kfr_last_error(void);     /* capi.h:128: thread-local, "" after a success */
+
+/* ---- host memory (pinned when a GPU is present, so staging copies run at DMA speed) ----------- */
+KFR_API_SPEC void* kfr_allocate(size_t size);                           /* capi.h:170 */
+KFR_API_SPEC void* kfr_allocate_aligned(size_t size, size_t alignment); /* capi.h:173 */
+KFR_API_SPEC void kfr_deallocate(void* ptr);                            /* capi.h:176 */
+
+/* ---- complex DFT ---------------------------------------------------------------------------------- */
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_plan_f32(size_t size);                              /* capi.h:207 */
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_2d_plan_f32(size_t size1, size_t size2);            /* capi.h:215 */
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_3d_plan_f32(size_t size1, size_t size2, size_t size3); /* capi.h:224 */
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_md_plan_f32(size_t dims, const unsigned* shape);    /* capi.h:232 */
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_plan_f64(size_t size);                              /* capi.h:239 */
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_2d_plan_f64(size_t size1, size_t size2);            /* capi.h:247 */
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_3d_plan_f64(size_t size1, size_t size2, size_t size3); /* capi.h:256 */
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_md_plan_f64(size_t dims, const unsigned* shape);    /* capi.h:264 */
+KFR_API_SPEC void kfr_dft_dump_f32(KFR_DFT_PLAN_F32* plan);                                       /* capi.h:270 */
+KFR_API_SPEC void kfr_dft_dump_f64(KFR_DFT_PLAN_F64* plan);                                       /* capi.h:276 */
+KFR_API_SPEC size_t kfr_dft_get_size_f32(KFR_DFT_PLAN_F32* plan);                                 /* capi.h:283 */
+KFR_API_SPEC size_t kfr_dft_get_size_f64(KFR_DFT_PLAN_F64* plan);                                 /* capi.h:290 */
+KFR_API_SPEC size_t kfr_dft_get_temp_size_f32(KFR_DFT_PLAN_F32* plan);                            /* capi.h:299 */
+KFR_API_SPEC size_t kfr_dft_get_temp_size_f64(KFR_DFT_PLAN_F64* plan);                            /* capi.h:308 */
+KFR_API_SPEC void kfr_dft_execute_f32(KFR_DFT_PLAN_F32* plan, kfr_c32* out, const kfr_c32* in,
+                                      uint8_t* temp); /* capi.h:320 */
+KFR_API_SPEC void kfr_dft_execute_f64(KFR_DFT_PLAN_F64* plan, kfr_c64* out, const kfr_c64* in,
+                                      uint8_t* temp); /* capi.h:333 */
+KFR_API_SPEC void kfr_dft_execute_inverse_f32(KFR_DFT_PLAN_F32* plan, kfr_c32* out, const kfr_c32* in,
+                                              uint8_t* temp); /* capi.h:346 */
+KFR_API_SPEC void kfr_dft_execute_inverse_f64(KFR_DFT_PLAN_F64* plan, kfr_c64* out, const kfr_c64* in,
+                                              uint8_t* temp); /* capi.h:359 */
+KFR_API_SPEC void kfr_dft_delete_plan_f32(KFR_DFT_PLAN_F32* plan); /* capi.h:366 */
+KFR_API_SPEC void kfr_dft_delete_plan_f64(KFR_DFT_PLAN_F64* plan); /* capi.h:372 */
+
+/* ---- real DFT -------------------------------------------------------------------------------------- */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_plan_f32(size_t size,
+                                                                 KFR_DFT_PACK_FORMAT pack_format); /* capi.h:380 */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_2d_plan_f32(size_t size1, size_t size2,
+                                                                    kfr_bool real_out_is_enough); /* capi.h:383 */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_3d_plan_f32(size_t size1, size_t size2, size_t size3,
+                                                                    kfr_bool real_out_is_enough); /* capi.h:385 */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_md_plan_f32(size_t dims, const unsigned* shape,
+                                                                    kfr_bool real_out_is_enough); /* capi.h:387 */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_plan_f64(size_t size,
+                                                                 KFR_DFT_PACK_FORMAT pack_format); /* capi.h:396 */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_2d_plan_f64(size_t size1, size_t size2,
+                                                                    kfr_bool real_out_is_enough); /* capi.h:399 */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_3d_plan_f64(size_t size1, size_t size2, size_t size3,
+                                                                    kfr_bool real_out_is_enough); /* capi.h:401 */
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_md_plan_f64(size_t dims, const unsigned* shape,
+                                                                    kfr_bool real_out_is_enough); /* capi.h:403 */
+KFR_API_SPEC void kfr_dft_real_dump_f32(KFR_DFT_REAL_PLAN_F32* plan);             /* capi.h:410 */
+KFR_API_SPEC void kfr_dft_real_dump_f64(KFR_DFT_REAL_PLAN_F64* plan);             /* capi.h:416 */
+KFR_API_SPEC size_t kfr_dft_real_get_size_f32(KFR_DFT_REAL_PLAN_F32* plan);       /* capi.h:423 */
+KFR_API_SPEC size_t kfr_dft_real_get_size_f64(KFR_DFT_REAL_PLAN_F64* plan);       /* capi.h:430 */
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_f32(KFR_DFT_REAL_PLAN_F32* plan);  /* capi.h:439 */
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_f64(KFR_DFT_REAL_PLAN_F64* plan);  /* capi.h:448 */
+KFR_API_SPEC void kfr_dft_real_execute_f32(KFR_DFT_REAL_PLAN_F32* plan, kfr_c32* out, const kfr_f32* in,
+                                           uint8_t* temp); /* capi.h:461 */
+KFR_API_SPEC void kfr_dft_real_execute_f64(KFR_DFT_REAL_PLAN_F64* plan, kfr_c64* out, const kfr_f64* in,
+                                           uint8_t* temp); /* capi.h:475 */
+KFR_API_SPEC void kfr_dft_real_execute_inverse_f32(KFR_DFT_REAL_PLAN_F32* plan, kfr_f32* out, const kfr_c32* in,
+                                                   uint8_t* temp); /* capi.h:489 */
+KFR_API_SPEC void kfr_dft_real_execute_inverse_f64(KFR_DFT_REAL_PLAN_F64* plan, kfr_f64* out, const kfr_c64* in,
+                                                   uint8_t* temp); /* capi.h:503 */
+KFR_API_SPEC void kfr_dft_real_delete_plan_f32(KFR_DFT_REAL_PLAN_F32* plan); /* capi.h:510 */
+KFR_API_SPEC void kfr_dft_real_delete_plan_f64(KFR_DFT_REAL_PLAN_F64* plan); /* capi.h:516 */
+
+/* ---- DCT-II / DCT-III ----------------------------------------------------------------------------- */
+KFR_API_SPEC KFR_DCT_PLAN_F32* kfr_dct_create_plan_f32(size_t size);     /* capi.h:523 */
+KFR_API_SPEC KFR_DCT_PLAN_F64* kfr_dct_create_plan_f64(size_t size);     /* capi.h:530 */
+KFR_API_SPEC void kfr_dct_dump_f32(KFR_DCT_PLAN_F32* plan);              /* capi.h:536 */
+KFR_API_SPEC void kfr_dct_dump_f64(KFR_DCT_PLAN_F64* plan);              /* capi.h:542 */
+KFR_API_SPEC size_t kfr_dct_get_size_f32(KFR_DCT_PLAN_F32* plan);        /* capi.h:549 */
+KFR_API_SPEC size_t kfr_dct_get_size_f64(KFR_DCT_PLAN_F64* plan);        /* capi.h:556 */
+KFR_API_SPEC size_t kfr_dct_get_temp_size_f32(KFR_DCT_PLAN_F32* plan);   /* capi.h:565 */
+KFR_API_SPEC size_t kfr_dct_get_temp_size_f64(KFR_DCT_PLAN_F64* plan);   /* capi.h:574 */
+KFR_API_SPEC void kfr_dct_execute_f32(KFR_DCT_PLAN_F32* plan, kfr_f32* out, const kfr_f32* in,
+                                      uint8_t* temp); /* capi.h:586 */
+KFR_API_SPEC void kfr_dct_execute_f64(KFR_DCT_PLAN_F64* plan, kfr_f64* out, const kfr_f64* in,
+                                      uint8_t* temp); /* capi.h:598 */
+KFR_API_SPEC void kfr_dct_execute_inverse_f32(KFR_DCT_PLAN_F32* plan, kfr_f32* out, const kfr_f32* in,
+                                              uint8_t* temp); /* capi.h:610 */
+KFR_API_SPEC void kfr_dct_execute_inverse_f64(KFR_DCT_PLAN_F64* plan, kfr_f64* out, const kfr_f64* in,
+                                              uint8_t* temp); /* capi.h:623 */
+KFR_API_SPEC void kfr_dct_delete_plan_f32(KFR_DCT_PLAN_F32* plan); /* capi.h:630 */
+KFR_API_SPEC void kfr_dct_delete_plan_f64(KFR_DCT_PLAN_F64* plan); /* capi.h:636 */
+
+/* ---- filters ------------------------------------------------------------------------------------------
+ * The FFT convolution filter (convolve_filter) is the GPU path.  The FIR and IIR creators are declared for
+ * link compatibility; they are not DFT work, are not built here and return NULL with an error message. */
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_fir_plan_f32(const kfr_f32* taps, size_t size); /* capi.h:644 */
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_fir_plan_f64(const kfr_f64* taps, size_t size); /* capi.h:652 */
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_convolution_plan_f32(const kfr_f32* taps, size_t size,
+                                                                    size_t block_size); /* capi.h:663 */
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_convolution_plan_f64(const kfr_f64* taps, size_t size,
+                                                                    size_t block_size); /* capi.h:675 */
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_iir_plan_f32(const kfr_f32* sos, size_t sos_count); /* capi.h:684 */
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_iir_plan_f64(const kfr_f64* sos, size_t sos_count); /* capi.h:692 */
+KFR_API_SPEC void kfr_filter_process_f32(KFR_FILTER_F32* plan, kfr_f32* output, const kfr_f32* input,
+                                         size_t size); /* capi.h:701 */
+KFR_API_SPEC void kfr_filter_process_f64(KFR_FILTER_F64* plan, kfr_f64* output, const kfr_f64* input,
+                                         size_t size); /* capi.h:711 */
+KFR_API_SPEC void kfr_filter_reset_f32(KFR_FILTER_F32* plan);       /* capi.h:718 */
+KFR_API_SPEC void kfr_filter_reset_f64(KFR_FILTER_F64* plan);       /* capi.h:724 */
+KFR_API_SPEC void kfr_filter_delete_plan_f32(KFR_FILTER_F32* plan); /* capi.h:730 */
+KFR_API_SPEC void kfr_filter_delete_plan_f64(KFR_FILTER_F64* plan); /* capi.h:736 */
+
+/* ======================================================================================================
+ * Extensions (no counterpart in the reference).
+ *
+ * Batched execution runs `batch` independent signals back to back in memory with one launch sequence:
+ * signal b of a complex plan starts at in + b*N; of a real plan at in + b*N (reals) and
+ * out + b*(N/2+1 or N/2) (complex); of a DCT plan at b*N.  `stream`: NULL runs synchronously (host or
+ * device pointers, like the single-signal calls); otherwise it is a cudaStream_t and the call only enqueues
+ * work on it, so all three pointers must be device memory and the caller synchronises.  temp: NULL or host
+ * uses plan-owned scratch (then calls on one plan must not overlap in time); a device pointer of
+ * *_get_temp_size_batch bytes is used instead.
+ * ====================================================================================================== */
+KFR_API_SPEC size_t kfr_dft_get_temp_size_batch_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
+KFR_API_SPEC size_t kfr_dft_get_temp_size_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch);
+KFR_API_SPEC void kfr_dft_execute_batch_f32(KFR_DFT_PLAN_F32* plan, size_t batch, kfr_c32* out, const kfr_c32* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream);
+KFR_API_SPEC void kfr_dft_execute_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch, kfr_c64* out, const kfr_c64* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream);
+
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch);
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch);
+KFR_API_SPEC void kfr_dft_real_execute_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_c32* out,
+                                                 const kfr_f32* in, uint8_t* temp, void* stream);
+KFR_API_SPEC void kfr_dft_real_execute_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_c64* out,
+                                                 const kfr_f64* in, uint8_t* temp, void* stream);
+KFR_API_SPEC void kfr_dft_real_execute_inverse_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_f32* out,
+                                                         const kfr_c32* in, uint8_t* temp, void* stream);
+KFR_API_SPEC void kfr_dft_real_execute_inverse_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_f64* out,
+                                                         const kfr_c64* in, uint8_t* temp, void* stream);
+
+KFR_API_SPEC size_t kfr_dct_get_temp_size_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch);
+KFR_API_SPEC size_t kfr_dct_get_temp_size_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch);
+KFR_API_SPEC void kfr_dct_execute_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch, kfr_f32* out, const kfr_f32* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream);
+KFR_API_SPEC void kfr_dct_execute_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch, kfr_f64* out, const kfr_f64* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream);
+
+/* Number of kernel launches one batched execute of this plan issues (forward direction). */
+KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KFR_GB300_CAPI_H */

@@ -1,0 +1,324 @@
+"""kfr_gb300: KFR's DFT hot path on one GB300 GPU, behind KFR's own C API.
+
+The product is the shared library kfr_gb300/lib/libkfr_capi.so (CUDA kernels for sm_103a plus the C ABI
+declared in include/kfr_capi.h).  This module is a thin ctypes mirror of the reference's plan objects, used
+by the tests and the benchmark and usable from Python directly:
+
+    dft_plan(n, "f32").execute(out, x)              # include/kfr/dft/fft.hpp:183-456
+    dft_plan_real(n, "CCs").execute(out, x)         # include/kfr/dft/fft.hpp:458-566
+    dct_plan(n).execute(out, x, inverse=False)      # include/kfr/dft/fft.hpp:926-978
+    convolve_filter(taps, block_size).apply(y, x)   # include/kfr/dft/convolution.hpp:98-148
+
+Buffers may be numpy arrays (host memory) or torch tensors / objects exposing data_ptr() (device or host).
+Errors reported by the library through kfr_last_error() are raised as KfrError.  There is no CPU fallback:
+if the library or a GPU is missing, calls fail.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libkfr_capi.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "kfr_capi.h")
+
+__all__ = ["KfrError", "lib", "dft_plan", "dft_plan_real", "dct_plan", "convolve_filter", "declared_symbols",
+           "CCs", "Perm"]
+
+CCs = 1
+Perm = 0
+
+
+class KfrError(RuntimeError):
+    pass
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_S = ctypes.c_size_t
+_B = ctypes.c_bool
+
+# name -> (restype, argtypes); every pointer is passed as an integer address
+_SIGS = {}
+for sfx in ("f32", "f64"):
+    _SIGS.update({
+        f"kfr_dft_create_plan_{sfx}": (_P, [_S]),
+        f"kfr_dft_create_2d_plan_{sfx}": (_P, [_S, _S]),
+        f"kfr_dft_create_3d_plan_{sfx}": (_P, [_S, _S, _S]),
+        f"kfr_dft_create_md_plan_{sfx}": (_P, [_S, _P]),
+        f"kfr_dft_dump_{sfx}": (None, [_P]),
+        f"kfr_dft_get_size_{sfx}": (_S, [_P]),
+        f"kfr_dft_get_temp_size_{sfx}": (_S, [_P]),
+        f"kfr_dft_get_temp_size_batch_{sfx}": (_S, [_P, _S]),
+        f"kfr_dft_execute_{sfx}": (None, [_P, _P, _P, _P]),
+        f"kfr_dft_execute_inverse_{sfx}": (None, [_P, _P, _P, _P]),
+        f"kfr_dft_execute_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _B, _P]),
+        f"kfr_dft_delete_plan_{sfx}": (None, [_P]),
+        f"kfr_dft_real_create_plan_{sfx}": (_P, [_S, ctypes.c_int]),
+        f"kfr_dft_real_create_2d_plan_{sfx}": (_P, [_S, _S, _B]),
+        f"kfr_dft_real_create_3d_plan_{sfx}": (_P, [_S, _S, _S, _B]),
+        f"kfr_dft_real_create_md_plan_{sfx}": (_P, [_S, _P, _B]),
+        f"kfr_dft_real_dump_{sfx}": (None, [_P]),
+        f"kfr_dft_real_get_size_{sfx}": (_S, [_P]),
+        f"kfr_dft_real_get_temp_size_{sfx}": (_S, [_P]),
+        f"kfr_dft_real_get_temp_size_batch_{sfx}": (_S, [_P, _S]),
+        f"kfr_dft_real_execute_{sfx}": (None, [_P, _P, _P, _P]),
+        f"kfr_dft_real_execute_inverse_{sfx}": (None, [_P, _P, _P, _P]),
+        f"kfr_dft_real_execute_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _P]),
+        f"kfr_dft_real_execute_inverse_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _P]),
+        f"kfr_dft_real_delete_plan_{sfx}": (None, [_P]),
+        f"kfr_dct_create_plan_{sfx}": (_P, [_S]),
+        f"kfr_dct_dump_{sfx}": (None, [_P]),
+        f"kfr_dct_get_size_{sfx}": (_S, [_P]),
+        f"kfr_dct_get_temp_size_{sfx}": (_S, [_P]),
+        f"kfr_dct_get_temp_size_batch_{sfx}": (_S, [_P, _S]),
+        f"kfr_dct_execute_{sfx}": (None, [_P, _P, _P, _P]),
+        f"kfr_dct_execute_inverse_{sfx}": (None, [_P, _P, _P, _P]),
+        f"kfr_dct_execute_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _B, _P]),
+        f"kfr_dct_delete_plan_{sfx}": (None, [_P]),
+        f"kfr_filter_create_fir_plan_{sfx}": (_P, [_P, _S]),
+        f"kfr_filter_create_iir_plan_{sfx}": (_P, [_P, _S]),
+        f"kfr_filter_create_convolution_plan_{sfx}": (_P, [_P, _S, _S]),
+        f"kfr_filter_process_{sfx}": (None, [_P, _P, _P, _S]),
+        f"kfr_filter_reset_{sfx}": (None, [_P]),
+        f"kfr_filter_delete_plan_{sfx}": (None, [_P]),
+    })
+_SIGS.update({
+    "kfr_version_string": (ctypes.c_char_p, []),
+    "kfr_version": (ctypes.c_uint32, []),
+    "kfr_enabled_archs": (ctypes.c_char_p, []),
+    "kfr_current_arch": (ctypes.c_int, []),
+    "kfr_last_error": (ctypes.c_char_p, []),
+    "kfr_allocate": (_P, [_S]),
+    "kfr_allocate_aligned": (_P, [_S, _S]),
+    "kfr_deallocate": (None, [_P]),
+    "kfr_dft_get_launch_count_f32": (_S, [_P, _S]),
+})
+
+
+def declared_symbols(header: str = HEADER) -> list[str]:
+    """Every function name declared in include/kfr_capi.h."""
+    text = open(header).read()
+    return sorted(set(re.findall(r"KFR_API_SPEC\s+[\w\s\*]+?\b(kfr_\w+)\s*\(", text)))
+
+
+def lib():
+    """The loaded C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise KfrError(f"{LIB_PATH} is missing: build it with `python -m kfr_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check():
+    msg = lib().kfr_last_error()
+    if msg:
+        raise KfrError(msg.decode())
+
+
+def _call(name, *args):
+    r = getattr(lib(), name)(*args)
+    _check()
+    return r
+
+
+def _addr(x):
+    """Address of a buffer: numpy array (host), torch tensor (host or device), int, or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("buffers must be contiguous")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if hasattr(x, "is_contiguous") and not x.is_contiguous():
+            raise ValueError("buffers must be contiguous")
+        return x.data_ptr()
+    raise TypeError(f"unsupported buffer type {type(x)}")
+
+
+def _sfx(dtype) -> str:
+    d = str(dtype)
+    if d in ("f32", "float32", "complex64", "<class 'numpy.float32'>", "<class 'numpy.complex64'>", "torch.float32",
+             "torch.complex64"):
+        return "f32"
+    if d in ("f64", "float64", "complex128", "<class 'numpy.float64'>", "<class 'numpy.complex128'>",
+             "torch.float64", "torch.complex128"):
+        return "f64"
+    raise ValueError(f"unsupported precision {dtype}")
+
+
+def _stream_addr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream) if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class _plan:
+    _prefix = ""
+
+    def __init__(self, handle, sfx):
+        if not handle:
+            _check()
+            raise KfrError("plan creation failed")
+        self.handle = handle
+        self.sfx = sfx
+
+    def _fn(self, op):
+        return f"{self._prefix}_{op}_{self.sfx}"
+
+    def close(self):
+        if getattr(self, "handle", None):
+            getattr(lib(), self._fn("delete_plan"))(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def dump(self):
+        _call(self._fn("dump"), self.handle)
+
+
+class dft_plan(_plan):
+    """Complex DFT of length `size` (dft_plan<T>, include/kfr/dft/fft.hpp:183-456); unscaled inverse."""
+
+    _prefix = "kfr_dft"
+
+    def __init__(self, size: int, dtype="f32"):
+        sfx = _sfx(dtype)
+        super().__init__(_call(f"kfr_dft_create_plan_{sfx}", size), sfx)
+
+    @property
+    def size(self):
+        return _call(self._fn("get_size"), self.handle)
+
+    @property
+    def temp_size(self):
+        return _call(self._fn("get_temp_size"), self.handle)
+
+    def temp_size_batch(self, batch):
+        return _call(self._fn("get_temp_size_batch"), self.handle, batch)
+
+    def execute(self, out, inp, temp=None, inverse=False):
+        op = "execute_inverse" if inverse else "execute"
+        _call(self._fn(op), self.handle, _addr(out), _addr(inp), _addr(temp))
+
+    def execute_batch(self, out, inp, batch, temp=None, inverse=False, stream=None):
+        _call(self._fn("execute_batch"), self.handle, batch, _addr(out), _addr(inp), _addr(temp), bool(inverse),
+              _stream_addr(stream))
+
+    def launch_count(self, batch=1):
+        return _call("kfr_dft_get_launch_count_f32", self.handle, batch) if self.sfx == "f32" else None
+
+
+class dft_plan_real(_plan):
+    """Real DFT of even length `size` (dft_plan_real<T>), CCs (N/2+1 bins) or Perm (N/2 bins) packing."""
+
+    _prefix = "kfr_dft_real"
+
+    def __init__(self, size: int, fmt="CCs", dtype="f32"):
+        sfx = _sfx(dtype)
+        self.fmt = CCs if fmt in ("CCs", CCs, "ccs") else Perm
+        self.n = size
+        super().__init__(_call(f"kfr_dft_real_create_plan_{sfx}", size, self.fmt), sfx)
+
+    @property
+    def complex_size(self):
+        return self.n // 2 + 1 if self.fmt == CCs else self.n // 2
+
+    @property
+    def size(self):
+        return _call(self._fn("get_size"), self.handle)
+
+    @property
+    def temp_size(self):
+        return _call(self._fn("get_temp_size"), self.handle)
+
+    def execute(self, out, inp, temp=None, inverse=False):
+        op = "execute_inverse" if inverse else "execute"
+        _call(self._fn(op), self.handle, _addr(out), _addr(inp), _addr(temp))
+
+    def execute_batch(self, out, inp, batch, temp=None, inverse=False, stream=None):
+        op = "execute_inverse_batch" if inverse else "execute_batch"
+        _call(self._fn(op), self.handle, batch, _addr(out), _addr(inp), _addr(temp), _stream_addr(stream))
+
+
+class dct_plan(_plan):
+    """DCT-II (forward) / DCT-III with X0 halved (inverse), unscaled (dct_plan<T>)."""
+
+    _prefix = "kfr_dct"
+
+    def __init__(self, size: int, dtype="f32"):
+        sfx = _sfx(dtype)
+        super().__init__(_call(f"kfr_dct_create_plan_{sfx}", size), sfx)
+
+    @property
+    def size(self):
+        return _call(self._fn("get_size"), self.handle)
+
+    @property
+    def temp_size(self):
+        return _call(self._fn("get_temp_size"), self.handle)
+
+    def execute(self, out, inp, temp=None, inverse=False):
+        op = "execute_inverse" if inverse else "execute"
+        _call(self._fn(op), self.handle, _addr(out), _addr(inp), _addr(temp))
+
+    def execute_batch(self, out, inp, batch, temp=None, inverse=False, stream=None):
+        _call(self._fn("execute_batch"), self.handle, batch, _addr(out), _addr(inp), _addr(temp), bool(inverse),
+              _stream_addr(stream))
+
+
+class convolve_filter(_plan):
+    """Streaming FFT convolution filter (convolve_filter<T>); state persists across apply() until reset()."""
+
+    _prefix = "kfr_filter"
+
+    def __init__(self, taps, block_size: int = 1024, dtype=None):
+        if dtype is None:
+            dtype = getattr(taps, "dtype", "f32")
+        sfx = _sfx(dtype)
+        if isinstance(taps, np.ndarray):
+            taps = np.ascontiguousarray(taps, dtype=np.float32 if sfx == "f32" else np.float64)
+        self._taps = taps
+        n = taps.numel() if hasattr(taps, "numel") else len(taps)
+        super().__init__(_call(f"kfr_filter_create_convolution_plan_{sfx}", _addr(taps), n, block_size), sfx)
+
+    def apply(self, out, inp, size=None):
+        if size is None:
+            size = inp.numel() if hasattr(inp, "numel") else len(inp)
+        _call(self._fn("process"), self.handle, _addr(out), _addr(inp), size)
+
+    def reset(self):
+        _call(self._fn("reset"), self.handle)
+
+
+def allocate(size: int, alignment: int = 64) -> int:
+    """kfr_allocate_aligned: host memory, pinned when a GPU is present."""
+    return _call("kfr_allocate_aligned", size, alignment)
+
+
+def deallocate(ptr: int) -> None:
+    _call("kfr_deallocate", ptr)
+
+
+def version_string() -> str:
+    return lib().kfr_version_string().decode()

@@ -1,0 +1,767 @@
+// extern "C" layer: the reference's C API (include/kfr/capi.h, implemented in src/capi/capi.cpp) over the GPU
+// engines.  Error convention of src/capi/capi.cpp:36-91: every entry point runs inside try_fn, which stores
+// the exception text in a thread-local 256-byte buffer and returns the fallback (NULL / 0).
+#include "kfr_capi.h"
+
+#include <algorithm>
+#include <array>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
+#include "conv.hpp"
+#include "plan.hpp"
+
+using namespace kfr_gpu;
+
+namespace
+{
+
+thread_local std::array<char, 256> g_last_error{};
+
+void reset_error() { g_last_error.fill(0); }
+
+void set_error(const char* s)
+{
+    const size_t n = std::min(std::strlen(s), g_last_error.size() - 1);
+    std::memcpy(g_last_error.data(), s, n);
+    std::fill(g_last_error.begin() + n, g_last_error.end(), 0);
+}
+
+template <typename Fn, typename R>
+R try_fn(Fn&& fn, R fallback)
+{
+    try
+    {
+        R r = fn();
+        reset_error();
+        return r;
+    }
+    catch (std::exception& e)
+    {
+        set_error(e.what());
+    }
+    catch (...)
+    {
+        set_error("(unknown exception)");
+    }
+    return fallback;
+}
+
+template <typename Fn>
+void try_void(Fn&& fn)
+{
+    try
+    {
+        fn();
+        reset_error();
+    }
+    catch (std::exception& e)
+    {
+        set_error(e.what());
+    }
+    catch (...)
+    {
+        set_error("(unknown exception)");
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Plan objects behind the opaque handles.  A tag word guards against NULL or mismatched handles.
+// ---------------------------------------------------------------------------------------------------
+
+enum : uint32_t
+{
+    TAG_DFT_F32  = 0x31465444u,
+    TAG_DFT_F64  = 0x32465444u,
+    TAG_REAL_F32 = 0x31455244u,
+    TAG_REAL_F64 = 0x32455244u,
+    TAG_DCT_F32  = 0x31544344u,
+    TAG_DCT_F64  = 0x32544344u,
+    TAG_FLT_F32  = 0x31544c46u,
+    TAG_FLT_F64  = 0x32544c46u,
+};
+
+struct plan_base
+{
+    uint32_t tag;
+    std::mutex mu;     // guards the plan-owned staging and scratch buffers
+    dbuf stage_in, stage_out, scratch;
+    explicit plan_base(uint32_t t) : tag(t) {}
+    virtual ~plan_base() { tag = 0; }
+};
+
+template <typename T>
+struct tags;
+template <>
+struct tags<float>
+{
+    static constexpr uint32_t dft = TAG_DFT_F32, real = TAG_REAL_F32, dct = TAG_DCT_F32, flt = TAG_FLT_F32;
+};
+template <>
+struct tags<double>
+{
+    static constexpr uint32_t dft = TAG_DFT_F64, real = TAG_REAL_F64, dct = TAG_DCT_F64, flt = TAG_FLT_F64;
+};
+
+template <typename T>
+struct dft_obj : plan_base
+{
+    size_t n;
+    complex_engine<T> eng;
+    explicit dft_obj(size_t n_) : plan_base(tags<T>::dft), n(n_), eng((long long)n_) {}
+};
+
+template <typename T>
+struct real_obj : plan_base
+{
+    size_t n;
+    bool ccs;
+    real_engine<T> eng;
+    real_obj(size_t n_, bool ccs_) : plan_base(tags<T>::real), n(n_), ccs(ccs_), eng(check_even(n_)) {}
+    static long long check_even(size_t n)
+    {
+        if (n % 2 != 0)
+            throw std::logic_error("dft_plan_real requires size to be even");
+        return (long long)n;
+    }
+    size_t clen() const { return ccs ? n / 2 + 1 : n / 2; }
+};
+
+template <typename T>
+struct dct_obj : plan_base
+{
+    size_t n;
+    dct_engine<T> eng;
+    explicit dct_obj(size_t n_) : plan_base(tags<T>::dct), n(n_), eng((long long)n_) {}
+};
+
+template <typename T>
+struct filter_obj : plan_base
+{
+    conv_filter<T> f;
+    filter_obj(const T* taps, size_t ntaps, size_t block) : plan_base(tags<T>::flt), f(taps, ntaps, block) {}
+};
+
+template <typename Obj>
+Obj* as(void* h, uint32_t tag)
+{
+    if (!h)
+        throw std::invalid_argument("plan is NULL");
+    plan_base* b = static_cast<plan_base*>(h);
+    if (b->tag != tag)
+        throw std::invalid_argument("invalid or mismatched plan handle");
+    return static_cast<Obj*>(b);
+}
+
+bool is_device_ptr(const void* p)
+{
+    if (!p)
+        return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+bool overlap(const void* a, size_t an, const void* b, size_t bn)
+{
+    const char* x = static_cast<const char*>(a);
+    const char* y = static_cast<const char*>(b);
+    return x < y + bn && y < x + an;
+}
+
+// Runs `fn(dout, din, scratch, stream)` with host buffers staged through plan-owned device memory.
+// stream == nullptr: synchronous on the legacy default stream, host or device pointers.
+// stream != nullptr: enqueued only; in/out must be device pointers.
+template <typename Fn>
+void run(plan_base& pl, void* out, size_t out_bytes, const void* in, size_t in_bytes, uint8_t* temp,
+         size_t scratch_bytes, void* stream, bool copy_aliased_input, Fn&& fn)
+{
+    if ((!out && out_bytes) || (!in && in_bytes))
+        throw std::invalid_argument("NULL data pointer");
+    const bool in_dev  = is_device_ptr(in);
+    const bool out_dev = is_device_ptr(out);
+    cudaStream_t st    = static_cast<cudaStream_t>(stream);
+    if (stream && (!in_dev || !out_dev))
+        throw std::invalid_argument("stream-ordered execution needs device pointers for in and out");
+    std::unique_lock<std::mutex> lock(pl.mu);
+    const void* din = in;
+    void* dout      = out;
+    if (!in_dev)
+    {
+        pl.stage_in.ensure(in_bytes);
+        check(cudaMemcpyAsync(pl.stage_in.get(), in, in_bytes, cudaMemcpyHostToDevice, st), "copy input to device");
+        din = pl.stage_in.get();
+    }
+    else if (copy_aliased_input && out_dev && overlap(in, in_bytes, out, out_bytes))
+    {
+        pl.stage_in.ensure(in_bytes);
+        check(cudaMemcpyAsync(pl.stage_in.get(), in, in_bytes, cudaMemcpyDeviceToDevice, st), "copy aliased input");
+        din = pl.stage_in.get();
+    }
+    if (!out_dev)
+    {
+        pl.stage_out.ensure(out_bytes);
+        dout = pl.stage_out.get();
+    }
+    void* scr = nullptr;
+    if (scratch_bytes)
+    {
+        if (temp && is_device_ptr(temp))
+            scr = temp;
+        else
+        {
+            pl.scratch.ensure(scratch_bytes);
+            scr = pl.scratch.get();
+        }
+    }
+    fn(dout, din, scr, st);
+    check(cudaGetLastError(), "kernel launch");
+    if (!out_dev)
+        check(cudaMemcpyAsync(out, dout, out_bytes, cudaMemcpyDeviceToHost, st), "copy result to host");
+    if (!stream)
+        check(cudaStreamSynchronize(st), "execute");
+}
+
+template <typename T>
+void* create_dft(size_t n)
+{
+    return static_cast<plan_base*>(new dft_obj<T>(n));
+}
+
+template <typename T>
+void exec_dft(void* h, size_t batch, void* out, const void* in, uint8_t* temp, bool inverse, void* stream)
+{
+    auto* p = as<dft_obj<T>>(h, tags<T>::dft);
+    if (batch == 0 || p->n == 0)
+        return;
+    const size_t bytes = batch * p->n * 2 * sizeof(T);
+    const size_t scr   = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(T);
+    run(*p, out, bytes, in, bytes, temp, scr, stream, false,
+        [&](void* o, const void* i, void* s, cudaStream_t st)
+        { p->eng.execute(o, i, (long long)batch, (long long)p->n, (long long)p->n, inverse, s, st); });
+}
+
+template <typename T>
+void exec_real(void* h, size_t batch, void* out, const void* in, uint8_t* temp, bool inverse, void* stream)
+{
+    auto* p = as<real_obj<T>>(h, tags<T>::real);
+    if (batch == 0)
+        return;
+    const size_t rbytes = batch * p->n * sizeof(T);
+    const size_t cbytes = batch * p->clen() * 2 * sizeof(T);
+    const size_t scr    = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(T);
+    if (!inverse)
+        run(*p, out, cbytes, in, rbytes, temp, scr, stream, batch > 1,
+            [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.forward(o, i, (long long)batch, p->ccs, s, st); });
+    else
+        run(*p, out, rbytes, in, cbytes, temp, scr, stream, batch > 1,
+            [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.inverse(o, i, (long long)batch, p->ccs, s, st); });
+}
+
+template <typename T>
+void exec_dct(void* h, size_t batch, void* out, const void* in, uint8_t* temp, bool inverse, void* stream)
+{
+    auto* p = as<dct_obj<T>>(h, tags<T>::dct);
+    if (batch == 0 || p->n == 0)
+        return;
+    const size_t bytes = batch * p->n * sizeof(T);
+    const size_t scr   = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(T);
+    run(*p, out, bytes, in, bytes, temp, scr, stream, false,
+        [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.execute(o, i, (long long)batch, inverse, s, st); });
+}
+
+template <typename T>
+void filter_process(void* h, T* out, const T* in, size_t n)
+{
+    auto* p = as<filter_obj<T>>(h, tags<T>::flt);
+    if (n == 0)
+        return;
+    const size_t bytes = n * sizeof(T);
+    run(*p, out, bytes, in, bytes, nullptr, 0, nullptr, true,
+        [&](void* o, const void* i, void*, cudaStream_t st)
+        { p->f.process(static_cast<T*>(o), static_cast<const T*>(i), n, st); });
+}
+
+void print_line(const std::string& s)
+{
+    std::printf("%s\n", s.c_str());
+    std::fflush(stdout);
+}
+
+std::string& version_string()
+{
+    static std::string s = [] {
+        int rt = 0;
+        cudaRuntimeGetVersion(&rt);
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "KFR 7.0.1 gb300 sm_103a 64-bit (CUDA runtime %d.%d)", rt / 1000,
+                      (rt % 1000) / 10);
+        return std::string(buf);
+    }();
+    return s;
+}
+
+// Host allocations carry a small header: the pointer returned by malloc and whether the block is pinned.
+struct alloc_header
+{
+    void* base;
+    size_t size;
+    int pinned;
+    int magic;
+};
+constexpr int kAllocMagic = 0x6b667241;
+
+void* host_alloc(size_t size, size_t alignment)
+{
+    if (alignment < alignof(alloc_header) || (alignment & (alignment - 1)))
+        throw std::invalid_argument("alignment must be a power of two");
+    const size_t total = size + alignment + sizeof(alloc_header);
+    void* base         = std::malloc(total);
+    if (!base)
+        throw std::bad_alloc();
+    uintptr_t p = (reinterpret_cast<uintptr_t>(base) + sizeof(alloc_header) + alignment - 1) & ~(uintptr_t(alignment) - 1);
+    alloc_header* h = reinterpret_cast<alloc_header*>(p) - 1;
+    h->base         = base;
+    h->size         = size;
+    h->magic        = kAllocMagic;
+    h->pinned       = 0;
+    int ndev        = 0;
+    if (size >= 4096 && cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0)
+    {
+        if (cudaHostRegister(reinterpret_cast<void*>(p), size, cudaHostRegisterDefault) == cudaSuccess)
+            h->pinned = 1;
+        else
+            cudaGetLastError();
+    }
+    else
+        cudaGetLastError();
+    return reinterpret_cast<void*>(p);
+}
+
+void host_free(void* p)
+{
+    if (!p)
+        return;
+    alloc_header* h = reinterpret_cast<alloc_header*>(p) - 1;
+    if (h->magic != kAllocMagic)
+        throw std::invalid_argument("pointer was not allocated by kfr_allocate");
+    if (h->pinned)
+    {
+        cudaHostUnregister(p);
+        cudaGetLastError();
+    }
+    h->magic = 0;
+    std::free(h->base);
+}
+
+[[noreturn]] void not_built(const char* what)
+{
+    throw std::logic_error(std::string(what) + " is not part of the GPU DFT path in this build");
+}
+
+} // namespace
+
+extern "C"
+{
+
+// ---- information ---------------------------------------------------------------------------------
+KFR_API_SPEC const char* kfr_version_string(void) { return version_string().c_str(); }
+KFR_API_SPEC uint32_t kfr_version(void) { return 70001; }
+KFR_API_SPEC const char* kfr_enabled_archs(void) { return "sm_103a"; }
+KFR_API_SPEC int kfr_current_arch(void)
+{
+    return try_fn(
+        []
+        {
+            int dev = 0, ma = 0, mi = 0;
+            check(cudaGetDevice(&dev), "cudaGetDevice");
+            check(cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, dev), "attribute");
+            check(cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, dev), "attribute");
+            return ma * 10 + mi;
+        },
+        -1);
+}
+KFR_API_SPEC const char* kfr_last_error(void) { return g_last_error.data(); }
+
+KFR_API_SPEC void* kfr_allocate(size_t size)
+{
+    return try_fn([&] { return host_alloc(size, KFR_DEFAULT_ALIGNMENT); }, (void*)nullptr);
+}
+KFR_API_SPEC void* kfr_allocate_aligned(size_t size, size_t alignment)
+{
+    return try_fn([&] { return host_alloc(size, alignment); }, (void*)nullptr);
+}
+KFR_API_SPEC void kfr_deallocate(void* ptr)
+{
+    try_void([&] { host_free(ptr); });
+}
+
+// ---- complex DFT ---------------------------------------------------------------------------------
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_plan_f32(size_t size)
+{
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F32*>(create_dft<float>(size)); },
+                  (KFR_DFT_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_plan_f64(size_t size)
+{
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F64*>(create_dft<double>(size)); },
+                  (KFR_DFT_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_2d_plan_f32(size_t, size_t)
+{
+    return try_fn([]() -> KFR_DFT_PLAN_F32* { not_built("kfr_dft_create_2d_plan_f32"); }, (KFR_DFT_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_3d_plan_f32(size_t, size_t, size_t)
+{
+    return try_fn([]() -> KFR_DFT_PLAN_F32* { not_built("kfr_dft_create_3d_plan_f32"); }, (KFR_DFT_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_md_plan_f32(size_t, const unsigned*)
+{
+    return try_fn([]() -> KFR_DFT_PLAN_F32* { not_built("kfr_dft_create_md_plan_f32"); }, (KFR_DFT_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_2d_plan_f64(size_t, size_t)
+{
+    return try_fn([]() -> KFR_DFT_PLAN_F64* { not_built("kfr_dft_create_2d_plan_f64"); }, (KFR_DFT_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_3d_plan_f64(size_t, size_t, size_t)
+{
+    return try_fn([]() -> KFR_DFT_PLAN_F64* { not_built("kfr_dft_create_3d_plan_f64"); }, (KFR_DFT_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_md_plan_f64(size_t, const unsigned*)
+{
+    return try_fn([]() -> KFR_DFT_PLAN_F64* { not_built("kfr_dft_create_md_plan_f64"); }, (KFR_DFT_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC void kfr_dft_dump_f32(KFR_DFT_PLAN_F32* plan)
+{
+    try_void([&] { print_line(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.describe()); });
+}
+KFR_API_SPEC void kfr_dft_dump_f64(KFR_DFT_PLAN_F64* plan)
+{
+    try_void([&] { print_line(as<dft_obj<double>>(plan, TAG_DFT_F64)->eng.describe()); });
+}
+KFR_API_SPEC size_t kfr_dft_get_size_f32(KFR_DFT_PLAN_F32* plan)
+{
+    return try_fn([&] { return as<dft_obj<float>>(plan, TAG_DFT_F32)->n; }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_get_size_f64(KFR_DFT_PLAN_F64* plan)
+{
+    return try_fn([&] { return as<dft_obj<double>>(plan, TAG_DFT_F64)->n; }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_get_temp_size_batch_f32(KFR_DFT_PLAN_F32* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.scratch_elems(batch)) * 8; },
+                  size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_get_temp_size_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<dft_obj<double>>(plan, TAG_DFT_F64)->eng.scratch_elems(batch)) * 16; },
+                  size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_get_temp_size_f32(KFR_DFT_PLAN_F32* plan) { return kfr_dft_get_temp_size_batch_f32(plan, 1); }
+KFR_API_SPEC size_t kfr_dft_get_temp_size_f64(KFR_DFT_PLAN_F64* plan) { return kfr_dft_get_temp_size_batch_f64(plan, 1); }
+KFR_API_SPEC void kfr_dft_execute_f32(KFR_DFT_PLAN_F32* plan, kfr_c32* out, const kfr_c32* in, uint8_t* temp)
+{
+    try_void([&] { exec_dft<float>(plan, 1, out, in, temp, false, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_execute_f64(KFR_DFT_PLAN_F64* plan, kfr_c64* out, const kfr_c64* in, uint8_t* temp)
+{
+    try_void([&] { exec_dft<double>(plan, 1, out, in, temp, false, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_execute_inverse_f32(KFR_DFT_PLAN_F32* plan, kfr_c32* out, const kfr_c32* in, uint8_t* temp)
+{
+    try_void([&] { exec_dft<float>(plan, 1, out, in, temp, true, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_execute_inverse_f64(KFR_DFT_PLAN_F64* plan, kfr_c64* out, const kfr_c64* in, uint8_t* temp)
+{
+    try_void([&] { exec_dft<double>(plan, 1, out, in, temp, true, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_execute_batch_f32(KFR_DFT_PLAN_F32* plan, size_t batch, kfr_c32* out, const kfr_c32* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    try_void([&] { exec_dft<float>(plan, batch, out, in, temp, inverse, stream); });
+}
+KFR_API_SPEC void kfr_dft_execute_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch, kfr_c64* out, const kfr_c64* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    try_void([&] { exec_dft<double>(plan, batch, out, in, temp, inverse, stream); });
+}
+KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.launches(batch)); }, size_t(0));
+}
+KFR_API_SPEC void kfr_dft_delete_plan_f32(KFR_DFT_PLAN_F32* plan)
+{
+    try_void([&] { if (plan) delete as<dft_obj<float>>(plan, TAG_DFT_F32); });
+}
+KFR_API_SPEC void kfr_dft_delete_plan_f64(KFR_DFT_PLAN_F64* plan)
+{
+    try_void([&] { if (plan) delete as<dft_obj<double>>(plan, TAG_DFT_F64); });
+}
+
+// ---- real DFT ------------------------------------------------------------------------------------
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_plan_f32(size_t size, KFR_DFT_PACK_FORMAT fmt)
+{
+    return try_fn(
+        [&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F32*>(static_cast<plan_base*>(new real_obj<float>(size, fmt == CCs))); },
+        (KFR_DFT_REAL_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_plan_f64(size_t size, KFR_DFT_PACK_FORMAT fmt)
+{
+    return try_fn(
+        [&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F64*>(static_cast<plan_base*>(new real_obj<double>(size, fmt == CCs))); },
+        (KFR_DFT_REAL_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_2d_plan_f32(size_t, size_t, kfr_bool)
+{
+    return try_fn([]() -> KFR_DFT_REAL_PLAN_F32* { not_built("kfr_dft_real_create_2d_plan_f32"); },
+                  (KFR_DFT_REAL_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_3d_plan_f32(size_t, size_t, size_t, kfr_bool)
+{
+    return try_fn([]() -> KFR_DFT_REAL_PLAN_F32* { not_built("kfr_dft_real_create_3d_plan_f32"); },
+                  (KFR_DFT_REAL_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_md_plan_f32(size_t, const unsigned*, kfr_bool)
+{
+    return try_fn([]() -> KFR_DFT_REAL_PLAN_F32* { not_built("kfr_dft_real_create_md_plan_f32"); },
+                  (KFR_DFT_REAL_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_2d_plan_f64(size_t, size_t, kfr_bool)
+{
+    return try_fn([]() -> KFR_DFT_REAL_PLAN_F64* { not_built("kfr_dft_real_create_2d_plan_f64"); },
+                  (KFR_DFT_REAL_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_3d_plan_f64(size_t, size_t, size_t, kfr_bool)
+{
+    return try_fn([]() -> KFR_DFT_REAL_PLAN_F64* { not_built("kfr_dft_real_create_3d_plan_f64"); },
+                  (KFR_DFT_REAL_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_md_plan_f64(size_t, const unsigned*, kfr_bool)
+{
+    return try_fn([]() -> KFR_DFT_REAL_PLAN_F64* { not_built("kfr_dft_real_create_md_plan_f64"); },
+                  (KFR_DFT_REAL_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC void kfr_dft_real_dump_f32(KFR_DFT_REAL_PLAN_F32* plan)
+{
+    try_void([&] { print_line(as<real_obj<float>>(plan, TAG_REAL_F32)->eng.describe()); });
+}
+KFR_API_SPEC void kfr_dft_real_dump_f64(KFR_DFT_REAL_PLAN_F64* plan)
+{
+    try_void([&] { print_line(as<real_obj<double>>(plan, TAG_REAL_F64)->eng.describe()); });
+}
+KFR_API_SPEC size_t kfr_dft_real_get_size_f32(KFR_DFT_REAL_PLAN_F32* plan)
+{
+    return try_fn([&] { return as<real_obj<float>>(plan, TAG_REAL_F32)->n; }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_real_get_size_f64(KFR_DFT_REAL_PLAN_F64* plan)
+{
+    return try_fn([&] { return as<real_obj<double>>(plan, TAG_REAL_F64)->n; }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<real_obj<float>>(plan, TAG_REAL_F32)->eng.scratch_elems(batch)) * 8; },
+                  size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<real_obj<double>>(plan, TAG_REAL_F64)->eng.scratch_elems(batch)) * 16; },
+                  size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_f32(KFR_DFT_REAL_PLAN_F32* plan)
+{
+    return kfr_dft_real_get_temp_size_batch_f32(plan, 1);
+}
+KFR_API_SPEC size_t kfr_dft_real_get_temp_size_f64(KFR_DFT_REAL_PLAN_F64* plan)
+{
+    return kfr_dft_real_get_temp_size_batch_f64(plan, 1);
+}
+KFR_API_SPEC void kfr_dft_real_execute_f32(KFR_DFT_REAL_PLAN_F32* plan, kfr_c32* out, const kfr_f32* in, uint8_t* temp)
+{
+    try_void([&] { exec_real<float>(plan, 1, out, in, temp, false, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_real_execute_f64(KFR_DFT_REAL_PLAN_F64* plan, kfr_c64* out, const kfr_f64* in, uint8_t* temp)
+{
+    try_void([&] { exec_real<double>(plan, 1, out, in, temp, false, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_real_execute_inverse_f32(KFR_DFT_REAL_PLAN_F32* plan, kfr_f32* out, const kfr_c32* in,
+                                                   uint8_t* temp)
+{
+    try_void([&] { exec_real<float>(plan, 1, out, in, temp, true, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_real_execute_inverse_f64(KFR_DFT_REAL_PLAN_F64* plan, kfr_f64* out, const kfr_c64* in,
+                                                   uint8_t* temp)
+{
+    try_void([&] { exec_real<double>(plan, 1, out, in, temp, true, nullptr); });
+}
+KFR_API_SPEC void kfr_dft_real_execute_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_c32* out,
+                                                 const kfr_f32* in, uint8_t* temp, void* stream)
+{
+    try_void([&] { exec_real<float>(plan, batch, out, in, temp, false, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_execute_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_c64* out,
+                                                 const kfr_f64* in, uint8_t* temp, void* stream)
+{
+    try_void([&] { exec_real<double>(plan, batch, out, in, temp, false, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_execute_inverse_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_f32* out,
+                                                         const kfr_c32* in, uint8_t* temp, void* stream)
+{
+    try_void([&] { exec_real<float>(plan, batch, out, in, temp, true, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_execute_inverse_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_f64* out,
+                                                         const kfr_c64* in, uint8_t* temp, void* stream)
+{
+    try_void([&] { exec_real<double>(plan, batch, out, in, temp, true, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_delete_plan_f32(KFR_DFT_REAL_PLAN_F32* plan)
+{
+    try_void([&] { if (plan) delete as<real_obj<float>>(plan, TAG_REAL_F32); });
+}
+KFR_API_SPEC void kfr_dft_real_delete_plan_f64(KFR_DFT_REAL_PLAN_F64* plan)
+{
+    try_void([&] { if (plan) delete as<real_obj<double>>(plan, TAG_REAL_F64); });
+}
+
+// ---- DCT -----------------------------------------------------------------------------------------------
+KFR_API_SPEC KFR_DCT_PLAN_F32* kfr_dct_create_plan_f32(size_t size)
+{
+    return try_fn([&] { return reinterpret_cast<KFR_DCT_PLAN_F32*>(static_cast<plan_base*>(new dct_obj<float>(size))); },
+                  (KFR_DCT_PLAN_F32*)nullptr);
+}
+KFR_API_SPEC KFR_DCT_PLAN_F64* kfr_dct_create_plan_f64(size_t size)
+{
+    return try_fn([&] { return reinterpret_cast<KFR_DCT_PLAN_F64*>(static_cast<plan_base*>(new dct_obj<double>(size))); },
+                  (KFR_DCT_PLAN_F64*)nullptr);
+}
+KFR_API_SPEC void kfr_dct_dump_f32(KFR_DCT_PLAN_F32* plan)
+{
+    try_void([&] { print_line(as<dct_obj<float>>(plan, TAG_DCT_F32)->eng.describe()); });
+}
+KFR_API_SPEC void kfr_dct_dump_f64(KFR_DCT_PLAN_F64* plan)
+{
+    try_void([&] { print_line(as<dct_obj<double>>(plan, TAG_DCT_F64)->eng.describe()); });
+}
+KFR_API_SPEC size_t kfr_dct_get_size_f32(KFR_DCT_PLAN_F32* plan)
+{
+    return try_fn([&] { return as<dct_obj<float>>(plan, TAG_DCT_F32)->n; }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dct_get_size_f64(KFR_DCT_PLAN_F64* plan)
+{
+    return try_fn([&] { return as<dct_obj<double>>(plan, TAG_DCT_F64)->n; }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dct_get_temp_size_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<dct_obj<float>>(plan, TAG_DCT_F32)->eng.scratch_elems(batch)) * 8; },
+                  size_t(0));
+}
+KFR_API_SPEC size_t kfr_dct_get_temp_size_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<dct_obj<double>>(plan, TAG_DCT_F64)->eng.scratch_elems(batch)) * 16; },
+                  size_t(0));
+}
+KFR_API_SPEC size_t kfr_dct_get_temp_size_f32(KFR_DCT_PLAN_F32* plan) { return kfr_dct_get_temp_size_batch_f32(plan, 1); }
+KFR_API_SPEC size_t kfr_dct_get_temp_size_f64(KFR_DCT_PLAN_F64* plan) { return kfr_dct_get_temp_size_batch_f64(plan, 1); }
+KFR_API_SPEC void kfr_dct_execute_f32(KFR_DCT_PLAN_F32* plan, kfr_f32* out, const kfr_f32* in, uint8_t* temp)
+{
+    try_void([&] { exec_dct<float>(plan, 1, out, in, temp, false, nullptr); });
+}
+KFR_API_SPEC void kfr_dct_execute_f64(KFR_DCT_PLAN_F64* plan, kfr_f64* out, const kfr_f64* in, uint8_t* temp)
+{
+    try_void([&] { exec_dct<double>(plan, 1, out, in, temp, false, nullptr); });
+}
+KFR_API_SPEC void kfr_dct_execute_inverse_f32(KFR_DCT_PLAN_F32* plan, kfr_f32* out, const kfr_f32* in, uint8_t* temp)
+{
+    try_void([&] { exec_dct<float>(plan, 1, out, in, temp, true, nullptr); });
+}
+KFR_API_SPEC void kfr_dct_execute_inverse_f64(KFR_DCT_PLAN_F64* plan, kfr_f64* out, const kfr_f64* in, uint8_t* temp)
+{
+    try_void([&] { exec_dct<double>(plan, 1, out, in, temp, true, nullptr); });
+}
+KFR_API_SPEC void kfr_dct_execute_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch, kfr_f32* out, const kfr_f32* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    try_void([&] { exec_dct<float>(plan, batch, out, in, temp, inverse, stream); });
+}
+KFR_API_SPEC void kfr_dct_execute_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch, kfr_f64* out, const kfr_f64* in,
+                                            uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    try_void([&] { exec_dct<double>(plan, batch, out, in, temp, inverse, stream); });
+}
+KFR_API_SPEC void kfr_dct_delete_plan_f32(KFR_DCT_PLAN_F32* plan)
+{
+    try_void([&] { if (plan) delete as<dct_obj<float>>(plan, TAG_DCT_F32); });
+}
+KFR_API_SPEC void kfr_dct_delete_plan_f64(KFR_DCT_PLAN_F64* plan)
+{
+    try_void([&] { if (plan) delete as<dct_obj<double>>(plan, TAG_DCT_F64); });
+}
+
+// ---- filters -------------------------------------------------------------------------------------------
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_fir_plan_f32(const kfr_f32*, size_t)
+{
+    return try_fn([]() -> KFR_FILTER_F32* { not_built("kfr_filter_create_fir_plan_f32"); }, (KFR_FILTER_F32*)nullptr);
+}
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_fir_plan_f64(const kfr_f64*, size_t)
+{
+    return try_fn([]() -> KFR_FILTER_F64* { not_built("kfr_filter_create_fir_plan_f64"); }, (KFR_FILTER_F64*)nullptr);
+}
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_iir_plan_f32(const kfr_f32*, size_t)
+{
+    return try_fn([]() -> KFR_FILTER_F32* { not_built("kfr_filter_create_iir_plan_f32"); }, (KFR_FILTER_F32*)nullptr);
+}
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_iir_plan_f64(const kfr_f64*, size_t)
+{
+    return try_fn([]() -> KFR_FILTER_F64* { not_built("kfr_filter_create_iir_plan_f64"); }, (KFR_FILTER_F64*)nullptr);
+}
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_convolution_plan_f32(const kfr_f32* taps, size_t size, size_t block_size)
+{
+    return try_fn(
+        [&] {
+            return reinterpret_cast<KFR_FILTER_F32*>(
+                static_cast<plan_base*>(new filter_obj<float>(taps, size, block_size ? block_size : 1024)));
+        },
+        (KFR_FILTER_F32*)nullptr);
+}
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_convolution_plan_f64(const kfr_f64* taps, size_t size, size_t block_size)
+{
+    return try_fn(
+        [&] {
+            return reinterpret_cast<KFR_FILTER_F64*>(
+                static_cast<plan_base*>(new filter_obj<double>(taps, size, block_size ? block_size : 1024)));
+        },
+        (KFR_FILTER_F64*)nullptr);
+}
+KFR_API_SPEC void kfr_filter_process_f32(KFR_FILTER_F32* plan, kfr_f32* output, const kfr_f32* input, size_t size)
+{
+    try_void([&] { filter_process<float>(plan, output, input, size); });
+}
+KFR_API_SPEC void kfr_filter_process_f64(KFR_FILTER_F64* plan, kfr_f64* output, const kfr_f64* input, size_t size)
+{
+    try_void([&] { filter_process<double>(plan, output, input, size); });
+}
+KFR_API_SPEC void kfr_filter_reset_f32(KFR_FILTER_F32* plan)
+{
+    try_void([&] { as<filter_obj<float>>(plan, TAG_FLT_F32)->f.reset(); });
+}
+KFR_API_SPEC void kfr_filter_reset_f64(KFR_FILTER_F64* plan)
+{
+    try_void([&] { as<filter_obj<double>>(plan, TAG_FLT_F64)->f.reset(); });
+}
+KFR_API_SPEC void kfr_filter_delete_plan_f32(KFR_FILTER_F32* plan)
+{
+    try_void([&] { if (plan) delete as<filter_obj<float>>(plan, TAG_FLT_F32); });
+}
+KFR_API_SPEC void kfr_filter_delete_plan_f64(KFR_FILTER_F64* plan)
+{
+    try_void([&] { if (plan) delete as<filter_obj<double>>(plan, TAG_FLT_F64); });
+}
+
+} // extern "C"

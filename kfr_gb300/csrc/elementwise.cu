@@ -1,0 +1,135 @@
+// Elementwise kernels of the multi-kernel paths (see launch.hpp: ew_op).
+#include "fft_device.cuh"
+#include "launch.hpp"
+
+namespace kfr_gpu
+{
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_elementwise(const int op, const ew_args a)
+{
+    const long long total = a.batch * a.n;
+    const cpx<T>* in      = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* out           = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* t0      = reinterpret_cast<const cpx<T>*>(a.t0);
+    const T* inr          = reinterpret_cast<const T*>(a.in);
+    T* outr               = reinterpret_cast<T*>(a.out);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x)
+    {
+        const long long s = i / a.n;
+        const long long e = i - s * a.n;
+        switch (op)
+        {
+        case EW_BS_PRE:
+        {
+            cpx<T> v = mk<T>(0, 0);
+            if (e < a.n_src)
+                v = conj_if(in[s * a.istride + e], a.flag != 0) * ldg(t0 + e);
+            out[s * a.ostride + e] = v;
+            break;
+        }
+        case EW_BS_MID:
+            out[s * a.ostride + e] = conj(in[s * a.istride + e] * ldg(t0 + e));
+            break;
+        case EW_BS_POST:
+            out[s * a.ostride + e] = conj_if(conj(in[s * a.istride + e]) * ldg(t0 + e), a.flag != 0);
+            break;
+        case EW_R2C:
+        {
+            const long long c = a.n_src;
+            const cpx<T>* z   = in + s * a.istride;
+            cpx<T> v;
+            if (e == 0)
+            {
+                const cpx<T> z0 = z[0];
+                v = a.flag ? mk<T>(z0.x + z0.y, 0) : mk<T>(z0.x + z0.y, z0.x - z0.y);
+            }
+            else if (e == c)
+            {
+                const cpx<T> z0 = z[0];
+                v               = mk<T>(z0.x - z0.y, 0);
+            }
+            else
+            {
+                const cpx<T> zk  = z[e];
+                const cpx<T> znk = conj(z[c - e]);
+                v = scale(zk + znk, T(0.5)) + ldg(t0 + e) * scale(mul_mi(zk - znk), T(0.5));
+            }
+            out[s * a.ostride + e] = v;
+            break;
+        }
+        case EW_C2R:
+        {
+            const long long c = a.n_src;
+            const cpx<T>* X   = in + s * a.istride;
+            cpx<T> z;
+            if (e == 0)
+            {
+                const T x0 = X[0].x;
+                const T xn = a.flag ? X[c].x : X[0].y;
+                z          = mk<T>(x0 + xn, x0 - xn);
+            }
+            else
+            {
+                const cpx<T> xk  = X[e];
+                const cpx<T> xnk = conj(X[c - e]);
+                z                = (xk + xnk) + mul_pi(conj(ldg(t0 + e)) * (xk - xnk));
+            }
+            out[s * a.ostride + e] = z;
+            break;
+        }
+        case EW_DCT2_PRE:
+        {
+            // e is the source index; write its mirrored position
+            const long long n   = a.n;
+            const long long pos = (e & 1) ? n - 1 - (e >> 1) : (e >> 1);
+            out[s * a.ostride + pos] = mk<T>(inr[s * a.istride + e], T(0));
+            break;
+        }
+        case EW_DCT2_POST:
+        {
+            const cpx<T> y = in[s * a.istride + e];
+            const cpx<T> w = ldg(t0 + e);
+            outr[s * a.ostride + e] = y.x * w.x + y.y * w.y;
+            break;
+        }
+        case EW_DCT3_PRE:
+        {
+            const T x      = inr[s * a.istride + e];
+            const cpx<T> w = ldg(t0 + e);
+            cpx<T> v       = mk<T>(x * w.x, -(x * w.y));
+            if (e == 0)
+                v = scale(v, T(0.5));
+            out[s * a.ostride + e] = v;
+            break;
+        }
+        case EW_DCT3_POST:
+        {
+            const long long n   = a.n;
+            const long long pos = (e & 1) ? n - 1 - (e >> 1) : (e >> 1);
+            outr[s * a.ostride + e] = in[s * a.istride + pos].x;
+            break;
+        }
+        default: break;
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st)
+{
+    const long long total = a.batch * a.n;
+    if (total <= 0)
+        return cudaSuccess;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152LL * 32)
+        blocks = 152LL * 32;
+    k_elementwise<T><<<unsigned(blocks), 256, 0, st>>>(op, a);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_elementwise<float>(int, const ew_args&, cudaStream_t);
+template cudaError_t launch_elementwise<double>(int, const ew_args&, cudaStream_t);
+
+} // namespace kfr_gpu

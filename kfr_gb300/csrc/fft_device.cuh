@@ -1,0 +1,497 @@
+// Device building blocks of the GB300 DFT engine: complex arithmetic, radix-R DFT codelets held in
+// registers, and the shared-memory block FFT that every transform kernel runs.
+//
+// The block FFT is a self-sorting (Stockham) mixed-radix sweep.  Pass p with radix R and
+// Ns = R_0 * ... * R_{p-1} turns butterfly j (0 <= j < N/R) into
+//     v[r] = buf[j + r*N/R] * W_{Ns*R}^{(j mod Ns)*r},   V = DFT_R(v),
+//     buf[(j - j mod Ns)*R + j mod Ns + r*Ns] = V[r],
+// so the result comes out in natural order with no digit-reverse pass.  This replaces the reference's
+// in-place stages plus reorder stage (src/dft/dft-impl.hpp:85-150, 368-494) and its radix-4 DIF passes plus
+// bit reversal (src/dft/fft-impl.hpp:846-1001).  Each pass reads all of its butterflies into registers,
+// synchronises, and writes them back, so a signal needs only N (+1/16 padding) slots of shared memory.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fft_desc.hpp"
+
+namespace kfr_gpu
+{
+
+template <typename T>
+struct alignas(2 * sizeof(T)) cpx
+{
+    T x, y;
+};
+
+template <typename T>
+__device__ __forceinline__ cpx<T> mk(T x, T y)
+{
+    cpx<T> r;
+    r.x = x;
+    r.y = y;
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> operator+(cpx<T> a, cpx<T> b)
+{
+    return mk(a.x + b.x, a.y + b.y);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> operator-(cpx<T> a, cpx<T> b)
+{
+    return mk(a.x - b.x, a.y - b.y);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> operator*(cpx<T> a, cpx<T> b)
+{
+    return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> scale(cpx<T> a, T s)
+{
+    return mk(a.x * s, a.y * s);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> conj(cpx<T> a)
+{
+    return mk(a.x, -a.y);
+}
+// a * (-i)
+template <typename T>
+__device__ __forceinline__ cpx<T> mul_mi(cpx<T> a)
+{
+    return mk(a.y, -a.x);
+}
+// a * (+i)
+template <typename T>
+__device__ __forceinline__ cpx<T> mul_pi(cpx<T> a)
+{
+    return mk(-a.y, a.x);
+}
+template <typename T>
+__device__ __forceinline__ cpx<T> conj_if(cpx<T> a, bool c)
+{
+    return c ? mk(a.x, -a.y) : a;
+}
+
+// Read-only cached load of one complex value.
+__device__ __forceinline__ cpx<float> ldg(const cpx<float>* p)
+{
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return mk(v.x, v.y);
+}
+__device__ __forceinline__ cpx<double> ldg(const cpx<double>* p)
+{
+    const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+    return mk(v.x, v.y);
+}
+
+// Shared-memory padding: one spare slot every 16 (8-byte elements) or 8 (16-byte elements) slots keeps
+// the power-of-two strided writes of the early passes free of bank conflicts.
+template <typename T>
+struct smem_pad
+{
+    static constexpr int shift = sizeof(T) == 4 ? 4 : 3;
+};
+template <typename T>
+__device__ __forceinline__ int pidx(int i)
+{
+    return i + (i >> smem_pad<T>::shift);
+}
+template <typename T>
+__host__ __device__ inline int padded_len(int n)
+{
+    return n + (n >> smem_pad<T>::shift) + 1;
+}
+
+// --------------------------------------------------------------------------------------------------
+// Codelets: forward DFT_R in registers, W_R = e^{-2 pi i / R}.
+// --------------------------------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ void dft2(cpx<T>& a, cpx<T>& b)
+{
+    cpx<T> t = a;
+    a        = t + b;
+    b        = t - b;
+}
+
+template <typename T>
+__device__ __forceinline__ void dft4(cpx<T>& x0, cpx<T>& x1, cpx<T>& x2, cpx<T>& x3)
+{
+    cpx<T> a0 = x0 + x2, a1 = x0 - x2;
+    cpx<T> b0 = x1 + x3, b1 = mul_mi(x1 - x3);
+    x0        = a0 + b0;
+    x2        = a0 - b0;
+    x1        = a1 + b1;
+    x3        = a1 - b1;
+}
+
+// cos / sin of 2*pi*k/R for odd R and k = 0..(R-1)/2, folded to constants once k is unrolled.
+__host__ __device__ constexpr double odd_cos(int R, int k)
+{
+    if (k == 0) // k*m can be a multiple of a composite radix (9)
+        return 1.0;
+    switch (R * 32 + k)
+    {
+    case 3 * 32 + 1: return -0.4999999999999998;
+    case 5 * 32 + 1: return 0.30901699437494745;
+    case 5 * 32 + 2: return -0.8090169943749473;
+    case 7 * 32 + 1: return 0.6234898018587336;
+    case 7 * 32 + 2: return -0.22252093395631434;
+    case 7 * 32 + 3: return -0.900968867902419;
+    case 9 * 32 + 1: return 0.766044443118978;
+    case 9 * 32 + 2: return 0.17364817766693041;
+    case 9 * 32 + 3: return -0.4999999999999998;
+    case 9 * 32 + 4: return -0.9396926207859083;
+    case 11 * 32 + 1: return 0.8412535328311812;
+    case 11 * 32 + 2: return 0.41541501300188644;
+    case 11 * 32 + 3: return -0.142314838273285;
+    case 11 * 32 + 4: return -0.654860733945285;
+    case 11 * 32 + 5: return -0.9594929736144974;
+    case 13 * 32 + 1: return 0.8854560256532099;
+    case 13 * 32 + 2: return 0.5680647467311559;
+    case 13 * 32 + 3: return 0.120536680255323;
+    case 13 * 32 + 4: return -0.35460488704253545;
+    case 13 * 32 + 5: return -0.7485107481711012;
+    case 13 * 32 + 6: return -0.970941817426052;
+    default: return 0.0;
+    }
+}
+__host__ __device__ constexpr double odd_sin(int R, int k)
+{
+    switch (R * 32 + k)
+    {
+    case 3 * 32 + 1: return 0.8660254037844387;
+    case 5 * 32 + 1: return 0.9510565162951535;
+    case 5 * 32 + 2: return 0.5877852522924732;
+    case 7 * 32 + 1: return 0.7818314824680298;
+    case 7 * 32 + 2: return 0.9749279121818236;
+    case 7 * 32 + 3: return 0.43388373911755823;
+    case 9 * 32 + 1: return 0.6427876096865393;
+    case 9 * 32 + 2: return 0.984807753012208;
+    case 9 * 32 + 3: return 0.8660254037844387;
+    case 9 * 32 + 4: return 0.3420201433256689;
+    case 11 * 32 + 1: return 0.5406408174555976;
+    case 11 * 32 + 2: return 0.9096319953545183;
+    case 11 * 32 + 3: return 0.9898214418809328;
+    case 11 * 32 + 4: return 0.7557495743542583;
+    case 11 * 32 + 5: return 0.28173255684142967;
+    case 13 * 32 + 1: return 0.4647231720437685;
+    case 13 * 32 + 2: return 0.8229838658936564;
+    case 13 * 32 + 3: return 0.992708874098054;
+    case 13 * 32 + 4: return 0.9350162426854148;
+    case 13 * 32 + 5: return 0.6631226582407952;
+    case 13 * 32 + 6: return 0.23931566428755768;
+    default: return 0.0;
+    }
+}
+
+// Odd-radix DFT by the symmetric pairing x_m +/- x_{R-m}:
+//   X_k = x0 + sum_m cos(2 pi k m / R)(x_m + x_{R-m}) - i sum_m sin(2 pi k m / R)(x_m - x_{R-m}),
+//   X_{R-k} = same with +i.
+template <typename T, int R>
+__device__ __forceinline__ void dft_odd(cpx<T>* v)
+{
+    constexpr int H = (R - 1) / 2;
+    cpx<T> s[H], d[H];
+#pragma unroll
+    for (int m = 1; m <= H; m++)
+    {
+        s[m - 1] = v[m] + v[R - m];
+        d[m - 1] = v[m] - v[R - m];
+    }
+    cpx<T> x0 = v[0];
+    cpx<T> sum = x0;
+#pragma unroll
+    for (int m = 0; m < H; m++)
+        sum = sum + s[m];
+#pragma unroll
+    for (int k = 1; k <= H; k++)
+    {
+        cpx<T> a = x0;
+        cpx<T> b = mk<T>(0, 0);
+#pragma unroll
+        for (int m = 1; m <= H; m++)
+        {
+            const int km = (k * m) % R;
+            // cos(2 pi km / R), sin(2 pi km / R) from the first-half tables
+            const int idx = km <= H ? km : R - km;
+            const T c     = T(odd_cos(R, idx));
+            const T sn    = km <= H ? T(odd_sin(R, idx)) : -T(odd_sin(R, idx));
+            a.x += c * s[m - 1].x;
+            a.y += c * s[m - 1].y;
+            b.x += sn * d[m - 1].x;
+            b.y += sn * d[m - 1].y;
+        }
+        v[k]     = a + mul_mi(b);
+        v[R - k] = a + mul_pi(b);
+    }
+    v[0] = sum;
+}
+
+template <typename T>
+__device__ __forceinline__ void dft8(cpx<T>* v)
+{
+    const T h = T(0.70710678118654752440084436210485);
+    dft4(v[0], v[2], v[4], v[6]);
+    dft4(v[1], v[3], v[5], v[7]);
+    cpx<T> o1 = mk(h * (v[3].x + v[3].y), h * (v[3].y - v[3].x)); // * W8
+    cpx<T> o2 = mul_mi(v[5]);                                    // * W8^2
+    cpx<T> o3 = mk(h * (v[7].y - v[7].x), -h * (v[7].x + v[7].y)); // * W8^3
+    cpx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    cpx<T> o0 = v[1];
+    v[0]      = e0 + o0;
+    v[4]      = e0 - o0;
+    v[1]      = e1 + o1;
+    v[5]      = e1 - o1;
+    v[2]      = e2 + o2;
+    v[6]      = e2 - o2;
+    v[3]      = e3 + o3;
+    v[7]      = e3 - o3;
+}
+
+// 16 = 4 x 4: column DFT4s, twiddles W16^{q k1}, row DFT4s done in place, so X[k1 + 4 k2] ends up in
+// v[4 k1 + k2] (a transposed order; see codelet_out).
+template <typename T>
+__device__ __forceinline__ void dft16(cpx<T>* v)
+{
+    const T c = T(0.92387953251128675612818318939679);
+    const T s = T(0.38268343236508977172845998403040);
+    const T h = T(0.70710678118654752440084436210485);
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        dft4(v[q], v[q + 4], v[q + 8], v[q + 12]);
+    // y[q][k1] lives in v[q + 4*k1]
+    v[5]  = v[5] * mk(c, -s);   // q=1,k1=1: W^1
+    v[9]  = v[9] * mk(h, -h);   // q=1,k1=2: W^2
+    v[13] = v[13] * mk(s, -c);  // q=1,k1=3: W^3
+    v[6]  = v[6] * mk(h, -h);   // q=2,k1=1: W^2
+    v[10] = mul_mi(v[10]);      // q=2,k1=2: W^4
+    v[14] = v[14] * mk(-h, -h); // q=2,k1=3: W^6
+    v[7]  = v[7] * mk(s, -c);   // q=3,k1=1: W^3
+    v[11] = v[11] * mk(-h, -h); // q=3,k1=2: W^6
+    v[15] = v[15] * mk(-c, s);  // q=3,k1=3: W^9
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++)
+        dft4(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+}
+
+// Register holding output r of codelet R (identity except for the transposed radix-16 codelet).
+template <int R>
+__device__ __forceinline__ constexpr int codelet_out(int r)
+{
+    return R == 16 ? (r & 3) * 4 + (r >> 2) : r;
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void dft_codelet(cpx<T>* v)
+{
+    if constexpr (R == 2)
+        dft2(v[0], v[1]);
+    else if constexpr (R == 4)
+        dft4(v[0], v[1], v[2], v[3]);
+    else if constexpr (R == 8)
+        dft8(v);
+    else if constexpr (R == 16)
+        dft16(v);
+    else
+        dft_odd<T, R>(v);
+}
+
+// --------------------------------------------------------------------------------------------------
+// Block FFT descriptor (built on the host by the planner).
+// --------------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t x, const fast_div f)
+{
+    if (f.d == 1)
+        return x;
+    uint32_t hi = __umulhi(x, f.m);
+    return (hi + ((x - hi) >> 1)) >> (f.s - 1);
+}
+
+// --------------------------------------------------------------------------------------------------
+// One pass, split into a load half (gather butterflies, twiddle, DFT_R, all in the thread's register
+// array v) and a store half (scatter to the self-sorted positions), with a barrier in between.  Every
+// radix works on the same array v[EPT] so that the runtime radix switch keeps one register layout;
+// threads lt in [0, ts) of a signal group own butterflies j = lt + b*ts.
+// --------------------------------------------------------------------------------------------------
+
+template <typename T, int R, int EPT>
+__device__ __forceinline__ void pass_load(cpx<T> (&v)[EPT], const cpx<T>* buf, const int n, const pass_desc& p,
+                                          const cpx<T>* __restrict__ tw, const int lt, const int ts)
+{
+    constexpr int NB = EPT / R;
+    const int nbf    = n / R;
+    const int ns     = p.ns;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * ts;
+        if (j < nbf)
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[b * R + r] = buf[pidx<T>(j + r * nbf)];
+            if (ns > 1)
+            {
+                const int k     = j - int(fdiv(uint32_t(j), p.div_ns)) * ns;
+                const cpx<T>* t = tw + p.tw_off + k;
+#pragma unroll
+                for (int r = 1; r < R; r++)
+                    v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * ns);
+            }
+            dft_codelet<T, R>(&v[b * R]);
+        }
+    }
+}
+
+template <typename T, int R, int EPT>
+__device__ __forceinline__ void pass_store(const cpx<T> (&v)[EPT], cpx<T>* buf, const int n, const pass_desc& p,
+                                           const int lt, const int ts)
+{
+    constexpr int NB = EPT / R;
+    const int nbf    = n / R;
+    const int ns     = p.ns;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * ts;
+        if (j < nbf)
+        {
+            const int k = ns > 1 ? j - int(fdiv(uint32_t(j), p.div_ns)) * ns : 0;
+            const int d = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                buf[pidx<T>(d + r * ns)] = v[b * R + codelet_out<R>(r)];
+        }
+    }
+}
+
+// Generic radix (any R, used for primes above 13): each thread computes up to EPT outputs
+// o = lt + e*ts, each a length-R dot product of the twiddled inputs (read from shared memory) with the
+// roots W_R^m.
+template <typename T, int EPT>
+__device__ __forceinline__ void pass_load_generic(cpx<T> (&v)[EPT], const cpx<T>* buf, const int n,
+                                                  const pass_desc& p, const cpx<T>* __restrict__ tw, const int lt,
+                                                  const int ts)
+{
+    const int R      = p.radix;
+    const int nbf    = n / R;
+    const int ns     = p.ns;
+    const cpx<T>* wr = tw + p.wr_off;
+#pragma unroll
+    for (int e = 0; e < EPT; e++)
+    {
+        const int oi = lt + e * ts;
+        if (oi < n)
+        {
+            const int q = oi / nbf;
+            const int j = oi - q * nbf;
+            const int k = ns > 1 ? j - int(fdiv(uint32_t(j), p.div_ns)) * ns : 0;
+            cpx<T> acc  = buf[pidx<T>(j)];
+            int widx    = 0;
+#pragma unroll 1
+            for (int r = 1; r < R; r++)
+            {
+                cpx<T> x = buf[pidx<T>(j + r * nbf)];
+                if (ns > 1)
+                    x = x * ldg(tw + p.tw_off + (r - 1) * ns + k);
+                widx += q;
+                if (widx >= R)
+                    widx -= R;
+                acc = acc + x * ldg(wr + widx);
+            }
+            v[e] = acc;
+        }
+    }
+}
+
+template <typename T, int EPT>
+__device__ __forceinline__ void pass_store_generic(const cpx<T> (&v)[EPT], cpx<T>* buf, const int n,
+                                                   const pass_desc& p, const int lt, const int ts)
+{
+    const int R   = p.radix;
+    const int nbf = n / R;
+    const int ns  = p.ns;
+#pragma unroll
+    for (int e = 0; e < EPT; e++)
+    {
+        const int oi = lt + e * ts;
+        if (oi < n)
+        {
+            const int q = oi / nbf;
+            const int j = oi - q * nbf;
+            const int k = ns > 1 ? j - int(fdiv(uint32_t(j), p.div_ns)) * ns : 0;
+            buf[pidx<T>((j - k) * R + k + q * ns)] = v[e];
+        }
+    }
+}
+
+// Runs every pass on the signal at buf.  The pass descriptors live in shared memory (staged by
+// stage_passes) so that the runtime pass loop never indexes the kernel's parameter block.  Must be reached
+// by all threads of the CTA (it synchronises); threads with lt >= ts only take part in the barriers.
+template <typename T, int EPT>
+__device__ __forceinline__ void block_fft(cpx<T>* buf, const pass_desc* sp, const int npass, const int n,
+                                          const cpx<T>* __restrict__ tw, const int lt, const int ts)
+{
+    const int lta = lt < ts ? lt : n; // inactive threads own no butterflies
+    cpx<T> v[EPT];
+#pragma unroll 1
+    for (int pi = 0; pi < npass; pi++)
+    {
+        const pass_desc p = sp[pi];
+        switch (p.radix)
+        {
+#define KFR_GPU_LOAD_CASE(R)                                                                               \
+    case R: pass_load<T, R, EPT>(v, buf, n, p, tw, lta, ts); break;
+            KFR_GPU_LOAD_CASE(2)
+            KFR_GPU_LOAD_CASE(3)
+            KFR_GPU_LOAD_CASE(4)
+            KFR_GPU_LOAD_CASE(5)
+            KFR_GPU_LOAD_CASE(7)
+            KFR_GPU_LOAD_CASE(8)
+            KFR_GPU_LOAD_CASE(9)
+            KFR_GPU_LOAD_CASE(11)
+            KFR_GPU_LOAD_CASE(13)
+            KFR_GPU_LOAD_CASE(16)
+#undef KFR_GPU_LOAD_CASE
+        default: pass_load_generic<T, EPT>(v, buf, n, p, tw, lta, ts); break;
+        }
+        __syncthreads();
+        switch (p.radix)
+        {
+#define KFR_GPU_STORE_CASE(R)                                                                              \
+    case R: pass_store<T, R, EPT>(v, buf, n, p, lta, ts); break;
+            KFR_GPU_STORE_CASE(2)
+            KFR_GPU_STORE_CASE(3)
+            KFR_GPU_STORE_CASE(4)
+            KFR_GPU_STORE_CASE(5)
+            KFR_GPU_STORE_CASE(7)
+            KFR_GPU_STORE_CASE(8)
+            KFR_GPU_STORE_CASE(9)
+            KFR_GPU_STORE_CASE(11)
+            KFR_GPU_STORE_CASE(13)
+            KFR_GPU_STORE_CASE(16)
+#undef KFR_GPU_STORE_CASE
+        default: pass_store_generic<T, EPT>(v, buf, n, p, lta, ts); break;
+        }
+        __syncthreads();
+    }
+}
+
+// Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a
+// barrier.
+__device__ __forceinline__ void stage_passes(pass_desc* sp, const fft_desc& d)
+{
+#pragma unroll
+    for (int i = 0; i < kMaxPasses; i++)
+        if (int(threadIdx.x) == i)
+            sp[i] = d.pass[i];
+    __syncthreads();
+}
+
+} // namespace kfr_gpu

@@ -1,0 +1,513 @@
+// Transform kernels.  Each kernel stages its signals in shared memory (coalesced global loads, with the
+// transform's pre-processing fused into the load), runs block_fft, and writes the result back with the
+// post-processing fused into the store, so a signal crosses HBM exactly once in each direction.
+//
+// Inverse transforms use conj(DFT(conj(x))), which is the unscaled inverse DFT of the reference
+// (include/kfr/dft/fft.hpp:262: no scaling), so only forward codelets and forward twiddles exist.
+#pragma once
+
+#include "fft_device.cuh"
+#include "launch.hpp"
+
+namespace kfr_gpu
+{
+
+// Largest CTA for a (precision, EPT) pair: the block FFT keeps EPT complex values per thread in registers.
+template <typename T, int EPT>
+struct ept_bounds
+{
+    static constexpr int threads = (sizeof(T) == 4 ? 1024 : 512) / (EPT / 16);
+};
+
+__device__ __forceinline__ uint32_t div_by(uint32_t x, const fast_div f) { return fdiv(x, f); }
+
+// thread -> (signal slot, lane within the signal's thread group)
+struct group_map
+{
+    int g, lt;
+    __device__ __forceinline__ group_map(int ts, int spc)
+    {
+        g  = int(threadIdx.x) / ts;
+        lt = g < spc ? int(threadIdx.x) - g * ts : ts;
+        if (g >= spc)
+            g = 0;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------------
+// Complex DFT, contiguous batch (dft_plan<T>::execute over many signals)
+// ---------------------------------------------------------------------------------------------------
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2c(const c2c_args a, const int ts, const int spc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int n       = a.d.n;
+    const int stride  = padded_len<T>(n);
+    const long long s0 = (long long)blockIdx.x * spc;
+    const cpx<T>* __restrict__ in = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* __restrict__ out      = reinterpret_cast<cpx<T>*>(a.out);
+    const bool inv  = a.inverse != 0;
+    const int total = spc * n;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < total; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int e = i - s * n;
+        const long long sig = s0 + s;
+        if (sig < a.batch)
+            sm[s * stride + pidx<T>(e)] = conj_if(in[sig * a.istride + e], inv);
+    }
+    __syncthreads();
+    const group_map gm(ts, spc);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+#pragma unroll 4
+    for (int i = threadIdx.x; i < total; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int e = i - s * n;
+        const long long sig = s0 + s;
+        if (sig < a.batch)
+            out[sig * a.ostride + e] = conj_if(sm[s * stride + pidx<T>(e)], inv);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Bluestein (dft_arblen_stage_impl, src/dft/dft-impl.hpp:248-272), fused into one kernel:
+//   a = x * chirp (zero padded to M) -> FFT_M -> * bhat -> inverse FFT_M -> * chirp
+// ---------------------------------------------------------------------------------------------------
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_bluestein(const bluestein_args a, const int ts,
+                                                                        const int spc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int m       = a.d.n;
+    const int n       = a.n;
+    const int stride  = padded_len<T>(m);
+    const long long s0 = (long long)blockIdx.x * spc;
+    const cpx<T>* __restrict__ in    = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* __restrict__ out         = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* __restrict__ chirp = reinterpret_cast<const cpx<T>*>(a.chirp);
+    const cpx<T>* __restrict__ bhat  = reinterpret_cast<const cpx<T>*>(a.bhat);
+    const bool inv = a.inverse != 0;
+    for (int i = threadIdx.x; i < spc * m; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_m));
+        const int e = i - s * m;
+        const long long sig = s0 + s;
+        cpx<T> v = mk<T>(0, 0);
+        if (e < n && sig < a.batch)
+            v = conj_if(in[sig * a.istride + e], inv) * ldg(chirp + e);
+        sm[s * stride + pidx<T>(e)] = v;
+    }
+    __syncthreads();
+    const group_map gm(ts, spc);
+    const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, tw, gm.lt, ts);
+    for (int i = threadIdx.x; i < spc * m; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_m));
+        const int e = i - s * m;
+        cpx<T>& r   = sm[s * stride + pidx<T>(e)];
+        r           = conj(r * ldg(bhat + e));
+    }
+    __syncthreads();
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, tw, gm.lt, ts);
+    for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int k = i - s * n;
+        const long long sig = s0 + s;
+        if (sig < a.batch)
+            out[sig * a.ostride + k] = conj_if(conj(sm[s * stride + pidx<T>(k)]) * ldg(chirp + k), inv);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Real forward DFT (dft_plan_real, CCs / Perm): c-point complex DFT of the reals viewed as c complex
+// values, then the split of to_fmt (src/dft/fft-impl.hpp:1799-1841) fused into the store.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_r2c(const real_args a, const int ts, const int spc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int c       = a.d.n;
+    const int stride  = padded_len<T>(c);
+    const long long s0 = (long long)blockIdx.x * spc;
+    const T* __restrict__ inr      = reinterpret_cast<const T*>(a.in);
+    cpx<T>* __restrict__ out       = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* __restrict__ rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
+    for (int i = threadIdx.x; i < spc * c; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int e = i - s * c;
+        const long long sig = s0 + s;
+        if (sig < a.batch)
+            sm[s * stride + pidx<T>(e)] = reinterpret_cast<const cpx<T>*>(inr + sig * a.istride)[e];
+    }
+    __syncthreads();
+    const group_map gm(ts, spc);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    const int olen = a.ccs ? c + 1 : c;
+    for (int i = threadIdx.x; i < spc * olen; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_out));
+        const int k = i - s * olen;
+        const long long sig = s0 + s;
+        if (sig >= a.batch)
+            continue;
+        const cpx<T>* z = sm + s * stride;
+        cpx<T> v;
+        if (k == 0)
+        {
+            const cpx<T> z0 = z[0];
+            v = a.ccs ? mk<T>(z0.x + z0.y, 0) : mk<T>(z0.x + z0.y, z0.x - z0.y);
+        }
+        else if (k == c)
+        {
+            const cpx<T> z0 = z[0];
+            v               = mk<T>(z0.x - z0.y, 0);
+        }
+        else
+        {
+            const cpx<T> zk  = z[pidx<T>(k)];
+            const cpx<T> znk = conj(z[pidx<T>(c - k)]);
+            const cpx<T> e   = scale(zk + znk, T(0.5));
+            const cpx<T> o   = scale(mul_mi(zk - znk), T(0.5));
+            v                = e + ldg(rtw + k) * o;
+        }
+        out[sig * a.ostride + k] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Real inverse DFT: the merge of from_fmt (src/dft/fft-impl.hpp:1852-1896) fused into the load, then an
+// unscaled inverse c-point complex DFT whose output is the 2c reals.  Only the real parts of the DC and
+// Nyquist bins are read, as in the reference.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2r(const real_args a, const int ts, const int spc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int c       = a.d.n;
+    const int stride  = padded_len<T>(c);
+    const long long s0 = (long long)blockIdx.x * spc;
+    const cpx<T>* __restrict__ in  = reinterpret_cast<const cpx<T>*>(a.in);
+    T* __restrict__ outr           = reinterpret_cast<T*>(a.out);
+    const cpx<T>* __restrict__ rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
+    for (int i = threadIdx.x; i < spc * c; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int k = i - s * c;
+        const long long sig = s0 + s;
+        if (sig >= a.batch)
+            continue;
+        const cpx<T>* X = in + sig * a.istride;
+        cpx<T> z;
+        if (k == 0)
+        {
+            const T x0 = X[0].x;
+            const T xn = a.ccs ? X[c].x : X[0].y;
+            z          = mk<T>(x0 + xn, x0 - xn);
+        }
+        else
+        {
+            const cpx<T> xk  = X[k];
+            const cpx<T> xnk = conj(X[c - k]);
+            const cpx<T> f1  = xk + xnk;
+            const cpx<T> f2  = xk - xnk;
+            z                = f1 + mul_pi(conj(ldg(rtw + k)) * f2);
+        }
+        sm[s * stride + pidx<T>(k)] = conj(z);
+    }
+    __syncthreads();
+    const group_map gm(ts, spc);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    for (int i = threadIdx.x; i < spc * c; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int e = i - s * c;
+        const long long sig = s0 + s;
+        if (sig < a.batch)
+            reinterpret_cast<cpx<T>*>(outr + sig * a.ostride)[e] = conj(sm[s * stride + pidx<T>(e)]);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// DCT-II (dct_plan::execute, include/kfr/dft/fft.hpp:938-950): even/odd mirror on load, n-point DFT,
+// Re*cos + Im*sin on store.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_dct2(const dct_args a, const int ts, const int spc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int n       = a.d.n;
+    const int stride  = padded_len<T>(n);
+    const long long s0 = (long long)blockIdx.x * spc;
+    const T* __restrict__ in       = reinterpret_cast<const T*>(a.in);
+    T* __restrict__ out            = reinterpret_cast<T*>(a.out);
+    const cpx<T>* __restrict__ dtw = reinterpret_cast<const cpx<T>*>(a.dtw);
+    for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
+    {
+        const int s   = int(div_by(uint32_t(i), a.div_n));
+        const int src = i - s * n;
+        const long long sig = s0 + s;
+        if (sig >= a.batch)
+            continue;
+        const int pos = (src & 1) ? n - 1 - (src >> 1) : (src >> 1);
+        sm[s * stride + pidx<T>(pos)] = mk<T>(in[sig * a.stride + src], T(0));
+    }
+    __syncthreads();
+    const group_map gm(ts, spc);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int k = i - s * n;
+        const long long sig = s0 + s;
+        if (sig >= a.batch)
+            continue;
+        const cpx<T> y = sm[s * stride + pidx<T>(k)];
+        const cpx<T> w = ldg(dtw + k);
+        out[sig * a.stride + k] = y.x * w.x + y.y * w.y;
+    }
+}
+
+// DCT-III, the reference's "inverse" (include/kfr/dft/fft.hpp:951-969): x_k * e^{-i pi k / 2n}, X0 halved,
+// forward n-point DFT, un-mirror the real parts.
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_dct3(const dct_args a, const int ts, const int spc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int n       = a.d.n;
+    const int stride  = padded_len<T>(n);
+    const long long s0 = (long long)blockIdx.x * spc;
+    const T* __restrict__ in       = reinterpret_cast<const T*>(a.in);
+    T* __restrict__ out            = reinterpret_cast<T*>(a.out);
+    const cpx<T>* __restrict__ dtw = reinterpret_cast<const cpx<T>*>(a.dtw);
+    for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int k = i - s * n;
+        const long long sig = s0 + s;
+        if (sig >= a.batch)
+            continue;
+        const T x      = in[sig * a.stride + k];
+        const cpx<T> w = ldg(dtw + k);
+        cpx<T> v       = mk<T>(x * w.x, -(x * w.y));
+        if (k == 0)
+            v = scale(v, T(0.5));
+        sm[s * stride + pidx<T>(k)] = v;
+    }
+    __syncthreads();
+    const group_map gm(ts, spc);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
+    {
+        const int s   = int(div_by(uint32_t(i), a.div_n));
+        const int dst = i - s * n;
+        const long long sig = s0 + s;
+        if (sig >= a.batch)
+            continue;
+        const int pos = (dst & 1) ? n - 1 - (dst >> 1) : (dst >> 1);
+        out[sig * a.stride + dst] = sm[s * stride + pidx<T>(pos)].x;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Four-step passes for lengths beyond one CTA (N = n1 * n2).  grid = (tiles, batch).
+// ---------------------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ cpx<T> twiddle_2level(const cpx<T>* __restrict__ A, const cpx<T>* __restrict__ B,
+                                                 long long m, int lbits)
+{
+    return ldg(A + (m >> lbits)) * ldg(B + (m & ((1LL << lbits) - 1)));
+}
+
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_fs_cols(const fourstep_args a, const int ts)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm       = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int n1     = a.n1, n2 = a.n2, S = a.tile;
+    const int stride = padded_len<T>(n1);
+    const int c0     = blockIdx.x * S;
+    const long long sig = blockIdx.y;
+    const cpx<T>* __restrict__ x = reinterpret_cast<const cpx<T>*>(a.in) + sig * a.sig_stride;
+    cpx<T>* __restrict__ y       = reinterpret_cast<cpx<T>*>(a.out) + sig * a.sig_stride;
+    const bool cin  = a.conj_in != 0;
+    const int total = S * n1;
+    for (int i = threadIdx.x; i < total; i += blockDim.x)
+    {
+        const int n1i = i / S; // S is a power of two
+        const int c   = i - n1i * S;
+        if (c0 + c < n2)
+            sm[c * stride + pidx<T>(n1i)] = conj_if(x[(long long)n1i * n2 + c0 + c], cin);
+    }
+    __syncthreads();
+    const group_map gm(ts, S);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    const cpx<T>* twA = reinterpret_cast<const cpx<T>*>(a.twA);
+    const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
+    for (int i = threadIdx.x; i < total; i += blockDim.x)
+    {
+        const int c  = int(div_by(uint32_t(i), a.div_n));
+        const int k1 = i - c * n1;
+        const int col = c0 + c;
+        if (col < n2)
+        {
+            cpx<T> v = sm[c * stride + pidx<T>(k1)];
+            v        = v * twiddle_2level(twA, twB, (long long)col * k1, a.lbits);
+            y[(long long)col * n1 + k1] = conj_if(v, a.conj_out != 0);
+        }
+    }
+}
+
+template <typename T, int EPT>
+__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_fs_rows(const fourstep_args a, const int ts)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    stage_passes(sp, a.d);
+    cpx<T>* sm       = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int n1     = a.n1, n2 = a.n2, S = a.tile;
+    const int stride = padded_len<T>(n2);
+    const int r0     = blockIdx.x * S;
+    const long long sig = blockIdx.y;
+    const cpx<T>* __restrict__ y = reinterpret_cast<const cpx<T>*>(a.in) + sig * a.sig_stride;
+    cpx<T>* __restrict__ X       = reinterpret_cast<cpx<T>*>(a.out) + sig * a.sig_stride;
+    const int total = S * n2;
+    const bool cin  = a.conj_in != 0;
+    for (int i = threadIdx.x; i < total; i += blockDim.x)
+    {
+        const int n2i = i / S;
+        const int r   = i - n2i * S;
+        if (r0 + r < n1)
+            sm[r * stride + pidx<T>(n2i)] = conj_if(y[(long long)n2i * n1 + r0 + r], cin);
+    }
+    __syncthreads();
+    const group_map gm(ts, S);
+    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    const bool cout = a.conj_out != 0;
+    for (int i = threadIdx.x; i < total; i += blockDim.x)
+    {
+        const int k2 = i / S;
+        const int r  = i - k2 * S;
+        if (r0 + r < n1)
+            X[(long long)(r0 + r) + (long long)n1 * k2] = conj_if(sm[r * stride + pidx<T>(k2)], cout);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------------------------------
+
+template <typename K>
+static cudaError_t prepare_smem(K kernel, int bytes)
+{
+    if (bytes > 48 * 1024)
+        return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return cudaSuccess;
+}
+
+#define KFR_GPU_DISPATCH_EPT(KERNEL, ARGS, ...)                                                            \
+    switch (c.ept)                                                                                         \
+    {                                                                                                      \
+    case 16:                                                                                               \
+    {                                                                                                      \
+        auto k = KERNEL<T, 16>;                                                                            \
+        cudaError_t e = prepare_smem(k, c.smem);                                                           \
+        if (e != cudaSuccess)                                                                              \
+            return e;                                                                                      \
+        k<<<ARGS>>>(__VA_ARGS__);                                                                          \
+        break;                                                                                             \
+    }                                                                                                      \
+    case 32:                                                                                               \
+    {                                                                                                      \
+        auto k = KERNEL<T, 32>;                                                                            \
+        cudaError_t e = prepare_smem(k, c.smem);                                                           \
+        if (e != cudaSuccess)                                                                              \
+            return e;                                                                                      \
+        k<<<ARGS>>>(__VA_ARGS__);                                                                          \
+        break;                                                                                             \
+    }                                                                                                      \
+    default: return cudaErrorInvalidValue;                                                                 \
+    }                                                                                                      \
+    return cudaGetLastError();
+
+#define KFR_GPU_LAUNCH1 dim3(unsigned(c.grid)), c.threads, c.smem, st
+
+template <typename T>
+cudaError_t launch_c2c(const c2c_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_c2c, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+}
+template <typename T>
+cudaError_t launch_bluestein(const bluestein_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_bluestein, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+}
+template <typename T>
+cudaError_t launch_r2c(const real_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_r2c, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+}
+template <typename T>
+cudaError_t launch_c2r(const real_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_c2r, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+}
+template <typename T>
+cudaError_t launch_dct2(const dct_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_dct2, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+}
+template <typename T>
+cudaError_t launch_dct3(const dct_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_dct3, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+}
+
+#define KFR_GPU_LAUNCH2 dim3(unsigned(c.grid), unsigned(a.batch)), c.threads, c.smem, st
+
+template <typename T>
+cudaError_t launch_fs_cols(const fourstep_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_fs_cols, KFR_GPU_LAUNCH2, a, c.ts)
+}
+template <typename T>
+cudaError_t launch_fs_rows(const fourstep_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_DISPATCH_EPT(k_fs_rows, KFR_GPU_LAUNCH2, a, c.ts)
+}
+
+#define KFR_GPU_INSTANTIATE(T)                                                                             \
+    template cudaError_t launch_c2c<T>(const c2c_args&, const block_cfg&, cudaStream_t);                   \
+    template cudaError_t launch_bluestein<T>(const bluestein_args&, const block_cfg&, cudaStream_t);       \
+    template cudaError_t launch_r2c<T>(const real_args&, const block_cfg&, cudaStream_t);                  \
+    template cudaError_t launch_c2r<T>(const real_args&, const block_cfg&, cudaStream_t);                  \
+    template cudaError_t launch_dct2<T>(const dct_args&, const block_cfg&, cudaStream_t);                  \
+    template cudaError_t launch_dct3<T>(const dct_args&, const block_cfg&, cudaStream_t);                  \
+    template cudaError_t launch_fs_cols<T>(const fourstep_args&, const block_cfg&, cudaStream_t);          \
+    template cudaError_t launch_fs_rows<T>(const fourstep_args&, const block_cfg&, cudaStream_t);
+
+} // namespace kfr_gpu

@@ -1,0 +1,158 @@
+// Kernel launch interface between the host planner (plan.cpp) and the CUDA kernels (kernels.cuh).
+// Everything here is plain C++: pointers are device addresses, strides are in elements.
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "fft_desc.hpp"
+
+namespace kfr_gpu
+{
+
+// Shape of one shared-memory FFT launch: `spc` signals per CTA, `ts` threads per signal, each thread owning
+// at most `ept` elements per pass.
+struct block_cfg
+{
+    int ept;
+    int ts;
+    int spc;
+    int threads;
+    int smem;
+    long long grid;
+};
+
+// Batched complex DFT of contiguous signals that fit one CTA's shared memory.
+struct c2c_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    long long istride, ostride; // complex elements between consecutive signals
+    int inverse;
+    const void* tw;
+    fast_div div_n;
+    fft_desc d;
+};
+
+// Bluestein chirp-z for lengths n whose power-of-two convolution size M = d.n fits one CTA.
+struct bluestein_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    long long istride, ostride;
+    int n;
+    int inverse;
+    const void* chirp; // n values e^{-i pi k^2 / n}
+    const void* bhat;  // M values: FFT_M of the conjugate chirp, scaled by 1/M
+    const void* tw;
+    fast_div div_n, div_m;
+    fft_desc d;
+};
+
+// Real DFT of even length 2c through a c-point complex DFT (d.n = c).
+// Forward: in = reals (istride reals apart), out = c+1 (CCs) or c (Perm) complex (ostride complex apart).
+// Inverse: in = c+1 / c complex (istride complex apart), out = 2c reals (ostride reals apart).
+struct real_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    long long istride, ostride;
+    int ccs;
+    const void* rtw; // W_{2c}^k for k = 0..c
+    const void* tw;
+    fast_div div_n, div_out;
+    fft_desc d;
+};
+
+// DCT-II / DCT-III of length n = d.n through an n-point complex DFT.
+struct dct_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    long long stride; // reals between consecutive signals (in and out)
+    const void* dtw;  // (cos(pi k / 2n), sin(pi k / 2n)) for k < n
+    const void* tw;
+    fast_div div_n;
+    fft_desc d;
+};
+
+// One pass of the four-step decomposition of N = n1 * n2 (x viewed as n1 rows by n2 columns).
+//   cols pass: FFT_n1 down each column, times W_N^{col * k1}, written column-contiguous to out[col*n1 + k1]
+//   rows pass: FFT_n2 along each k1 of the cols output, written to out[k1 + n1*k2]
+struct fourstep_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    long long sig_stride; // complex elements between consecutive signals
+    int n1, n2;
+    int tile;             // columns (cols pass) or k1 rows (rows pass) per CTA
+    int conj_in, conj_out;
+    const void* tw;
+    fft_desc d;
+    // two-level table for W_N^m: W_N^m = twA[m >> lbits] * twB[m & ((1 << lbits) - 1)]
+    const void* twA;
+    const void* twB;
+    int lbits;
+    fast_div div_n;  // divides by the FFT length of this pass
+};
+
+template <typename T>
+cudaError_t launch_c2c(const c2c_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_bluestein(const bluestein_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_r2c(const real_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_c2r(const real_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_dct2(const dct_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_dct3(const dct_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_fs_cols(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
+cudaError_t launch_fs_rows(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
+
+// Grid-stride elementwise kernels for the multi-kernel paths: Bluestein at lengths whose convolution does
+// not fit one CTA, and real-DFT / DCT pre- and post-processing around a multi-kernel complex DFT.  The
+// single-CTA paths fuse the same arithmetic into the FFT kernels.
+struct ew_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    long long n;     // elements per signal of the produced array
+    long long istride, ostride;
+    const void* t0;  // first table
+    const void* t1;  // second table
+    long long n_src; // length of the source signal (Bluestein) or the complex length c (real DFT)
+    int flag;        // inverse (Bluestein) / CCs (real DFT)
+};
+
+enum ew_op
+{
+    EW_BS_PRE    = 0, // out[e] = e < n_src ? conj_if(in[e], flag) * chirp[e] : 0   (n = M)
+    EW_BS_MID    = 1, // out[e] = conj(in[e] * bhat[e])                               (n = M)
+    EW_BS_POST   = 2, // out[k] = conj_if(conj(in[k]) * chirp[k], flag)               (n = N)
+    EW_R2C       = 3, // real forward split of a c-point spectrum Z; n = c+1 (CCs) or c (Perm)
+    EW_C2R       = 4, // real inverse merge into conj of a c-point spectrum (n = c)
+    EW_DCT2_PRE  = 5, // mirrored complex input (n = N)
+    EW_DCT2_POST = 6, // Re*cos + Im*sin (n = N)
+    EW_DCT3_PRE  = 7, // x * e^{-i pi k / 2N}, X0 halved (n = N)
+    EW_DCT3_POST = 8, // un-mirror real parts (n = N)
+};
+
+template <typename T>
+cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st);
+
+// Largest thread count a block FFT kernel may be launched with (elem_bytes = sizeof(real type)).
+int max_threads_for(int elem_bytes, int ept);
+// Largest dynamic shared memory a kernel may use on this device.
+int max_smem_bytes();
+
+} // namespace kfr_gpu

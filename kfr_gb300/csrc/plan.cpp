@@ -1,0 +1,938 @@
+// Host-side planner and executors (see plan.hpp).
+#include "plan.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+
+namespace kfr_gpu
+{
+
+void check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError(); // clear a sticky-free error so the next call starts clean
+        throw cuda_error(std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------
+// dbuf
+// ------------------------------------------------------------------------------------------------------
+
+void dbuf::alloc(size_t bytes)
+{
+    release();
+    if (bytes == 0)
+        return;
+    check(cudaMalloc(&p_, bytes), "cudaMalloc");
+    bytes_ = bytes;
+}
+
+void dbuf::ensure(size_t bytes)
+{
+    if (bytes > bytes_)
+        alloc(bytes);
+}
+
+void dbuf::release()
+{
+    if (p_)
+        cudaFree(p_);
+    p_     = nullptr;
+    bytes_ = 0;
+}
+
+void dbuf::upload(const void* host, size_t bytes)
+{
+    alloc(bytes);
+    if (bytes)
+        check(cudaMemcpy(p_, host, bytes, cudaMemcpyHostToDevice), "cudaMemcpy (tables)");
+}
+
+// ------------------------------------------------------------------------------------------------------
+// Twiddles and factorisation
+// ------------------------------------------------------------------------------------------------------
+
+std::complex<double> twiddle(long long k, long long n)
+{
+    k %= n;
+    if (k < 0)
+        k += n;
+    int q = 0;
+    if (n % 2 == 0 && k >= n / 2)
+    {
+        q += 2;
+        k -= n / 2;
+    }
+    if (n % 4 == 0 && k >= n / 4)
+    {
+        q += 1;
+        k -= n / 4;
+    }
+    double re = 1.0, im = 0.0;
+    if (k != 0)
+    {
+        const double a = 2.0 * M_PI * (double(k) / double(n));
+        re             = std::cos(a);
+        im             = -std::sin(a);
+    }
+    if (q & 1)
+    {
+        const double t = re;
+        re             = im;
+        im             = -t;
+    }
+    if (q & 2)
+    {
+        re = -re;
+        im = -im;
+    }
+    return { re, im };
+}
+
+void host_fft_pow2(std::vector<std::complex<double>>& b)
+{
+    const long long m = (long long)b.size();
+    // iterative radix-2 decimation in time, bit-reversed input order
+    for (long long i = 1, j = 0; i < m; i++)
+    {
+        long long bit = m >> 1;
+        for (; j & bit; bit >>= 1)
+            j ^= bit;
+        j ^= bit;
+        if (i < j)
+            std::swap(b[i], b[j]);
+    }
+    for (long long len = 2; len <= m; len <<= 1)
+        for (long long i = 0; i < m; i += len)
+            for (long long k = 0; k < len / 2; k++)
+            {
+                const std::complex<double> w = twiddle(k, len);
+                const std::complex<double> u = b[i + k], v = b[i + k + len / 2] * w;
+                b[i + k]                     = u + v;
+                b[i + k + len / 2]           = u - v;
+            }
+}
+
+std::vector<int> factor_radices(long long n)
+{
+    std::vector<int> r;
+    if (n <= 1)
+        return r;
+    int a = 0;
+    while (n % 2 == 0)
+    {
+        n /= 2;
+        a++;
+    }
+    const int q = a / 4, rem = a % 4;
+    if (rem == 1 && q >= 1)
+    {
+        for (int i = 0; i < q - 1; i++)
+            r.push_back(16);
+        r.push_back(8);
+        r.push_back(4);
+    }
+    else
+    {
+        for (int i = 0; i < q; i++)
+            r.push_back(16);
+        if (rem == 1)
+            r.push_back(2);
+        else if (rem == 2)
+            r.push_back(4);
+        else if (rem == 3)
+            r.push_back(8);
+    }
+    while (n % 9 == 0)
+    {
+        r.push_back(9);
+        n /= 9;
+    }
+    for (int p : { 3, 5, 7, 11, 13 })
+        while (n % p == 0)
+        {
+            r.push_back(p);
+            n /= p;
+        }
+    for (long long p = 17; p * p <= n; p += 2)
+        while (n % p == 0)
+        {
+            if (p > kGenericMax)
+                return {};
+            r.push_back(int(p));
+            n /= p;
+        }
+    if (n > 1)
+    {
+        if (n > kGenericMax)
+            return {};
+        r.push_back(int(n));
+    }
+    return r;
+}
+
+static bool is_codelet(int r)
+{
+    switch (r)
+    {
+    case 2:
+    case 3:
+    case 4:
+    case 5:
+    case 7:
+    case 8:
+    case 9:
+    case 11:
+    case 13:
+    case 16: return true;
+    default: return false;
+    }
+}
+
+// Threads per signal needed by a radix sequence at `ept` elements per thread (0 = infeasible).
+static int threads_needed(long long n, const std::vector<int>& radices, int ept)
+{
+    long long ts = 1;
+    for (int r : radices)
+    {
+        long long need;
+        if (is_codelet(r))
+        {
+            if (ept < r)
+                return 0;
+            const long long per = ept / r;
+            need                = (n / r + per - 1) / per;
+        }
+        else
+            need = (n + ept - 1) / ept;
+        ts = std::max(ts, need);
+    }
+    return int(std::min<long long>(ts, 1 << 20));
+}
+
+static int smem_budget()
+{
+    // dynamic shared memory left after the static pass-descriptor array and a small reserve
+    static const int budget = max_smem_bytes() - int(sizeof(pass_desc)) * kMaxPasses - 1024;
+    return budget;
+}
+
+// ------------------------------------------------------------------------------------------------------
+// block_program
+// ------------------------------------------------------------------------------------------------------
+
+template <typename T>
+bool block_program<T>::feasible(long long n)
+{
+    if (n < 2 || n > (1 << 20))
+        return false;
+    const auto rad = factor_radices(n);
+    if (rad.empty() || int(rad.size()) > kMaxPasses)
+        return false;
+    if (static_cast<long long>(padded_len_host<T>(int(n))) * static_cast<long long>(2 * sizeof(T)) > smem_budget())
+        return false;
+    for (int ept : { 16, 32 })
+    {
+        const int ts = threads_needed(n, rad, ept);
+        if (ts > 0 && ts <= max_threads_for(int(sizeof(T)), ept))
+            return true;
+    }
+    return false;
+}
+
+template <typename T>
+void block_program<T>::build(int n_)
+{
+    n       = n_;
+    radices = factor_radices(n);
+    if (radices.empty() || int(radices.size()) > kMaxPasses)
+        throw std::invalid_argument("internal: length has no one-CTA radix plan");
+    ept = 0;
+    for (int e : { 16, 32 })
+    {
+        const int t = threads_needed(n, radices, e);
+        if (t > 0 && t <= max_threads_for(int(sizeof(T)), e))
+        {
+            ept = e;
+            ts  = t;
+            break;
+        }
+    }
+    if (ept == 0)
+        throw std::invalid_argument("internal: length exceeds one CTA");
+    std::memset(&desc, 0, sizeof(desc));
+    desc.n     = n;
+    desc.npass = int(radices.size());
+    std::vector<std::complex<T>> table;
+    long long ns = 1;
+    for (size_t i = 0; i < radices.size(); i++)
+    {
+        const int R     = radices[i];
+        pass_desc& p    = desc.pass[i];
+        p.radix         = R;
+        p.ns            = int(ns);
+        p.div_ns        = make_fast_div(uint32_t(ns));
+        p.tw_off        = int(table.size());
+        const long long L = ns * R;
+        if (ns > 1)
+            for (int r = 1; r < R; r++)
+                for (long long k = 0; k < ns; k++)
+                {
+                    const auto w = twiddle(k * r, L);
+                    table.emplace_back(T(w.real()), T(w.imag()));
+                }
+        p.wr_off = int(table.size());
+        if (!is_codelet(R))
+            for (int m = 0; m < R; m++)
+            {
+                const auto w = twiddle(m, R);
+                table.emplace_back(T(w.real()), T(w.imag()));
+            }
+        ns = L;
+    }
+    if (table.empty())
+        table.emplace_back(T(1), T(0));
+    tw.upload(table.data(), table.size() * sizeof(std::complex<T>));
+}
+
+template <typename T>
+block_cfg block_program<T>::cfg(long long batch, int spc_cap) const
+{
+    block_cfg c;
+    c.ept              = ept;
+    c.ts               = ts;
+    const int per_sig  = padded_len_host<T>(n) * int(2 * sizeof(T));
+    const int max_thr  = max_threads_for(int(sizeof(T)), ept);
+    int spc            = std::max(1, 256 / ts);
+    spc                = std::min(spc, std::max(1, max_thr / ts));
+    spc                = std::min(spc, std::max(1, smem_budget() / per_sig));
+    // keep at least ~2 CTAs per SM when the batch allows it
+    const long long want_ctas = 2LL * 152;
+    if (batch < want_ctas * spc)
+        spc = int(std::max<long long>(1, std::min<long long>(spc, (batch + want_ctas - 1) / want_ctas)));
+    if (spc_cap > 0)
+        spc = std::min(spc, spc_cap);
+    c.spc     = spc;
+    c.threads = ((spc * ts + 31) / 32) * 32;
+    c.smem    = spc * per_sig;
+    c.grid    = (batch + spc - 1) / spc;
+    return c;
+}
+
+template <typename T>
+block_cfg block_program<T>::cfg_tile(int tile) const
+{
+    block_cfg c;
+    c.ept     = ept;
+    c.ts      = ts;
+    c.spc     = tile;
+    c.threads = ((tile * ts + 31) / 32) * 32;
+    c.smem    = tile * padded_len_host<T>(n) * int(2 * sizeof(T));
+    c.grid    = 1;
+    return c;
+}
+
+template <typename T>
+std::string block_program<T>::describe() const
+{
+    std::ostringstream s;
+    s << "block_fft n=" << n << " radices=";
+    for (size_t i = 0; i < radices.size(); i++)
+        s << (i ? "x" : "") << radices[i];
+    s << " ept=" << ept << " threads/signal=" << ts;
+    return s.str();
+}
+
+// ------------------------------------------------------------------------------------------------------
+// complex_engine
+// ------------------------------------------------------------------------------------------------------
+
+template <typename T>
+complex_engine<T>::complex_engine(long long n) : n_(n)
+{
+    if (n <= 1)
+    {
+        k_ = kind::trivial;
+        return;
+    }
+    if (block_program<T>::feasible(n))
+    {
+        k_ = kind::smem;
+        prog_.build(int(n));
+        return;
+    }
+    const auto rad = factor_radices(n);
+    if (rad.empty())
+    {
+        // a prime factor above kGenericMax: Bluestein
+        init_bluestein(n);
+        return;
+    }
+    if (plan_fourstep(n))
+        return;
+    init_bluestein(n);
+}
+
+template <typename T>
+void complex_engine<T>::init_bluestein(long long n)
+{
+    long long m = 1;
+    while (m < 2 * n - 1)
+        m <<= 1;
+    m_ = m;
+    // chirp[k] = e^{-i pi k^2 / n} with the phase k^2 mod 2n kept in integers, as the reference does
+    // (src/dft/dft-impl.hpp:217-226)
+    std::vector<std::complex<T>> chirp(n);
+    std::vector<std::complex<double>> chirp64(n);
+    long long ph = 0;
+    for (long long k = 0; k < n; k++)
+    {
+        if (k > 0)
+        {
+            ph += 2 * k - 1;
+            if (ph >= 2 * n)
+                ph -= 2 * n;
+        }
+        chirp64[k] = twiddle(ph, 2 * n);
+        chirp[k]   = std::complex<T>(T(chirp64[k].real()), T(chirp64[k].imag()));
+    }
+    chirp_.upload(chirp.data(), chirp.size() * sizeof(std::complex<T>));
+    // bhat = conj(FFT_M(b)) / M with b[k] = b[M-k] = chirp[k]: evaluated in double on the host by a plain
+    // radix-2 FFT so the table is exact to double rounding before it is stored as T.
+    std::vector<std::complex<double>> b(m, { 0.0, 0.0 });
+    for (long long k = 0; k < n; k++)
+    {
+        b[k] = chirp64[k];
+        if (k)
+            b[m - k] = chirp64[k];
+    }
+    host_fft_pow2(b);
+    std::vector<std::complex<T>> bh(m);
+    const double inv_m = 1.0 / double(m);
+    for (long long k = 0; k < m; k++)
+        bh[k] = std::complex<T>(T(b[k].real() * inv_m), T(-b[k].imag() * inv_m));
+    bhat_.upload(bh.data(), bh.size() * sizeof(std::complex<T>));
+    if (block_program<T>::feasible(m))
+    {
+        k_ = kind::bluestein_smem;
+        prog_.build(int(m));
+    }
+    else
+    {
+        k_ = kind::bluestein_multi;
+        inner_.reset(new complex_engine<T>(m));
+    }
+}
+
+template <typename T>
+static int tile_for(const block_program<T>& p)
+{
+    const int per_sig = padded_len_host<T>(p.n) * int(2 * sizeof(T));
+    const int max_thr = max_threads_for(int(sizeof(T)), p.ept);
+    int s             = 16;
+    while (s > 1 && (s * per_sig > smem_budget() || s * p.ts > max_thr))
+        s /= 2;
+    if (s * per_sig > smem_budget() || s * p.ts > max_thr)
+        return 0;
+    return s;
+}
+
+template <typename T>
+bool complex_engine<T>::plan_fourstep(long long n)
+{
+    long long best_n1 = 0;
+    int best_score    = -1;
+    double best_bal   = 1e30;
+    for (long long n1 = 2; n1 * 2 <= n && n1 <= (1 << 16); n1++)
+    {
+        if (n % n1)
+            continue;
+        const long long n2 = n / n1;
+        if (n2 > (1 << 16) || n1 * n2 != n)
+            continue;
+        if (!block_program<T>::feasible(n1) || !block_program<T>::feasible(n2))
+            continue;
+        block_program<T> a, b;
+        a.n = int(n1);
+        b.n = int(n2);
+        // thread shape without uploading tables
+        a.radices = factor_radices(n1);
+        b.radices = factor_radices(n2);
+        for (auto* p : { &a, &b })
+            for (int e : { 16, 32 })
+            {
+                const int t = threads_needed(p->n, p->radices, e);
+                if (t > 0 && t <= max_threads_for(int(sizeof(T)), e))
+                {
+                    p->ept = e;
+                    p->ts  = t;
+                    break;
+                }
+            }
+        const int sc = tile_for(a), sr = tile_for(b);
+        if (sc == 0 || sr == 0)
+            continue;
+        const int score   = std::min(std::min(sc, sr), 16);
+        const double bal  = std::fabs(std::log(double(n1)) - std::log(double(n2)));
+        if (score > best_score || (score == best_score && bal < best_bal))
+        {
+            best_score = score;
+            best_bal   = bal;
+            best_n1    = n1;
+        }
+    }
+    if (best_n1 == 0)
+        return false;
+    k_  = kind::fourstep;
+    n1_ = best_n1;
+    n2_ = n / best_n1;
+    pcols_.build(int(n1_));
+    prows_.build(int(n2_));
+    tile_c_ = tile_for(pcols_);
+    tile_r_ = tile_for(prows_);
+    // two-level table for W_N^m, m < N
+    int lb = 0;
+    while ((1LL << (2 * lb)) < n)
+        lb++;
+    lbits_             = lb;
+    const long long nb = 1LL << lb;
+    const long long na = (n + nb - 1) / nb;
+    std::vector<std::complex<T>> A(na), B(nb);
+    for (long long i = 0; i < na; i++)
+    {
+        const auto w = twiddle(i * nb, n);
+        A[i]         = std::complex<T>(T(w.real()), T(w.imag()));
+    }
+    for (long long j = 0; j < nb; j++)
+    {
+        const auto w = twiddle(j, n);
+        B[j]         = std::complex<T>(T(w.real()), T(w.imag()));
+    }
+    twA_.upload(A.data(), A.size() * sizeof(std::complex<T>));
+    twB_.upload(B.data(), B.size() * sizeof(std::complex<T>));
+    return true;
+}
+
+template <typename T>
+long long complex_engine<T>::scratch_elems(long long batch) const
+{
+    switch (k_)
+    {
+    case kind::fourstep: return batch * n_;
+    case kind::bluestein_multi: return batch * m_ + inner_->scratch_elems(batch);
+    default: return 0;
+    }
+}
+
+template <typename T>
+int complex_engine<T>::launches(long long batch) const
+{
+    switch (k_)
+    {
+    case kind::trivial: return 1;
+    case kind::smem:
+    case kind::bluestein_smem: return 1;
+    case kind::fourstep: return 2 * int((batch + 65534) / 65535);
+    case kind::bluestein_multi: return 3 + 2 * inner_->launches(batch);
+    }
+    return 0;
+}
+
+template <typename T>
+void complex_engine<T>::execute(void* out, const void* in, long long batch, long long istride, long long ostride,
+                                bool inverse, void* scratch, cudaStream_t st) const
+{
+    if (batch <= 0)
+        return;
+    const size_t esz = 2 * sizeof(T);
+    switch (k_)
+    {
+    case kind::trivial:
+    {
+        if (n_ == 1 && out != in)
+        {
+            if (istride == 1 && ostride == 1)
+                check(cudaMemcpyAsync(out, in, batch * esz, cudaMemcpyDeviceToDevice, st), "copy");
+            else
+                check(cudaMemcpy2DAsync(out, ostride * esz, in, istride * esz, esz, batch,
+                                        cudaMemcpyDeviceToDevice, st),
+                      "copy");
+        }
+        return;
+    }
+    case kind::smem:
+    {
+        c2c_args a;
+        a.in      = in;
+        a.out     = out;
+        a.batch   = batch;
+        a.istride = istride;
+        a.ostride = ostride;
+        a.inverse = inverse;
+        a.tw      = prog_.tw.get();
+        a.div_n   = make_fast_div(uint32_t(n_));
+        a.d       = prog_.desc;
+        check(launch_c2c<T>(a, prog_.cfg(batch), st), "launch c2c");
+        return;
+    }
+    case kind::bluestein_smem:
+    {
+        bluestein_args a;
+        a.in      = in;
+        a.out     = out;
+        a.batch   = batch;
+        a.istride = istride;
+        a.ostride = ostride;
+        a.n       = int(n_);
+        a.inverse = inverse;
+        a.chirp   = chirp_.get();
+        a.bhat    = bhat_.get();
+        a.tw      = prog_.tw.get();
+        a.div_n   = make_fast_div(uint32_t(n_));
+        a.div_m   = make_fast_div(uint32_t(m_));
+        a.d       = prog_.desc;
+        check(launch_bluestein<T>(a, prog_.cfg(batch), st), "launch bluestein");
+        return;
+    }
+    case kind::fourstep:
+    {
+        if (istride != n_ || ostride != n_)
+            throw std::invalid_argument("internal: four-step needs contiguous signals");
+        for (long long b0 = 0; b0 < batch; b0 += 65535)
+        {
+            const long long nb  = std::min<long long>(65535, batch - b0);
+            const char* inb     = static_cast<const char*>(in) + b0 * n_ * esz;
+            char* outb          = static_cast<char*>(out) + b0 * n_ * esz;
+            char* scr           = static_cast<char*>(scratch) + b0 * n_ * esz;
+            fourstep_args a;
+            a.batch      = nb;
+            a.sig_stride = n_;
+            a.n1         = int(n1_);
+            a.n2         = int(n2_);
+            a.twA        = twA_.get();
+            a.twB        = twB_.get();
+            a.lbits      = lbits_;
+            // column pass: x -> scratch
+            a.in       = inb;
+            a.out      = scr;
+            a.tile     = tile_c_;
+            a.conj_in  = inverse;
+            a.conj_out = 0;
+            a.tw       = pcols_.tw.get();
+            a.d        = pcols_.desc;
+            a.div_n    = make_fast_div(uint32_t(n1_));
+            block_cfg cc = pcols_.cfg_tile(tile_c_);
+            cc.grid      = (n2_ + tile_c_ - 1) / tile_c_;
+            check(launch_fs_cols<T>(a, cc, st), "launch four-step columns");
+            // row pass: scratch -> out
+            a.in       = scr;
+            a.out      = outb;
+            a.tile     = tile_r_;
+            a.conj_in  = 0;
+            a.conj_out = inverse;
+            a.tw       = prows_.tw.get();
+            a.d        = prows_.desc;
+            a.div_n    = make_fast_div(uint32_t(n2_));
+            block_cfg cr = prows_.cfg_tile(tile_r_);
+            cr.grid      = (n1_ + tile_r_ - 1) / tile_r_;
+            check(launch_fs_rows<T>(a, cr, st), "launch four-step rows");
+        }
+        return;
+    }
+    case kind::bluestein_multi:
+    {
+        if (istride != n_ || ostride != n_)
+            throw std::invalid_argument("internal: Bluestein needs contiguous signals");
+        char* A     = static_cast<char*>(scratch);
+        char* inner = A + batch * m_ * esz;
+        ew_args e;
+        e.batch   = batch;
+        e.t1      = nullptr;
+        e.flag    = inverse;
+        // A = x * chirp, zero padded to M
+        e.in      = in;
+        e.out     = A;
+        e.n       = m_;
+        e.istride = n_;
+        e.ostride = m_;
+        e.t0      = chirp_.get();
+        e.n_src   = n_;
+        check(launch_elementwise<T>(EW_BS_PRE, e, st), "launch bluestein pre");
+        inner_->execute(A, A, batch, m_, m_, false, inner, st);
+        e.in      = A;
+        e.out     = A;
+        e.istride = m_;
+        e.t0      = bhat_.get();
+        check(launch_elementwise<T>(EW_BS_MID, e, st), "launch bluestein mid");
+        inner_->execute(A, A, batch, m_, m_, false, inner, st);
+        e.in      = A;
+        e.out     = out;
+        e.n       = n_;
+        e.istride = m_;
+        e.ostride = n_;
+        e.t0      = chirp_.get();
+        check(launch_elementwise<T>(EW_BS_POST, e, st), "launch bluestein post");
+        return;
+    }
+    }
+}
+
+template <typename T>
+std::string complex_engine<T>::describe() const
+{
+    std::ostringstream s;
+    switch (k_)
+    {
+    case kind::trivial: s << "trivial n=" << n_; break;
+    case kind::smem: s << "smem " << prog_.describe(); break;
+    case kind::bluestein_smem: s << "bluestein_smem n=" << n_ << " m=" << m_ << " [" << prog_.describe() << "]"; break;
+    case kind::fourstep:
+        s << "fourstep n=" << n_ << " = " << n1_ << " x " << n2_ << " cols[" << pcols_.describe() << " tile=" << tile_c_
+          << "] rows[" << prows_.describe() << " tile=" << tile_r_ << "]";
+        break;
+    case kind::bluestein_multi: s << "bluestein_multi n=" << n_ << " m=" << m_ << " inner{" << inner_->describe() << "}"; break;
+    }
+    return s.str();
+}
+
+// ------------------------------------------------------------------------------------------------------
+// real_engine
+// ------------------------------------------------------------------------------------------------------
+
+template <typename T>
+real_engine<T>::real_engine(long long n) : n_(n), c_(n / 2), ceng_(n / 2)
+{
+    if (n <= 0 || n % 2)
+        throw std::invalid_argument("dft_plan_real requires size to be even");
+    // W_n^k for k = 0..c
+    std::vector<std::complex<T>> r(c_ + 1);
+    for (long long k = 0; k <= c_; k++)
+    {
+        const auto w = twiddle(k, n);
+        r[k]         = std::complex<T>(T(w.real()), T(w.imag()));
+    }
+    rtw_.upload(r.data(), r.size() * sizeof(std::complex<T>));
+    fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
+}
+
+template <typename T>
+long long real_engine<T>::scratch_elems(long long batch) const
+{
+    if (fused_)
+        return 0;
+    return batch * (c_ + 1) + ceng_.scratch_elems(batch);
+}
+
+template <typename T>
+int real_engine<T>::launches(long long batch) const
+{
+    return fused_ ? 1 : 1 + ceng_.launches(batch);
+}
+
+template <typename T>
+void real_engine<T>::forward(void* out, const void* in, long long batch, bool ccs, void* scratch,
+                             cudaStream_t st) const
+{
+    if (batch <= 0)
+        return;
+    const long long olen = ccs ? c_ + 1 : c_;
+    if (c_ == 1)
+    {
+        // n = 2: X0 = x0 + x1, X1 = x0 - x1 (the split of a one-point DFT)
+        ew_args e;
+        e.in      = in;
+        e.out     = out;
+        e.batch   = batch;
+        e.n       = olen;
+        e.istride = 1;
+        e.ostride = olen;
+        e.t0      = rtw_.get();
+        e.t1      = nullptr;
+        e.n_src   = 1;
+        e.flag    = ccs;
+        check(launch_elementwise<T>(EW_R2C, e, st), "launch r2c split");
+        return;
+    }
+    if (fused_)
+    {
+        const block_program<T>& p = ceng_.program();
+        real_args a;
+        a.in      = in;
+        a.out     = out;
+        a.batch   = batch;
+        a.istride = n_;
+        a.ostride = olen;
+        a.ccs     = ccs;
+        a.rtw     = rtw_.get();
+        a.tw      = p.tw.get();
+        a.div_n   = make_fast_div(uint32_t(c_));
+        a.div_out = make_fast_div(uint32_t(olen));
+        a.d       = p.desc;
+        check(launch_r2c<T>(a, p.cfg(batch), st), "launch r2c");
+        return;
+    }
+    char* Z     = static_cast<char*>(scratch);
+    char* inner = Z + batch * (c_ + 1) * 2 * sizeof(T);
+    ceng_.execute(Z, in, batch, c_, c_, false, inner, st);
+    ew_args e;
+    e.in      = Z;
+    e.out     = out;
+    e.batch   = batch;
+    e.n       = olen;
+    e.istride = c_;
+    e.ostride = olen;
+    e.t0      = rtw_.get();
+    e.t1      = nullptr;
+    e.n_src   = c_;
+    e.flag    = ccs;
+    check(launch_elementwise<T>(EW_R2C, e, st), "launch r2c split");
+}
+
+template <typename T>
+void real_engine<T>::inverse(void* out, const void* in, long long batch, bool ccs, void* scratch,
+                             cudaStream_t st) const
+{
+    if (batch <= 0)
+        return;
+    const long long ilen = ccs ? c_ + 1 : c_;
+    if (fused_)
+    {
+        const block_program<T>& p = ceng_.program();
+        real_args a;
+        a.in      = in;
+        a.out     = out;
+        a.batch   = batch;
+        a.istride = ilen;
+        a.ostride = n_;
+        a.ccs     = ccs;
+        a.rtw     = rtw_.get();
+        a.tw      = p.tw.get();
+        a.div_n   = make_fast_div(uint32_t(c_));
+        a.div_out = make_fast_div(uint32_t(c_));
+        a.d       = p.desc;
+        check(launch_c2r<T>(a, p.cfg(batch), st), "launch c2r");
+        return;
+    }
+    char* Z     = static_cast<char*>(scratch);
+    char* inner = Z + batch * (c_ + 1) * 2 * sizeof(T);
+    ew_args e;
+    e.in      = in;
+    e.out     = Z;
+    e.batch   = batch;
+    e.n       = c_;
+    e.istride = ilen;
+    e.ostride = c_;
+    e.t0      = rtw_.get();
+    e.t1      = nullptr;
+    e.n_src   = c_;
+    e.flag    = ccs;
+    check(launch_elementwise<T>(EW_C2R, e, st), "launch c2r merge");
+    ceng_.execute(out, Z, batch, c_, c_, true, inner, st);
+}
+
+template <typename T>
+std::string real_engine<T>::describe() const
+{
+    std::ostringstream s;
+    s << "real n=" << n_ << (fused_ ? " fused split/merge" : " separate split/merge") << " complex{" << ceng_.describe()
+      << "}";
+    return s.str();
+}
+
+// ------------------------------------------------------------------------------------------------------
+// dct_engine
+// ------------------------------------------------------------------------------------------------------
+
+template <typename T>
+dct_engine<T>::dct_engine(long long n) : n_(n), ceng_(n)
+{
+    if (n <= 0)
+        throw std::invalid_argument("dct_plan requires a positive size");
+    std::vector<std::complex<T>> d(n);
+    for (long long k = 0; k < n; k++)
+    {
+        // (cos, sin) of pi k / (2n) = -twiddle(k, 4n)
+        const auto w = twiddle(k, 4 * n);
+        d[k]         = std::complex<T>(T(w.real()), T(-w.imag()));
+    }
+    dtw_.upload(d.data(), d.size() * sizeof(std::complex<T>));
+    fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
+}
+
+template <typename T>
+long long dct_engine<T>::scratch_elems(long long batch) const
+{
+    if (fused_)
+        return 0;
+    return batch * n_ + ceng_.scratch_elems(batch);
+}
+
+template <typename T>
+int dct_engine<T>::launches(long long batch) const
+{
+    return fused_ ? 1 : 2 + ceng_.launches(batch);
+}
+
+template <typename T>
+void dct_engine<T>::execute(void* out, const void* in, long long batch, bool inverse, void* scratch,
+                            cudaStream_t st) const
+{
+    if (batch <= 0)
+        return;
+    if (fused_)
+    {
+        const block_program<T>& p = ceng_.program();
+        dct_args a;
+        a.in     = in;
+        a.out    = out;
+        a.batch  = batch;
+        a.stride = n_;
+        a.dtw    = dtw_.get();
+        a.tw     = p.tw.get();
+        a.div_n  = make_fast_div(uint32_t(n_));
+        a.d      = p.desc;
+        check(inverse ? launch_dct3<T>(a, p.cfg(batch), st) : launch_dct2<T>(a, p.cfg(batch), st), "launch dct");
+        return;
+    }
+    char* V     = static_cast<char*>(scratch);
+    char* inner = V + batch * n_ * 2 * sizeof(T);
+    ew_args e;
+    e.batch = batch;
+    e.n     = n_;
+    e.t0    = dtw_.get();
+    e.t1    = nullptr;
+    e.n_src = n_;
+    e.flag  = 0;
+    e.in      = in;
+    e.out     = V;
+    e.istride = n_;
+    e.ostride = n_;
+    check(launch_elementwise<T>(inverse ? EW_DCT3_PRE : EW_DCT2_PRE, e, st), "launch dct pre");
+    ceng_.execute(V, V, batch, n_, n_, false, inner, st);
+    e.in  = V;
+    e.out = out;
+    check(launch_elementwise<T>(inverse ? EW_DCT3_POST : EW_DCT2_POST, e, st), "launch dct post");
+}
+
+template <typename T>
+std::string dct_engine<T>::describe() const
+{
+    std::ostringstream s;
+    s << "dct n=" << n_ << (fused_ ? " fused" : " separate pre/post") << " complex{" << ceng_.describe() << "}";
+    return s.str();
+}
+
+template struct block_program<float>;
+template struct block_program<double>;
+template class complex_engine<float>;
+template class complex_engine<double>;
+template class real_engine<float>;
+template class real_engine<double>;
+template class dct_engine<float>;
+template class dct_engine<double>;
+
+} // namespace kfr_gpu

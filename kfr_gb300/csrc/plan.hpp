@@ -1,0 +1,176 @@
+// Host-side planner and executors of the GB300 DFT engine.
+//
+// A plan for length N picks one of five strategies (the GPU counterpart of the reference's stage lists,
+// include/kfr/dft/fft.hpp:372-381, built by init_fft / init_dft, src/dft/fft-impl.hpp:1903-1918 and
+// src/dft/dft-impl.hpp:512-583):
+//   trivial          N <= 1
+//   smem             one CTA per signal (or several signals per CTA): load, all passes in shared memory,
+//                    store.  N up to 16384 (c32) / 8192 (c64).
+//   bluestein_smem   a prime factor above kGenericMax and M = next_pow2(2N-1) fits one CTA: the whole
+//                    chirp-z transform in one kernel.
+//   fourstep         N = n1 * n2, both one-CTA lengths: a column pass (FFT_n1, twiddle, transpose-store)
+//                    and a row pass (FFT_n2, transpose-store), each one HBM round trip.
+//   bluestein_multi  anything else: chirp pre-multiply, M-point engine, spectral product, M-point engine,
+//                    chirp post-multiply.
+#pragma once
+
+#include <complex>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "launch.hpp"
+
+namespace kfr_gpu
+{
+
+constexpr int kGenericMax = 127; // largest prime handled by a generic radix pass (above: Bluestein)
+
+struct cuda_error : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
+};
+
+void check(cudaError_t e, const char* what);
+
+// Owning device allocation.
+class dbuf
+{
+public:
+    dbuf() = default;
+    dbuf(const dbuf&)            = delete;
+    dbuf& operator=(const dbuf&) = delete;
+    ~dbuf() { release(); }
+    void alloc(size_t bytes);
+    void ensure(size_t bytes); // grows (never shrinks) the allocation
+    void release();
+    void upload(const void* host, size_t bytes);
+    void* get() const { return p_; }
+    size_t size() const { return bytes_; }
+
+private:
+    void* p_      = nullptr;
+    size_t bytes_ = 0;
+};
+
+// e^{-2 pi i k / n} in double, with the exact quadrant folding of the reference's calculate_twiddle
+// (src/dft/ft.hpp:1803-1827).
+std::complex<double> twiddle(long long k, long long n);
+
+// In-place forward DFT of a power-of-two length in double precision (host; used for precomputed spectra).
+void host_fft_pow2(std::vector<std::complex<double>>& a);
+
+// Radix sequence for a one-CTA length; empty if a prime factor exceeds kGenericMax.
+std::vector<int> factor_radices(long long n);
+
+// Descriptor, twiddles and thread shape of a one-CTA FFT of length n.
+template <typename T>
+struct block_program
+{
+    int n   = 0;
+    int ept = 16;
+    int ts  = 1;
+    fft_desc desc{};
+    std::vector<int> radices;
+    dbuf tw;
+
+    // False if n cannot run in one CTA (size, registers or a large prime factor).
+    static bool feasible(long long n);
+    void build(int n);
+    // Launch shape for `batch` signals (`spc_cap` bounds the signals per CTA, 0 = no bound).
+    block_cfg cfg(long long batch, int spc_cap = 0) const;
+    // Launch shape of a four-step tile: exactly `tile` signals per CTA.
+    block_cfg cfg_tile(int tile) const;
+    std::string describe() const;
+};
+
+template <typename T>
+class complex_engine
+{
+public:
+    enum class kind
+    {
+        trivial,
+        smem,
+        bluestein_smem,
+        fourstep,
+        bluestein_multi
+    };
+
+    explicit complex_engine(long long n);
+
+    // Device scratch (in complex elements) that execute() needs for `batch` signals.
+    long long scratch_elems(long long batch) const;
+    // out/in: `batch` signals, istride/ostride complex elements apart (fourstep and bluestein_multi
+    // require istride == ostride == n).  out may alias in.  scratch: scratch_elems(batch) elements.
+    void execute(void* out, const void* in, long long batch, long long istride, long long ostride, bool inverse,
+                 void* scratch, cudaStream_t st) const;
+    std::string describe() const;
+    kind strategy() const { return k_; }
+    // The one-CTA program (smem: length n; bluestein_smem: length m).
+    const block_program<T>& program() const { return prog_; }
+    long long size() const { return n_; }
+    // Kernel launches one execute() issues (for the launch count reported by the benchmark).
+    int launches(long long batch) const;
+
+private:
+    long long n_;
+    kind k_ = kind::trivial;
+    block_program<T> prog_; // smem: length n; bluestein_smem: length m
+    // Bluestein
+    long long m_ = 0;
+    dbuf chirp_, bhat_;
+    std::unique_ptr<complex_engine<T>> inner_;
+    // four-step
+    long long n1_ = 0, n2_ = 0;
+    block_program<T> pcols_, prows_;
+    int tile_c_ = 1, tile_r_ = 1;
+    dbuf twA_, twB_;
+    int lbits_ = 0;
+
+    void init_bluestein(long long n);
+    bool plan_fourstep(long long n);
+};
+
+// dft_plan_real<T>: N even, N/2-point complex engine plus the CCs/Perm split / merge.
+template <typename T>
+class real_engine
+{
+public:
+    explicit real_engine(long long n);
+    long long scratch_elems(long long batch) const;
+    void forward(void* out, const void* in, long long batch, bool ccs, void* scratch, cudaStream_t st) const;
+    void inverse(void* out, const void* in, long long batch, bool ccs, void* scratch, cudaStream_t st) const;
+    std::string describe() const;
+    long long size() const { return n_; }
+    int launches(long long batch) const;
+
+private:
+    long long n_, c_;
+    complex_engine<T> ceng_;
+    dbuf rtw_;
+    bool fused_ = false;
+};
+
+// dct_plan<T>: DCT-II forward, DCT-III (X0 halved) inverse, unscaled.
+template <typename T>
+class dct_engine
+{
+public:
+    explicit dct_engine(long long n);
+    long long scratch_elems(long long batch) const;
+    void execute(void* out, const void* in, long long batch, bool inverse, void* scratch, cudaStream_t st) const;
+    std::string describe() const;
+    long long size() const { return n_; }
+    int launches(long long batch) const;
+
+private:
+    long long n_;
+    complex_engine<T> ceng_;
+    dbuf dtw_;
+    bool fused_ = false;
+};
+
+} // namespace kfr_gpu

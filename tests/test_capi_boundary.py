@@ -1,0 +1,88 @@
+"""CPU checks of the drop-in boundary: the C-ABI library loads and exports every symbol that
+include/kfr_capi.h declares, the declarations match the reference's C API surface, and the planner's pure
+host logic behaves.  No GPU call is made here."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import kfr_gb300 as k
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# The reference's C API entry points for the DFT path (include/kfr/capi.h:116-736), minus the
+# KFR_MANAGED_ALLOCATION-only helpers (capi.h:178-193), which the reference compiles out by default.
+REFERENCE_DFT_API = [
+    "kfr_version_string", "kfr_version", "kfr_enabled_archs", "kfr_current_arch", "kfr_last_error",
+    "kfr_allocate", "kfr_allocate_aligned", "kfr_deallocate",
+] + [f"kfr_dft_{op}_{p}" for p in ("f32", "f64") for op in (
+    "create_plan", "create_2d_plan", "create_3d_plan", "create_md_plan", "dump", "get_size", "get_temp_size",
+    "execute", "execute_inverse", "delete_plan")] + [f"kfr_dft_real_{op}_{p}" for p in ("f32", "f64") for op in (
+        "create_plan", "create_2d_plan", "create_3d_plan", "create_md_plan", "dump", "get_size", "get_temp_size",
+        "execute", "execute_inverse", "delete_plan")] + [f"kfr_dct_{op}_{p}" for p in ("f32", "f64") for op in (
+            "create_plan", "dump", "get_size", "get_temp_size", "execute", "execute_inverse", "delete_plan")] + [
+    f"kfr_filter_{op}_{p}" for p in ("f32", "f64") for op in (
+        "create_fir_plan", "create_convolution_plan", "create_iir_plan", "process", "reset", "delete_plan")]
+
+
+@pytest.fixture(scope="module")
+def L():
+    if not os.path.exists(k.LIB_PATH):
+        k_build = __import__("kfr_gb300.build", fromlist=["build"])
+        k_build.build()
+    return k.lib()
+
+
+def test_header_declares_reference_api():
+    declared = set(k.declared_symbols())
+    missing = [s for s in REFERENCE_DFT_API if s not in declared]
+    assert not missing, missing
+
+
+def test_library_exports_every_declared_symbol(L):
+    out = os.popen(f"nm -D --defined-only {k.LIB_PATH}").read()
+    exported = set(line.split()[-1] for line in out.splitlines() if line.strip())
+    declared = k.declared_symbols()
+    assert declared, "no declarations parsed"
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    # nothing but the C API leaks out of the library
+    extra = [s for s in exported if not s.startswith("kfr_") and not s.startswith("_init") and not s.startswith("_fini")]
+    assert not extra, extra[:10]
+
+
+def test_reference_header_types_match():
+    """ABI-relevant constants: pack-format values and the default alignment (include/kfr/capi.h:165-200)."""
+    text = open(os.path.join(ROOT, "include", "kfr_capi.h")).read()
+    assert re.search(r"Perm\s*=\s*0", text) and re.search(r"CCs\s*=\s*1", text)
+    assert "#define KFR_DEFAULT_ALIGNMENT 64" in text
+    for t in ("KFR_DFT_PLAN_F32", "KFR_DFT_REAL_PLAN_F64", "KFR_DCT_PLAN_F32", "KFR_FILTER_F64", "KFR_FILTER_C32"):
+        assert f"KFR_OPAQUE_STRUCT({t})" in text
+
+
+def test_version_and_error_convention(L):
+    assert L.kfr_version() == 70001
+    assert k.version_string().startswith("KFR 7.0.1")
+    assert L.kfr_enabled_archs() == b"sm_103a"
+    # NULL handles never crash: size queries return 0 and leave a message
+    assert L.kfr_dft_get_size_f32(None) == 0
+    assert b"NULL" in L.kfr_last_error()
+    L.kfr_dft_delete_plan_f32(None)  # NULL is allowed (capi.h:366)
+    assert L.kfr_last_error() == b""
+
+
+def test_host_allocation_without_gpu(L):
+    p = L.kfr_allocate(1000)
+    assert p and p % 64 == 0
+    ctypes.memset(p, 1, 1000)
+    L.kfr_deallocate(p)
+    p = L.kfr_allocate_aligned(100, 4096)
+    assert p % 4096 == 0
+    L.kfr_deallocate(p)
+    assert L.kfr_last_error() == b""
+
+
+def test_out_of_scope_filters_report_errors(L):
+    assert not L.kfr_filter_create_fir_plan_f32(None, 0)
+    assert b"not part of the GPU DFT path" in L.kfr_last_error()

@@ -1,0 +1,326 @@
+"""GPU parity of the DFT path, called through the C ABI (libkfr_capi.so via the kfr_gb300 ctypes mirror).
+
+Checked against:
+  * the golden fixtures produced by KFR 7.0.1 itself (tests/golden/), at every length they hold;
+  * the CPU oracle (oracle/, pinned to the same fixtures) at lengths and batches the fixtures do not hold.
+Tolerances are the benchmark spec's bounds on relative RMS error against a double-precision reference:
+  c32: 2 * log2(N) * 2^-24        c64: 4 * log2(N) * 2^-53   (N >= 2)
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle.oracle import c32_tolerance, c64_tolerance, rel_rms
+
+torch = pytest.importorskip("torch")
+import kfr_gb300 as k  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def tol(n, sfx):
+    return c32_tolerance(n) if sfx == "f32" else c64_tolerance(n)
+
+
+def cdt(sfx):
+    return np.complex64 if sfx == "f32" else np.complex128
+
+
+def tdt(sfx):
+    return torch.complex64 if sfx == "f32" else torch.complex128
+
+
+def dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+# ------------------------------------------------------------------------------------------------------
+# Complex DFT
+# ------------------------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("sfx", ["f32", "f64"])
+def test_complex_dft_reference_fixtures_host_buffers(sfx):
+    """Single-signal kfr_dft_execute / kfr_dft_execute_inverse with host (numpy) buffers at every fixture
+    length: all radix 2..16 codelets, generic primes 17..61, Bluestein (101, 127, 8191), KFR's 48/60."""
+    g = load_golden("dft_complex.npz")
+    for n in g["sizes"]:
+        n = int(n)
+        plan = k.dft_plan(n, sfx)
+        assert plan.size == n
+        for b in range(g[f"x_{n}"].shape[0]):
+            x = g[f"x_{n}"][b].astype(cdt(sfx))
+            out = np.zeros_like(x)
+            plan.execute(out, x)
+            assert rel_rms(out, g[f"fwd64_{n}"][b]) <= tol(n, sfx), (n, rel_rms(out, g[f"fwd64_{n}"][b]))
+            plan.execute(out, x, inverse=True)
+            assert rel_rms(out, g[f"inv64_{n}"][b]) <= tol(n, sfx), n
+
+
+@pytest.mark.parametrize("sfx", ["f32", "f64"])
+def test_complex_dft_reference_fixtures_device_batched(sfx):
+    g = load_golden("dft_complex.npz")
+    for n in g["sizes"]:
+        n = int(n)
+        x = g[f"x_{n}"].astype(cdt(sfx))
+        xd = dev(x)
+        yd = torch.empty_like(xd)
+        plan = k.dft_plan(n, sfx)
+        plan.execute_batch(yd, xd, x.shape[0])
+        assert rel_rms(yd.cpu().numpy(), g[f"fwd64_{n}"]) <= tol(n, sfx), n
+        plan.execute_batch(yd, xd, x.shape[0], inverse=True)
+        assert rel_rms(yd.cpu().numpy(), g[f"inv64_{n}"]) <= tol(n, sfx), n
+
+
+# lengths x batch: the mixed-radix / prime parity set, multi-signal CTAs, four-step and multi-kernel Bluestein
+BATCHED = [(4096, 64), (1000, 37), (1536, 21), (2187, 15), (30720, 3), (127, 70), (8191, 4), (16384, 3),
+           (65536, 2), (9990, 5), (17 * 19 * 23, 3), (2 * 3 * 5 * 7 * 11 * 13, 2), (1 << 20, 1),
+           (40009, 2), (3 * 65537, 1), (1, 5), (2, 9), (3, 7)]
+
+
+@pytest.mark.parametrize("n,batch", BATCHED)
+@pytest.mark.parametrize("sfx", ["f32", "f64"])
+def test_complex_dft_batched_against_oracle(orc, n, batch, sfx):
+    rng = np.random.default_rng(n * 7 + batch)
+    x = (rng.uniform(-1, 1, (batch, n)) + 1j * rng.uniform(-1, 1, (batch, n))).astype(cdt(sfx))
+    ref = orc.dft(x.astype(np.complex128), threads=8)
+    refi = orc.dft(x.astype(np.complex128), inverse=True, threads=8)
+    plan = k.dft_plan(n, sfx)
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    plan.execute_batch(yd, xd, batch)
+    assert rel_rms(yd.cpu().numpy(), ref) <= tol(n, sfx), (n, rel_rms(yd.cpu().numpy(), ref))
+    plan.execute_batch(yd, xd, batch, inverse=True)
+    assert rel_rms(yd.cpu().numpy(), refi) <= tol(n, sfx), n
+    # in place
+    zd = xd.clone()
+    plan.execute_batch(zd, zd, batch)
+    assert rel_rms(zd.cpu().numpy(), ref) <= tol(n, sfx), n
+
+
+@pytest.mark.parametrize("n", [1 << 24, 30720000])
+def test_complex_dft_large_single(orc, n):
+    """The large single transforms of the mixed-radix parity set (c32)."""
+    rng = np.random.default_rng(n)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    ref = orc.dft(x.astype(np.complex128).reshape(1, n))[0]
+    plan = k.dft_plan(n, "f32")
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    plan.execute(yd, xd)
+    assert rel_rms(yd.cpu().numpy(), ref) <= c32_tolerance(n)
+    # round trip through the inverse: x * N
+    plan.execute(yd, yd, inverse=True)
+    assert rel_rms(yd.cpu().numpy() / n, x) <= 2 * c32_tolerance(n)
+
+
+def test_complex_dft_c64_large(orc):
+    n = 1 << 20
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = orc.dft(x.reshape(1, n))[0]
+    plan = k.dft_plan(n, "f64")
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    plan.execute(yd, xd)
+    assert rel_rms(yd.cpu().numpy(), ref) <= c64_tolerance(n)
+
+
+def test_complex_dft_linearity_and_parseval_full_batch():
+    """Size-independent properties at a full parity-config batch (N=1000, 256 MiB of c32)."""
+    n, batch = 1000, (256 << 20) // (8 * 1000)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    a = torch.randn(batch, n, dtype=torch.complex64, device="cuda", generator=g)
+    b = torch.randn(batch, n, dtype=torch.complex64, device="cuda", generator=g)
+    plan = k.dft_plan(n, "f32")
+    fa, fb, fab = torch.empty_like(a), torch.empty_like(b), torch.empty_like(a)
+    plan.execute_batch(fa, a, batch)
+    plan.execute_batch(fb, b, batch)
+    ab = a + 2 * b
+    plan.execute_batch(fab, ab, batch)
+    err = torch.linalg.vector_norm(fab - (fa + 2 * fb)) / torch.linalg.vector_norm(fab)
+    assert err.item() <= 4 * c32_tolerance(n)
+    # Parseval: sum |X|^2 = N sum |x|^2 (per signal)
+    ea = (a.abs() ** 2).double().sum(dim=1) * n
+    eA = (fa.abs() ** 2).double().sum(dim=1)
+    assert torch.max(torch.abs(eA / ea - 1)).item() < 1e-5
+
+
+def test_plan_queries_and_errors():
+    p = k.dft_plan(4096)
+    assert p.size == 4096 and p.temp_size == 0
+    p2 = k.dft_plan(1 << 20)
+    assert p2.temp_size == (1 << 20) * 8  # four-step intermediate
+    with pytest.raises(k.KfrError, match="even"):
+        k.dft_plan_real(7)
+    L = k.lib()
+    assert L.kfr_dft_get_size_f32(None) == 0 and b"NULL" in L.kfr_last_error()
+
+
+def test_caller_provided_device_temp(orc):
+    n = 1 << 18
+    p = k.dft_plan(n, "f32")
+    temp = torch.empty(p.temp_size, dtype=torch.uint8, device="cuda")
+    rng = np.random.default_rng(9)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    out = np.zeros_like(x)
+    p.execute(out, x, temp=temp)
+    assert rel_rms(out, orc.dft(x.astype(np.complex128).reshape(1, n))[0]) <= c32_tolerance(n)
+
+
+# ------------------------------------------------------------------------------------------------------
+# Real DFT
+# ------------------------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("sfx", ["f32", "f64"])
+def test_real_dft_reference_fixtures(sfx):
+    g = load_golden("dft_real.npz")
+    rdt = np.float32 if sfx == "f32" else np.float64
+    for n in g["sizes"]:
+        n = int(n)
+        for fmt in ("ccs", "perm"):
+            plan = k.dft_plan_real(n, "CCs" if fmt == "ccs" else "Perm", sfx)
+            x = g[f"x_{n}"].astype(rdt)
+            X = np.zeros((x.shape[0], plan.complex_size), dtype=cdt(sfx))
+            for b in range(x.shape[0]):
+                plan.execute(X[b], x[b])
+            assert rel_rms(X, g[f"fwd_{fmt}_{n}"]) <= tol(n, sfx), (n, fmt)
+            S = g[f"spec_{fmt}_{n}"].astype(cdt(sfx))
+            y = np.zeros((S.shape[0], n), dtype=rdt)
+            plan.execute_batch(y, S, S.shape[0], inverse=True)
+            assert rel_rms(y, g[f"inv_{fmt}_{n}"]) <= tol(n, sfx), (n, fmt)
+
+
+@pytest.mark.parametrize("n,batch", [(1920, 40), (44100, 3), (48000, 3), (4096, 33), (2048, 17), (2, 5),
+                                     (1 << 16, 2), (2 * 8191, 3), (40000, 2)])
+@pytest.mark.parametrize("fmt", ["CCs", "Perm"])
+def test_real_dft_batched_against_oracle(orc, n, batch, fmt):
+    rng = np.random.default_rng(n + batch)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    ccs = fmt == "CCs"
+    ref = orc.dft_real(x.astype(np.float64), ccs=ccs, threads=8)
+    plan = k.dft_plan_real(n, fmt, "f32")
+    xd = dev(x)
+    Xd = torch.empty((batch, plan.complex_size), dtype=torch.complex64, device="cuda")
+    plan.execute_batch(Xd, xd, batch)
+    assert rel_rms(Xd.cpu().numpy(), ref) <= c32_tolerance(n), n
+    yd = torch.empty_like(xd)
+    plan.execute_batch(yd, Xd, batch, inverse=True)
+    assert rel_rms(yd.cpu().numpy() / n, x) <= 2 * c32_tolerance(n), n
+
+
+# ------------------------------------------------------------------------------------------------------
+# DCT
+# ------------------------------------------------------------------------------------------------------
+
+def _dct2(x):
+    n = x.shape[-1]
+    kk = np.arange(n)[:, None]
+    m = np.arange(n)[None, :]
+    return x @ np.cos(np.pi * kk * (2 * m + 1) / (2 * n)).T
+
+
+def _dct3(x):
+    n = x.shape[-1]
+    m = np.arange(n)[:, None]
+    kk = np.arange(n)[None, :]
+    w = np.ones(n)
+    w[0] = 0.5
+    return (x * w) @ np.cos(np.pi * kk * (2 * m + 1) / (2 * n)).T
+
+
+@pytest.mark.parametrize("sfx", ["f32", "f64"])
+def test_dct_reference_fixtures(sfx):
+    g = load_golden("dct.npz")
+    rdt = np.float32 if sfx == "f32" else np.float64
+    for n in g["sizes"]:
+        n = int(n)
+        plan = k.dct_plan(n, sfx)
+        x = g[f"x_{n}"].astype(rdt)
+        y = np.zeros_like(x)
+        plan.execute_batch(y, x, x.shape[0])
+        assert rel_rms(y, g[f"fwd_{n}"]) <= 2 * tol(max(n, 2), sfx), n
+        plan.execute_batch(y, x, x.shape[0], inverse=True)
+        assert rel_rms(y, g[f"inv_{n}"]) <= 2 * tol(max(n, 2), sfx), n
+
+
+def test_dct_known_answer_16():
+    """tests/dft_test.cpp:396-423 of the reference."""
+    plan = k.dct_plan(16)
+    x = np.arange(16, dtype=np.float32)
+    y = np.zeros(16, dtype=np.float32)
+    plan.execute(y, x)
+    fwd = np.array([120.0, -51.79283109806667, 0.0, -5.6781471211595695, 0.0, -1.9843883778092053, 0.0,
+                    -0.9603691873838152, 0.0, -0.5308329190495176, 0.0, -0.3030379000702155, 0.0,
+                    -0.1584982220313824, 0.0, -0.0494839805703826])
+    assert np.sqrt(np.mean((y - fwd) ** 2)) < 1e-5
+
+
+@pytest.mark.parametrize("n,batch", [(512, 4096), (600, 7), (1000, 5), (30720, 2), (127, 9), (1, 3), (3, 4)])
+def test_dct_batched_documented_formula(n, batch):
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-1, 1, (batch, n)).astype(np.float32)
+    plan = k.dct_plan(n)
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    x64 = x.astype(np.float64)
+    if n <= 4096:
+        r2, r3 = _dct2(x64), _dct3(x64)
+    else:
+        from oracle.oracle import Oracle
+        o = Oracle("orc")
+        r2, r3 = o.dct(x64), o.dct(x64, inverse=True)
+    plan.execute_batch(yd, xd, batch)
+    assert rel_rms(yd.cpu().numpy(), r2) <= 2 * c32_tolerance(max(n, 2)), n
+    plan.execute_batch(yd, xd, batch, inverse=True)
+    assert rel_rms(yd.cpu().numpy(), r3) <= 2 * c32_tolerance(max(n, 2)), n
+
+
+# ------------------------------------------------------------------------------------------------------
+# FFT convolution filter
+# ------------------------------------------------------------------------------------------------------
+
+def test_convolve_filter_known_answer():
+    """tests/dft_test.cpp:127-135 of the reference."""
+    f = k.convolve_filter(np.array([1, 2, 3, 4, 5], dtype=np.float32))
+    x = np.array([0.25, 0.5, 1.0, -2.0, 1.5], dtype=np.float32)
+    y = np.zeros(5, dtype=np.float32)
+    f.apply(y, x)
+    assert np.sqrt(np.mean((y - np.array([0.25, 1.0, 2.75, 2.5, 3.75])) ** 2)) < 1e-4
+
+
+@pytest.mark.parametrize("sfx", ["f32", "f64"])
+def test_convolve_filter_streaming_fixtures(sfx):
+    """Streaming with uneven chunks, state across calls, then reset() (real filters: the C API's)."""
+    g = load_golden("convolution.npz")
+    rdt = np.float32 if sfx == "f32" else np.float64
+    for i in range(int(g["nfilters"])):
+        taps = g[f"ftaps_real_{i}"].astype(rdt)
+        f = k.convolve_filter(taps, int(g[f"fblock_real_{i}"]))
+        for j in range(int(g[f"fnchunks_real_{i}"])):
+            x = g[f"fin_real_{i}_{j}"].astype(rdt)
+            y = np.zeros_like(x)
+            f.apply(y, x)
+            assert rel_rms(y, g[f"fout_real_{i}_{j}"]) <= 8 * tol(len(taps) + len(x), sfx), (i, j)
+        f.reset()
+        x = g[f"fin_real_{i}_reset"].astype(rdt)
+        y = np.zeros_like(x)
+        f.apply(y, x)
+        assert rel_rms(y, g[f"fout_real_{i}_reset"]) <= 8 * tol(len(taps) + len(x), sfx), i
+
+
+def test_convolve_filter_long_signal_device(orc):
+    """1023-tap filter over 2^18 samples in device memory, against the streaming oracle."""
+    rng = np.random.default_rng(11)
+    taps = rng.standard_normal(1023).astype(np.float32)
+    x = rng.standard_normal(1 << 18).astype(np.float32)
+    ref = orc.filter(taps.astype(np.float64), 1024).process(x.astype(np.float64))
+    f = k.convolve_filter(taps, 1024)
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    f.apply(yd, xd)
+    assert rel_rms(yd.cpu().numpy(), ref) <= 8 * c32_tolerance(1 << 18)
+    # in place on the device
+    f.reset()
+    zd = xd.clone()
+    f.apply(zd, zd)
+    assert rel_rms(zd.cpu().numpy(), ref) <= 8 * c32_tolerance(1 << 18)
