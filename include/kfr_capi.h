@@ -239,6 +239,28 @@ KFR_API_SPEC void kfr_dct_execute_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
 
+/* Allocation-free execution (no counterpart in the reference).
+ *
+ * Same transform as kfr_dft_execute_batch_f32, for callers that must not allocate GPU memory while they
+ * run: real-time audio or control threads, code inside CUDA stream capture, and hosts that reserve all
+ * device memory up front.  kfr_dft_execute_batch_f32 allocates plan-owned scratch on first use (and
+ * staging buffers for host pointers); this entry point never calls cudaMalloc, cudaFree or any other
+ * allocating routine.  Plans whose length needs scratch (the two-pass path for long transforms and the
+ * multi-kernel Bluestein path) use one fixed device array of KFR_STATIC_SCRATCH_BYTES that the library
+ * holds on every GPU it runs on until the process exits.
+ *   - in and out must be device pointers (host pointers would need staging buffers): error otherwise;
+ *   - batch * the plan's per-signal scratch must fit KFR_STATIC_SCRATCH_BYTES: error otherwise
+ *     (kfr_dft_get_temp_size_batch_f32 gives the requirement);
+ *   - stream: NULL = synchronous on the default stream, else a cudaStream_t the work is enqueued on;
+ *   - the first call on each device does the one-time set-up (looks up the array's device address, which
+ *     also loads this library's device code there): make that first call before any stream capture;
+ *   - every call shares the one array and no call needs it cleared; calls that overlap on the GPU (on
+ *     different streams, or from different threads) race on it and must be serialised by the caller.
+ * Errors are reported through kfr_last_error() like every other entry point. */
+#define KFR_STATIC_SCRATCH_BYTES (32u << 20)
+KFR_API_SPEC void kfr_dft_execute_static_scratch_f32(KFR_DFT_PLAN_F32* plan, size_t batch, kfr_c32* out,
+                                                     const kfr_c32* in, kfr_bool inverse, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,7 @@ _SIGS.update({
     "kfr_allocate_aligned": (_P, [_S, _S]),
     "kfr_deallocate": (None, [_P]),
     "kfr_dft_get_launch_count_f32": (_S, [_P, _S]),
+    "kfr_dft_execute_static_scratch_f32": (None, [_P, _S, _P, _P, _B, _P]),
 })
 
 

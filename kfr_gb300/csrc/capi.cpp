@@ -497,6 +497,41 @@ KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t 
 {
     return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.launches(batch)); }, size_t(0));
 }
+
+} // extern "C"
+
+namespace kfr_gpu
+{
+// Body of kfr_dft_execute_static_scratch_f32 (static_scratch.cu owns the scratch array and passes its
+// device address through `scratch_of`).  Nothing here allocates: no staging, no plan-owned scratch.
+void run_static_scratch_f32(void* plan, size_t batch, void* out, const void* in, bool inverse, void* stream,
+                            void* (*scratch_of)(), size_t scratch_limit)
+{
+    try_void(
+        [&]
+        {
+            auto* p = as<dft_obj<float>>(plan, TAG_DFT_F32);
+            if (batch == 0 || p->n == 0)
+                return;
+            if (!is_device_ptr(in) || !is_device_ptr(out))
+                throw std::invalid_argument("kfr_dft_execute_static_scratch_f32 needs device pointers for in and out");
+            const size_t need = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(float);
+            if (need > scratch_limit)
+                throw std::invalid_argument("kfr_dft_execute_static_scratch_f32: this plan and batch need " +
+                                            std::to_string(need) + " bytes of scratch, more than the " +
+                                            std::to_string(scratch_limit) + "-byte static scratch");
+            void* scr       = need ? scratch_of() : nullptr;
+            cudaStream_t st = static_cast<cudaStream_t>(stream);
+            p->eng.execute(out, in, (long long)batch, (long long)p->n, (long long)p->n, inverse, scr, st);
+            check(cudaGetLastError(), "kernel launch");
+            if (!stream)
+                check(cudaStreamSynchronize(st), "execute");
+        });
+}
+} // namespace kfr_gpu
+
+extern "C"
+{
 KFR_API_SPEC void kfr_dft_delete_plan_f32(KFR_DFT_PLAN_F32* plan)
 {
     try_void([&] { if (plan) delete as<dft_obj<float>>(plan, TAG_DFT_F32); });
