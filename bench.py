@@ -203,7 +203,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--sizes", type=str, default=None, help="comma-separated subset of the lengths (profiling)")
+    ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
     args = ap.parse_args()
+    global SIZES, BYTES_PER_SIZE
+    if args.sizes:
+        SIZES = [int(v) for v in args.sizes.split(",")]
+    if args.batch_mib:
+        BYTES_PER_SIZE = args.batch_mib << 20
     if args.impl == "reference":
         return run_reference(args)
 

@@ -27,7 +27,10 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "elementwise.cu", "conv.cu", "static_scratch.cu"]
+CU_SOURCES = [
+    "kernels_f32.cu", "kernels_f64.cu", "kernels_ct_a.cu", "kernels_ct_b.cu", "kernels_ct_c.cu", "elementwise.cu",
+    "conv.cu", "static_scratch.cu",
+]
 CPP_SOURCES = ["plan.cpp", "capi.cpp"]
 
 

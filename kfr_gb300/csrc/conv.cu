@@ -1,18 +1,12 @@
 // FFT convolution filter kernels and host class (see conv.hpp).
 #include "conv.hpp"
-#include "fft_device.cuh"
+#include "kernels.cuh"
 
 #include <algorithm>
 #include <vector>
 
 namespace kfr_gpu
 {
-
-template <typename T, int EPT>
-struct conv_bounds
-{
-    static constexpr int threads = (sizeof(T) == 4 ? 1024 : 512) / (EPT / 16);
-};
 
 // Real-DFT split of bins (k, c-k) from the c-point complex spectrum of the packed reals.
 template <typename T>
@@ -30,14 +24,14 @@ __device__ __forceinline__ cpx<T> rmerge(cpx<T> yk, cpx<T> ykk, cpx<T> w)
 }
 
 // One overlap-save block per CTA: blockIdx.x = output block, blockIdx.y = channel.
-template <typename T, int EPT>
-__global__ void __launch_bounds__(conv_bounds<T, EPT>::threads, 1) k_conv_os(const conv_args a, const int ts)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_conv_os(const conv_args a, const int ts)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm       = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int c      = a.d.n;
+    const int c      = fft.n;
     const long long b = blockIdx.x;
     const int ch     = blockIdx.y;
     const T* in      = reinterpret_cast<const T*>(a.in) + (long long)ch * a.n;
@@ -58,7 +52,7 @@ __global__ void __launch_bounds__(conv_bounds<T, EPT>::threads, 1) k_conv_os(con
     __syncthreads();
     const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
     const int lt     = int(threadIdx.x) < ts ? int(threadIdx.x) : ts;
-    block_fft<T, EPT>(sm, sp, a.d.npass, c, tw, lt, ts);
+    fft.run(sm, tw, lt);
     const cpx<T>* H   = reinterpret_cast<const cpx<T>*>(a.hspec);
     const cpx<T>* rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
     for (int k = threadIdx.x; k <= c / 2; k += blockDim.x)
@@ -85,7 +79,7 @@ __global__ void __launch_bounds__(conv_bounds<T, EPT>::threads, 1) k_conv_os(con
         }
     }
     __syncthreads();
-    block_fft<T, EPT>(sm, sp, a.d.npass, c, tw, lt, ts);
+    fft.run(sm, tw, lt);
     for (long long t = threadIdx.x; t < a.bo; t += blockDim.x)
     {
         const long long no = base + t;
@@ -116,35 +110,25 @@ template <typename T>
 cudaError_t launch_conv_os(const conv_args& a, const block_cfg& c, long long nblocks, cudaStream_t st)
 {
     const dim3 grid(unsigned(nblocks), unsigned(a.channels));
-    switch (c.ept)
+    if (c.ct)
     {
-    case 16:
-    {
-        auto k = k_conv_os<T, 16>;
-        if (c.smem > 48 * 1024)
+        if constexpr (std::is_same<T, float>::value)
         {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem);
-            if (e != cudaSuccess)
-                return e;
+#define CT_KERNEL k_conv_os
+#define CT_GRID grid
+#define CT_ARGS a, c.ts
+            switch (c.ct)
+            {
+                KFR_CT_CONV_F32(KFR_GPU_CT_CASE)
+            default: return cudaErrorInvalidValue;
+            }
+#undef CT_KERNEL
+#undef CT_GRID
+#undef CT_ARGS
         }
-        k<<<grid, c.threads, c.smem, st>>>(a, c.ts);
-        break;
+        return cudaErrorInvalidValue;
     }
-    case 32:
-    {
-        auto k = k_conv_os<T, 32>;
-        if (c.smem > 48 * 1024)
-        {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem);
-            if (e != cudaSuccess)
-                return e;
-        }
-        k<<<grid, c.threads, c.smem, st>>>(a, c.ts);
-        break;
-    }
-    default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+    KFR_GPU_RUNTIME_DISPATCH(k_conv_os, grid, a, c.ts)
 }
 
 template <typename T>
@@ -206,7 +190,7 @@ conv_filter<T>::conv_filter(const T* taps, size_t ntaps, size_t block_size, int 
     f_  = f;
     c_  = f / 2;
     bo_ = f - m1;
-    prog_.build(int(c_));
+    prog_.build(int(c_), CT_CONV);
     // taps spectrum FFT_F(h padded) / F, bins 0..c (set_data, src/dft/convolution-impl.cpp:53-71)
     std::vector<std::complex<double>> a(f, { 0.0, 0.0 });
     for (size_t i = 0; i < ntaps; i++)

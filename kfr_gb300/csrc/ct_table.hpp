@@ -1,0 +1,63 @@
+// Lengths with compile-time specialised block FFTs (single precision).  Each entry is
+//   X(N, TS, radices...)   N = product of the radices, TS = threads per signal
+// chosen so that no thread holds more than 16 complex values in any pass.  The planner uses an entry when
+// the kernel kind and length match (block_program::build then lays the twiddles out in this radix order);
+// every other length runs the runtime-radix kernel.  Lists are per kernel kind to bound compile time:
+// they cover the parity and benchmark configurations and the power-of-two lengths up to 16384.
+#pragma once
+
+// complex DFT of one-CTA lengths (dft_plan<float>)
+#define KFR_CT_C2C_F32(X)                                                                                   \
+    X(64, 4, 16, 4)                                                                                          \
+    X(128, 8, 16, 8)                                                                                         \
+    X(256, 16, 16, 16)                                                                                       \
+    X(512, 64, 8, 8, 8)                                                                                      \
+    X(1000, 128, 8, 5, 5, 5)                                                                                 \
+    X(1024, 64, 16, 16, 4)                                                                                   \
+    X(1536, 192, 8, 8, 8, 3)                                                                                 \
+    X(2048, 128, 16, 16, 8)                                                                                  \
+    X(2187, 243, 9, 9, 9, 3)                                                                                 \
+    X(4096, 256, 16, 16, 16)                                                                                 \
+    X(8192, 512, 16, 16, 16, 2)                                                                              \
+    X(16384, 1024, 16, 16, 16, 4)
+
+// convolution lengths M = next_pow2(2N - 1) of the one-CTA Bluestein kernel (any N with that M)
+#define KFR_CT_BLUESTEIN_F32(X)                                                                             \
+    X(256, 16, 16, 16)                                                                                       \
+    X(512, 64, 8, 8, 8)                                                                                      \
+    X(1024, 64, 16, 16, 4)                                                                                   \
+    X(2048, 128, 16, 16, 8)                                                                                  \
+    X(4096, 256, 16, 16, 16)                                                                                 \
+    X(8192, 512, 16, 16, 16, 2)                                                                              \
+    X(16384, 1024, 16, 16, 16, 4)
+
+// four-step pass lengths (columns and rows): the factors of 30720 = 160 x 192 and of the power-of-two
+// lengths 2^15 .. 2^24
+#define KFR_CT_FOURSTEP_F32(X)                                                                              \
+    X(128, 8, 16, 8)                                                                                         \
+    X(160, 32, 8, 4, 5)                                                                                      \
+    X(192, 16, 16, 4, 3)                                                                                     \
+    X(256, 16, 16, 16)                                                                                       \
+    X(512, 64, 8, 8, 8)                                                                                      \
+    X(1024, 64, 16, 16, 4)                                                                                   \
+    X(2048, 128, 16, 16, 8)                                                                                  \
+    X(4096, 256, 16, 16, 16)
+
+// half lengths c = N/2 of the fused real DFT (dft_plan_real<float>): N = 1920, 2048, 4096, 8192
+#define KFR_CT_REAL_F32(X)                                                                                  \
+    X(960, 64, 16, 4, 3, 5)                                                                                  \
+    X(1024, 64, 16, 16, 4)                                                                                   \
+    X(2048, 128, 16, 16, 8)                                                                                  \
+    X(4096, 256, 16, 16, 16)
+
+// DCT lengths (dct_plan<float>)
+#define KFR_CT_DCT_F32(X)                                                                                   \
+    X(512, 64, 8, 8, 8)                                                                                      \
+    X(1024, 64, 16, 16, 4)                                                                                   \
+    X(4096, 256, 16, 16, 16)
+
+// half FFT lengths c = F/2 of the overlap-save convolution kernel (F = 2048, 4096, 8192)
+#define KFR_CT_CONV_F32(X)                                                                                  \
+    X(1024, 64, 16, 16, 4)                                                                                   \
+    X(2048, 128, 16, 16, 8)                                                                                  \
+    X(4096, 256, 16, 16, 16)

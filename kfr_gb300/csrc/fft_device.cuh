@@ -483,6 +483,86 @@ __device__ __forceinline__ void block_fft(cpx<T>* buf, const pass_desc* sp, cons
     }
 }
 
+// --------------------------------------------------------------------------------------------------
+// Compile-time block FFT: the same Stockham passes for a length and radix sequence fixed at compile time,
+// so every index, divisor and twiddle offset folds to a constant and each pass's butterfly loop unrolls.
+// Used for the lengths listed in ct_table.hpp; the twiddle table layout matches block_program::build with
+// the same radix order.
+// --------------------------------------------------------------------------------------------------
+
+template <int N, int TS, int R>
+__host__ __device__ constexpr int ct_nb()
+{
+    return (N / R + TS - 1) / TS;
+}
+template <int N, int TS, int... Rs>
+__host__ __device__ constexpr int ct_ept()
+{
+    int e = 1;
+    ((e = (ct_nb<N, TS, Rs>() * Rs > e ? ct_nb<N, TS, Rs>() * Rs : e)), ...);
+    return e;
+}
+
+template <typename T, int N, int TS, int EPT, int R, int NS, int TWOFF>
+__device__ __forceinline__ void ct_pass(cpx<T> (&v)[EPT], cpx<T>* buf, const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int NBF = N / R;
+    constexpr int NB  = (NBF + TS - 1) / TS;
+    static_assert(NB * R <= EPT, "register array too small");
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[b * R + r] = buf[pidx<T>(j + r * NBF)];
+            if constexpr (NS > 1)
+            {
+                const int k     = j % NS;
+                const cpx<T>* t = tw + TWOFF + k;
+#pragma unroll
+                for (int r = 1; r < R; r++)
+                    v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * NS);
+            }
+            dft_codelet<T, R>(&v[b * R]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+            const int k = NS > 1 ? j % NS : 0;
+            const int d = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                buf[pidx<T>(d + r * NS)] = v[b * R + codelet_out<R>(r)];
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int N, int TS, int EPT, int NS, int TWOFF, int R, int... Rest>
+__device__ __forceinline__ void ct_passes(cpx<T> (&v)[EPT], cpx<T>* buf, const cpx<T>* __restrict__ tw, const int lt)
+{
+    ct_pass<T, N, TS, EPT, R, NS, TWOFF>(v, buf, tw, lt);
+    if constexpr (sizeof...(Rest) > 0)
+        ct_passes<T, N, TS, EPT, NS * R, TWOFF + (NS > 1 ? NS * (R - 1) : 0), Rest...>(v, buf, tw, lt);
+}
+
+template <typename T, int N, int TS, int... Rs>
+__device__ __forceinline__ void ct_block_fft(cpx<T>* buf, const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int EPT = ct_ept<N, TS, Rs...>();
+    const int lta     = lt < TS ? lt : N;
+    cpx<T> v[EPT];
+    ct_passes<T, N, TS, EPT, 1, 0, Rs...>(v, buf, tw, lta);
+}
+
 // Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a
 // barrier.
 __device__ __forceinline__ void stage_passes(pass_desc* sp, const fft_desc& d)

@@ -6,17 +6,47 @@
 // (include/kfr/dft/fft.hpp:262: no scaling), so only forward codelets and forward twiddles exist.
 #pragma once
 
+#include <type_traits>
+
+#include "ct_table.hpp"
 #include "fft_device.cuh"
 #include "launch.hpp"
 
 namespace kfr_gpu
 {
 
-// Largest CTA for a (precision, EPT) pair: the block FFT keeps EPT complex values per thread in registers.
+// FFT policies.  A kernel is instantiated with one of them:
+//   rt_fft<T, EPT>          runtime radix sequence (any one-CTA length), pass list staged in shared memory
+//   ct_fft<T, N, TS, Rs...> compile-time length and radices (ct_table.hpp)
+// Both expose n (length), ts (threads per signal), max_threads (launch bound) and run(buf, tw, lt).
 template <typename T, int EPT>
-struct ept_bounds
+struct rt_fft
 {
-    static constexpr int threads = (sizeof(T) == 4 ? 1024 : 512) / (EPT / 16);
+    // the block FFT keeps EPT complex values per thread in registers
+    static constexpr int max_threads = (sizeof(T) == 4 ? 1024 : 512) / (EPT / 16);
+    const pass_desc* sp;
+    int npass, n, ts;
+    __device__ __forceinline__ rt_fft(pass_desc* s, const fft_desc& d, int ts_) : sp(s), npass(d.npass), n(d.n), ts(ts_)
+    {
+        stage_passes(s, d);
+    }
+    __device__ __forceinline__ void run(cpx<T>* buf, const cpx<T>* __restrict__ tw, int lt) const
+    {
+        block_fft<T, EPT>(buf, sp, npass, n, tw, lt, ts);
+    }
+};
+
+template <typename T, int N, int TS, int... Rs>
+struct ct_fft
+{
+    static constexpr int max_threads = sizeof(T) == 4 ? 1024 : 512;
+    static constexpr int n           = N;
+    static constexpr int ts          = TS;
+    __device__ __forceinline__ ct_fft(pass_desc*, const fft_desc&, int) {}
+    __device__ __forceinline__ void run(cpx<T>* buf, const cpx<T>* __restrict__ tw, int lt) const
+    {
+        ct_block_fft<T, N, TS, Rs...>(buf, tw, lt);
+    }
 };
 
 __device__ __forceinline__ uint32_t div_by(uint32_t x, const fast_div f) { return fdiv(x, f); }
@@ -37,14 +67,14 @@ struct group_map
 // ---------------------------------------------------------------------------------------------------
 // Complex DFT, contiguous batch (dft_plan<T>::execute over many signals)
 // ---------------------------------------------------------------------------------------------------
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2c(const c2c_args a, const int ts, const int spc)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_c2c(const c2c_args a, const int ts, const int spc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int n       = a.d.n;
+    const int n       = fft.n;
     const int stride  = padded_len<T>(n);
     const long long s0 = (long long)blockIdx.x * spc;
     const cpx<T>* __restrict__ in = reinterpret_cast<const cpx<T>*>(a.in);
@@ -62,7 +92,7 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2c(const c2
     }
     __syncthreads();
     const group_map gm(ts, spc);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
 #pragma unroll 4
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {
@@ -78,15 +108,15 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2c(const c2
 // Bluestein (dft_arblen_stage_impl, src/dft/dft-impl.hpp:248-272), fused into one kernel:
 //   a = x * chirp (zero padded to M) -> FFT_M -> * bhat -> inverse FFT_M -> * chirp
 // ---------------------------------------------------------------------------------------------------
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_bluestein(const bluestein_args a, const int ts,
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_bluestein(const bluestein_args a, const int ts,
                                                                         const int spc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int m       = a.d.n;
+    const int m       = fft.n;
     const int n       = a.n;
     const int stride  = padded_len<T>(m);
     const long long s0 = (long long)blockIdx.x * spc;
@@ -108,7 +138,7 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_bluestein(co
     __syncthreads();
     const group_map gm(ts, spc);
     const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, tw, gm.lt, ts);
+    fft.run(sm + gm.g * stride, tw, gm.lt);
     for (int i = threadIdx.x; i < spc * m; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_m));
@@ -117,7 +147,7 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_bluestein(co
         r           = conj(r * ldg(bhat + e));
     }
     __syncthreads();
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, tw, gm.lt, ts);
+    fft.run(sm + gm.g * stride, tw, gm.lt);
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -132,14 +162,14 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_bluestein(co
 // Real forward DFT (dft_plan_real, CCs / Perm): c-point complex DFT of the reals viewed as c complex
 // values, then the split of to_fmt (src/dft/fft-impl.hpp:1799-1841) fused into the store.
 // ---------------------------------------------------------------------------------------------------
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_r2c(const real_args a, const int ts, const int spc)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_r2c(const real_args a, const int ts, const int spc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int c       = a.d.n;
+    const int c       = fft.n;
     const int stride  = padded_len<T>(c);
     const long long s0 = (long long)blockIdx.x * spc;
     const T* __restrict__ inr      = reinterpret_cast<const T*>(a.in);
@@ -155,7 +185,7 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_r2c(const re
     }
     __syncthreads();
     const group_map gm(ts, spc);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     const int olen = a.ccs ? c + 1 : c;
     for (int i = threadIdx.x; i < spc * olen; i += blockDim.x)
     {
@@ -193,14 +223,14 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_r2c(const re
 // unscaled inverse c-point complex DFT whose output is the 2c reals.  Only the real parts of the DC and
 // Nyquist bins are read, as in the reference.
 // ---------------------------------------------------------------------------------------------------
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2r(const real_args a, const int ts, const int spc)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_c2r(const real_args a, const int ts, const int spc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int c       = a.d.n;
+    const int c       = fft.n;
     const int stride  = padded_len<T>(c);
     const long long s0 = (long long)blockIdx.x * spc;
     const cpx<T>* __restrict__ in  = reinterpret_cast<const cpx<T>*>(a.in);
@@ -233,7 +263,7 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2r(const re
     }
     __syncthreads();
     const group_map gm(ts, spc);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     for (int i = threadIdx.x; i < spc * c; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -248,14 +278,14 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_c2r(const re
 // DCT-II (dct_plan::execute, include/kfr/dft/fft.hpp:938-950): even/odd mirror on load, n-point DFT,
 // Re*cos + Im*sin on store.
 // ---------------------------------------------------------------------------------------------------
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_dct2(const dct_args a, const int ts, const int spc)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_dct2(const dct_args a, const int ts, const int spc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int n       = a.d.n;
+    const int n       = fft.n;
     const int stride  = padded_len<T>(n);
     const long long s0 = (long long)blockIdx.x * spc;
     const T* __restrict__ in       = reinterpret_cast<const T*>(a.in);
@@ -273,7 +303,7 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_dct2(const d
     }
     __syncthreads();
     const group_map gm(ts, spc);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -289,14 +319,14 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_dct2(const d
 
 // DCT-III, the reference's "inverse" (include/kfr/dft/fft.hpp:951-969): x_k * e^{-i pi k / 2n}, X0 halved,
 // forward n-point DFT, un-mirror the real parts.
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_dct3(const dct_args a, const int ts, const int spc)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_dct3(const dct_args a, const int ts, const int spc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int n       = a.d.n;
+    const int n       = fft.n;
     const int stride  = padded_len<T>(n);
     const long long s0 = (long long)blockIdx.x * spc;
     const T* __restrict__ in       = reinterpret_cast<const T*>(a.in);
@@ -318,7 +348,7 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_dct3(const d
     }
     __syncthreads();
     const group_map gm(ts, spc);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s   = int(div_by(uint32_t(i), a.div_n));
@@ -341,14 +371,14 @@ __device__ __forceinline__ cpx<T> twiddle_2level(const cpx<T>* __restrict__ A, c
     return ldg(A + (m >> lbits)) * ldg(B + (m & ((1LL << lbits) - 1)));
 }
 
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_fs_cols(const fourstep_args a, const int ts)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_fs_cols(const fourstep_args a, const int ts)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm       = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int n1     = a.n1, n2 = a.n2, S = a.tile;
+    const int n1     = fft.n, n2 = a.n2, S = a.tile, sh = a.tile_shift;
     const int stride = padded_len<T>(n1);
     const int c0     = blockIdx.x * S;
     const long long sig = blockIdx.y;
@@ -358,14 +388,14 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_fs_cols(cons
     const int total = S * n1;
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {
-        const int n1i = i / S; // S is a power of two
-        const int c   = i - n1i * S;
+        const int n1i = i >> sh; // S is a power of two
+        const int c   = i & (S - 1);
         if (c0 + c < n2)
             sm[c * stride + pidx<T>(n1i)] = conj_if(x[(long long)n1i * n2 + c0 + c], cin);
     }
     __syncthreads();
     const group_map gm(ts, S);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     const cpx<T>* twA = reinterpret_cast<const cpx<T>*>(a.twA);
     const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
     for (int i = threadIdx.x; i < total; i += blockDim.x)
@@ -382,14 +412,14 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_fs_cols(cons
     }
 }
 
-template <typename T, int EPT>
-__global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_fs_rows(const fourstep_args a, const int ts)
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_fs_rows(const fourstep_args a, const int ts)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ pass_desc sp[kMaxPasses];
-    stage_passes(sp, a.d);
+    const F fft(sp, a.d, ts);
     cpx<T>* sm       = reinterpret_cast<cpx<T>*>(smem_raw);
-    const int n1     = a.n1, n2 = a.n2, S = a.tile;
+    const int n1     = a.n1, n2 = fft.n, S = a.tile, sh = a.tile_shift;
     const int stride = padded_len<T>(n2);
     const int r0     = blockIdx.x * S;
     const long long sig = blockIdx.y;
@@ -399,106 +429,114 @@ __global__ void __launch_bounds__(ept_bounds<T, EPT>::threads, 1) k_fs_rows(cons
     const bool cin  = a.conj_in != 0;
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {
-        const int n2i = i / S;
-        const int r   = i - n2i * S;
+        const int n2i = i >> sh;
+        const int r   = i & (S - 1);
         if (r0 + r < n1)
             sm[r * stride + pidx<T>(n2i)] = conj_if(y[(long long)n2i * n1 + r0 + r], cin);
     }
     __syncthreads();
     const group_map gm(ts, S);
-    block_fft<T, EPT>(sm + gm.g * stride, sp, a.d.npass, a.d.n, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt, ts);
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     const bool cout = a.conj_out != 0;
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {
-        const int k2 = i / S;
-        const int r  = i - k2 * S;
+        const int k2 = i >> sh;
+        const int r  = i & (S - 1);
         if (r0 + r < n1)
             X[(long long)(r0 + r) + (long long)n1 * k2] = conj_if(sm[r * stride + pidx<T>(k2)], cout);
     }
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Launchers
+// Launchers.  A block_cfg with ct != 0 selects the compile-time kernel of that length (single precision,
+// launched by the launch_ct_* functions of kernels_ct_*.cu); otherwise cfg.ept picks the runtime kernel.
 // ---------------------------------------------------------------------------------------------------
 
-template <typename K>
-static cudaError_t prepare_smem(K kernel, int bytes)
+template <typename K, typename... Args>
+static cudaError_t go(K kernel, dim3 grid, const block_cfg& c, cudaStream_t st, Args... args)
 {
-    if (bytes > 48 * 1024)
-        return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    return cudaSuccess;
+    if (c.smem > 48 * 1024)
+    {
+        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    kernel<<<grid, c.threads, c.smem, st>>>(args...);
+    return cudaGetLastError();
 }
 
-#define KFR_GPU_DISPATCH_EPT(KERNEL, ARGS, ...)                                                            \
+#define KFR_GPU_RUNTIME_DISPATCH(KERNEL, GRID, ...)                                                        \
     switch (c.ept)                                                                                         \
     {                                                                                                      \
-    case 16:                                                                                               \
-    {                                                                                                      \
-        auto k = KERNEL<T, 16>;                                                                            \
-        cudaError_t e = prepare_smem(k, c.smem);                                                           \
-        if (e != cudaSuccess)                                                                              \
-            return e;                                                                                      \
-        k<<<ARGS>>>(__VA_ARGS__);                                                                          \
-        break;                                                                                             \
-    }                                                                                                      \
-    case 32:                                                                                               \
-    {                                                                                                      \
-        auto k = KERNEL<T, 32>;                                                                            \
-        cudaError_t e = prepare_smem(k, c.smem);                                                           \
-        if (e != cudaSuccess)                                                                              \
-            return e;                                                                                      \
-        k<<<ARGS>>>(__VA_ARGS__);                                                                          \
-        break;                                                                                             \
-    }                                                                                                      \
+    case 16: return go(KERNEL<T, rt_fft<T, 16>>, GRID, c, st, __VA_ARGS__);                                \
+    case 32: return go(KERNEL<T, rt_fft<T, 32>>, GRID, c, st, __VA_ARGS__);                                \
     default: return cudaErrorInvalidValue;                                                                 \
-    }                                                                                                      \
-    return cudaGetLastError();
+    }
 
-#define KFR_GPU_LAUNCH1 dim3(unsigned(c.grid)), c.threads, c.smem, st
+#define KFR_GPU_CT_HOOK(CTFN)                                                                              \
+    if (c.ct)                                                                                              \
+    {                                                                                                      \
+        if constexpr (std::is_same<T, float>::value)                                                       \
+            return CTFN(a, c, st);                                                                         \
+        else                                                                                               \
+            return cudaErrorInvalidValue;                                                                  \
+    }
+
+#define KFR_GPU_GRID1 dim3(unsigned(c.grid))
+#define KFR_GPU_GRID2 dim3(unsigned(c.grid), unsigned(a.batch))
 
 template <typename T>
 cudaError_t launch_c2c(const c2c_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_c2c, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+    KFR_GPU_CT_HOOK(launch_ct_c2c_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_c2c, KFR_GPU_GRID1, a, c.ts, c.spc)
 }
 template <typename T>
 cudaError_t launch_bluestein(const bluestein_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_bluestein, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+    KFR_GPU_CT_HOOK(launch_ct_bluestein_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_bluestein, KFR_GPU_GRID1, a, c.ts, c.spc)
 }
 template <typename T>
 cudaError_t launch_r2c(const real_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_r2c, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+    KFR_GPU_CT_HOOK(launch_ct_r2c_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_r2c, KFR_GPU_GRID1, a, c.ts, c.spc)
 }
 template <typename T>
 cudaError_t launch_c2r(const real_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_c2r, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+    KFR_GPU_CT_HOOK(launch_ct_c2r_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_c2r, KFR_GPU_GRID1, a, c.ts, c.spc)
 }
 template <typename T>
 cudaError_t launch_dct2(const dct_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_dct2, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+    KFR_GPU_CT_HOOK(launch_ct_dct2_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_dct2, KFR_GPU_GRID1, a, c.ts, c.spc)
 }
 template <typename T>
 cudaError_t launch_dct3(const dct_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_dct3, KFR_GPU_LAUNCH1, a, c.ts, c.spc)
+    KFR_GPU_CT_HOOK(launch_ct_dct3_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_dct3, KFR_GPU_GRID1, a, c.ts, c.spc)
 }
-
-#define KFR_GPU_LAUNCH2 dim3(unsigned(c.grid), unsigned(a.batch)), c.threads, c.smem, st
-
 template <typename T>
 cudaError_t launch_fs_cols(const fourstep_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_fs_cols, KFR_GPU_LAUNCH2, a, c.ts)
+    KFR_GPU_CT_HOOK(launch_ct_fs_cols_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_fs_cols, KFR_GPU_GRID2, a, c.ts)
 }
 template <typename T>
 cudaError_t launch_fs_rows(const fourstep_args& a, const block_cfg& c, cudaStream_t st)
 {
-    KFR_GPU_DISPATCH_EPT(k_fs_rows, KFR_GPU_LAUNCH2, a, c.ts)
+    KFR_GPU_CT_HOOK(launch_ct_fs_rows_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_fs_rows, KFR_GPU_GRID2, a, c.ts)
 }
+
+// Compile-time kernel cases for the launch_ct_* functions: CT_KERNEL and CT_ARGS are defined by the caller.
+#define KFR_GPU_CT_CASE(N, TS, ...)                                                                        \
+    case N: return go(CT_KERNEL<float, ct_fft<float, N, TS, __VA_ARGS__>>, CT_GRID, c, st, CT_ARGS);
 
 #define KFR_GPU_INSTANTIATE(T)                                                                             \
     template cudaError_t launch_c2c<T>(const c2c_args&, const block_cfg&, cudaStream_t);                   \

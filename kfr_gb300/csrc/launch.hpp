@@ -20,6 +20,7 @@ struct block_cfg
     int threads;
     int smem;
     long long grid;
+    int ct = 0; // nonzero: length of the compile-time specialised kernel to use (ct_table.hpp)
 };
 
 // Batched complex DFT of contiguous signals that fit one CTA's shared memory.
@@ -98,6 +99,7 @@ struct fourstep_args
     const void* twA;
     const void* twB;
     int lbits;
+    int tile_shift;  // log2(tile)
     fast_div div_n;  // divides by the FFT length of this pass
 };
 
@@ -149,6 +151,16 @@ enum ew_op
 
 template <typename T>
 cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st);
+
+// Compile-time specialised kernels (single precision; lengths in ct_table.hpp).  kind: see ct_kind.
+cudaError_t launch_ct_c2c_f32(const c2c_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_r2c_f32(const real_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_c2r_f32(const real_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_dct2_f32(const dct_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_dct3_f32(const dct_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_fs_cols_f32(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_fs_rows_f32(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
 
 // Largest thread count a block FFT kernel may be launched with (elem_bytes = sizeof(real type)).
 int max_threads_for(int elem_bytes, int ept);

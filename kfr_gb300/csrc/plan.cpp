@@ -1,6 +1,8 @@
 // Host-side planner and executors (see plan.hpp).
 #include "plan.hpp"
 
+#include "ct_table.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -193,6 +195,11 @@ static bool is_codelet(int r)
     }
 }
 
+// A generic radix-p pass costs about n*p complex multiply-adds; a one-CTA Bluestein transform about
+// 2 * M log2 M * 1.5 for M = next_pow2(2n - 1).  Prefer Bluestein where it is cheaper and fits one CTA.
+template <typename T>
+static bool bluestein_cheaper_impl(long long n);
+
 // Threads per signal needed by a radix sequence at `ept` elements per thread (0 = infeasible).
 static int threads_needed(long long n, const std::vector<int>& radices, int ept)
 {
@@ -214,12 +221,53 @@ static int threads_needed(long long n, const std::vector<int>& radices, int ept)
     return int(std::min<long long>(ts, 1 << 20));
 }
 
+static int ilog2(int x)
+{
+    int s = 0;
+    while ((1 << s) < x)
+        s++;
+    return s;
+}
+
 static int smem_budget()
 {
     // dynamic shared memory left after the static pass-descriptor array and a small reserve
     static const int budget = max_smem_bytes() - int(sizeof(pass_desc)) * kMaxPasses - 1024;
     return budget;
 }
+
+// ------------------------------------------------------------------------------------------------------
+// Compile-time kernel registry
+// ------------------------------------------------------------------------------------------------------
+
+template <typename T>
+bool ct_lookup(int kind, int n, int& ts, std::vector<int>& radices)
+{
+    if (!std::is_same<T, float>::value)
+        return false;
+#define KFR_CT_HOST(N, TS, ...)                                                                            \
+    if (n == N)                                                                                            \
+    {                                                                                                      \
+        ts      = TS;                                                                                      \
+        radices = { __VA_ARGS__ };                                                                         \
+        return true;                                                                                       \
+    }
+    switch (kind)
+    {
+    case CT_C2C: KFR_CT_C2C_F32(KFR_CT_HOST) break;
+    case CT_BLUESTEIN: KFR_CT_BLUESTEIN_F32(KFR_CT_HOST) break;
+    case CT_FOURSTEP: KFR_CT_FOURSTEP_F32(KFR_CT_HOST) break;
+    case CT_REAL: KFR_CT_REAL_F32(KFR_CT_HOST) break;
+    case CT_DCT: KFR_CT_DCT_F32(KFR_CT_HOST) break;
+    case CT_CONV: KFR_CT_CONV_F32(KFR_CT_HOST) break;
+    default: break;
+    }
+#undef KFR_CT_HOST
+    return false;
+}
+
+template bool ct_lookup<float>(int, int, int&, std::vector<int>&);
+template bool ct_lookup<double>(int, int, int&, std::vector<int>&);
 
 // ------------------------------------------------------------------------------------------------------
 // block_program
@@ -245,25 +293,56 @@ bool block_program<T>::feasible(long long n)
 }
 
 template <typename T>
-void block_program<T>::build(int n_)
+static bool bluestein_cheaper_impl(long long n)
 {
-    n       = n_;
-    radices = factor_radices(n);
-    if (radices.empty() || int(radices.size()) > kMaxPasses)
-        throw std::invalid_argument("internal: length has no one-CTA radix plan");
-    ept = 0;
-    for (int e : { 16, 32 })
+    const auto rad = factor_radices(n);
+    double generic = 0;
+    for (int r : rad)
+        if (!is_codelet(r))
+            generic += double(n) * r;
+    if (generic == 0)
+        return false;
+    long long m = 1;
+    while (m < 2 * n - 1)
+        m <<= 1;
+    if (!block_program<T>::feasible(m))
+        return false;
+    return generic > 3.0 * double(m) * std::log2(double(m));
+}
+
+template <typename T>
+void block_program<T>::build(int n_, int kind)
+{
+    n  = n_;
+    ct = 0;
+    int cts = 0;
+    std::vector<int> ctr;
+    if (kind != CT_NONE && ct_lookup<T>(kind, n, cts, ctr))
     {
-        const int t = threads_needed(n, radices, e);
-        if (t > 0 && t <= max_threads_for(int(sizeof(T)), e))
-        {
-            ept = e;
-            ts  = t;
-            break;
-        }
+        radices = ctr;
+        ts      = cts;
+        ept     = 16;
+        ct      = n;
     }
-    if (ept == 0)
-        throw std::invalid_argument("internal: length exceeds one CTA");
+    else
+    {
+        radices = factor_radices(n);
+        if (radices.empty() || int(radices.size()) > kMaxPasses)
+            throw std::invalid_argument("internal: length has no one-CTA radix plan");
+        ept = 0;
+        for (int e : { 16, 32 })
+        {
+            const int t = threads_needed(n, radices, e);
+            if (t > 0 && t <= max_threads_for(int(sizeof(T)), e))
+            {
+                ept = e;
+                ts  = t;
+                break;
+            }
+        }
+        if (ept == 0)
+            throw std::invalid_argument("internal: length exceeds one CTA");
+    }
     std::memset(&desc, 0, sizeof(desc));
     desc.n     = n;
     desc.npass = int(radices.size());
@@ -306,7 +385,7 @@ block_cfg block_program<T>::cfg(long long batch, int spc_cap) const
     c.ept              = ept;
     c.ts               = ts;
     const int per_sig  = padded_len_host<T>(n) * int(2 * sizeof(T));
-    const int max_thr  = max_threads_for(int(sizeof(T)), ept);
+    const int max_thr  = ct ? (sizeof(T) == 4 ? 1024 : 512) : max_threads_for(int(sizeof(T)), ept);
     int spc            = std::max(1, 256 / ts);
     spc                = std::min(spc, std::max(1, max_thr / ts));
     spc                = std::min(spc, std::max(1, smem_budget() / per_sig));
@@ -320,6 +399,7 @@ block_cfg block_program<T>::cfg(long long batch, int spc_cap) const
     c.threads = ((spc * ts + 31) / 32) * 32;
     c.smem    = spc * per_sig;
     c.grid    = (batch + spc - 1) / spc;
+    c.ct      = ct;
     return c;
 }
 
@@ -333,6 +413,7 @@ block_cfg block_program<T>::cfg_tile(int tile) const
     c.threads = ((tile * ts + 31) / 32) * 32;
     c.smem    = tile * padded_len_host<T>(n) * int(2 * sizeof(T));
     c.grid    = 1;
+    c.ct      = ct;
     return c;
 }
 
@@ -343,13 +424,22 @@ std::string block_program<T>::describe() const
     s << "block_fft n=" << n << " radices=";
     for (size_t i = 0; i < radices.size(); i++)
         s << (i ? "x" : "") << radices[i];
-    s << " ept=" << ept << " threads/signal=" << ts;
+    s << (ct ? " compile-time" : " ept=") ;
+    if (!ct)
+        s << ept;
+    s << " threads/signal=" << ts;
     return s.str();
 }
 
 // ------------------------------------------------------------------------------------------------------
 // complex_engine
 // ------------------------------------------------------------------------------------------------------
+
+template <typename T>
+static bool bluestein_cheaper(long long n)
+{
+    return bluestein_cheaper_impl<T>(n);
+}
 
 template <typename T>
 complex_engine<T>::complex_engine(long long n) : n_(n)
@@ -359,13 +449,18 @@ complex_engine<T>::complex_engine(long long n) : n_(n)
         k_ = kind::trivial;
         return;
     }
-    if (block_program<T>::feasible(n))
+    if (block_program<T>::feasible(n) && !bluestein_cheaper<T>(n))
     {
         k_ = kind::smem;
-        prog_.build(int(n));
+        prog_.build(int(n), CT_C2C);
         return;
     }
     const auto rad = factor_radices(n);
+    if (!rad.empty() && bluestein_cheaper<T>(n))
+    {
+        init_bluestein(n);
+        return;
+    }
     if (rad.empty())
     {
         // a prime factor above kGenericMax: Bluestein
@@ -419,7 +514,7 @@ void complex_engine<T>::init_bluestein(long long n)
     if (block_program<T>::feasible(m))
     {
         k_ = kind::bluestein_smem;
-        prog_.build(int(m));
+        prog_.build(int(m), CT_BLUESTEIN);
     }
     else
     {
@@ -432,7 +527,7 @@ template <typename T>
 static int tile_for(const block_program<T>& p)
 {
     const int per_sig = padded_len_host<T>(p.n) * int(2 * sizeof(T));
-    const int max_thr = max_threads_for(int(sizeof(T)), p.ept);
+    const int max_thr = p.ct ? (sizeof(T) == 4 ? 1024 : 512) : max_threads_for(int(sizeof(T)), p.ept);
     int s             = 16;
     while (s > 1 && (s * per_sig > smem_budget() || s * p.ts > max_thr))
         s /= 2;
@@ -490,8 +585,8 @@ bool complex_engine<T>::plan_fourstep(long long n)
     k_  = kind::fourstep;
     n1_ = best_n1;
     n2_ = n / best_n1;
-    pcols_.build(int(n1_));
-    prows_.build(int(n2_));
+    pcols_.build(int(n1_), CT_FOURSTEP);
+    prows_.build(int(n2_), CT_FOURSTEP);
     tile_c_ = tile_for(pcols_);
     tile_r_ = tile_for(prows_);
     // two-level table for W_N^m, m < N
@@ -619,8 +714,9 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             // column pass: x -> scratch
             a.in       = inb;
             a.out      = scr;
-            a.tile     = tile_c_;
-            a.conj_in  = inverse;
+            a.tile       = tile_c_;
+            a.tile_shift = ilog2(tile_c_);
+            a.conj_in    = inverse;
             a.conj_out = 0;
             a.tw       = pcols_.tw.get();
             a.d        = pcols_.desc;
@@ -631,8 +727,9 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             // row pass: scratch -> out
             a.in       = scr;
             a.out      = outb;
-            a.tile     = tile_r_;
-            a.conj_in  = 0;
+            a.tile       = tile_r_;
+            a.tile_shift = ilog2(tile_r_);
+            a.conj_in    = 0;
             a.conj_out = inverse;
             a.tw       = prows_.tw.get();
             a.d        = prows_.desc;
@@ -717,6 +814,8 @@ real_engine<T>::real_engine(long long n) : n_(n), c_(n / 2), ceng_(n / 2)
     }
     rtw_.upload(r.data(), r.size() * sizeof(std::complex<T>));
     fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
+    if (fused_)
+        prog_.build(int(c_), CT_REAL);
 }
 
 template <typename T>
@@ -759,7 +858,7 @@ void real_engine<T>::forward(void* out, const void* in, long long batch, bool cc
     }
     if (fused_)
     {
-        const block_program<T>& p = ceng_.program();
+        const block_program<T>& p = prog_;
         real_args a;
         a.in      = in;
         a.out     = out;
@@ -801,7 +900,7 @@ void real_engine<T>::inverse(void* out, const void* in, long long batch, bool cc
     const long long ilen = ccs ? c_ + 1 : c_;
     if (fused_)
     {
-        const block_program<T>& p = ceng_.program();
+        const block_program<T>& p = prog_;
         real_args a;
         a.in      = in;
         a.out     = out;
@@ -861,6 +960,8 @@ dct_engine<T>::dct_engine(long long n) : n_(n), ceng_(n)
     }
     dtw_.upload(d.data(), d.size() * sizeof(std::complex<T>));
     fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
+    if (fused_)
+        prog_.build(int(n), CT_DCT);
 }
 
 template <typename T>
@@ -885,7 +986,7 @@ void dct_engine<T>::execute(void* out, const void* in, long long batch, bool inv
         return;
     if (fused_)
     {
-        const block_program<T>& p = ceng_.program();
+        const block_program<T>& p = prog_;
         dct_args a;
         a.in     = in;
         a.out    = out;

@@ -65,6 +65,22 @@ void host_fft_pow2(std::vector<std::complex<double>>& a);
 // Radix sequence for a one-CTA length; empty if a prime factor exceeds kGenericMax.
 std::vector<int> factor_radices(long long n);
 
+// Kernel kinds with compile-time specialised lengths (ct_table.hpp).
+enum ct_kind
+{
+    CT_NONE = -1,
+    CT_C2C,
+    CT_BLUESTEIN,
+    CT_FOURSTEP,
+    CT_REAL,
+    CT_DCT,
+    CT_CONV
+};
+
+// True (with the thread count and radix order) if `kind` has a compile-time kernel of length n for T.
+template <typename T>
+bool ct_lookup(int kind, int n, int& ts, std::vector<int>& radices);
+
 // Descriptor, twiddles and thread shape of a one-CTA FFT of length n.
 template <typename T>
 struct block_program
@@ -72,13 +88,15 @@ struct block_program
     int n   = 0;
     int ept = 16;
     int ts  = 1;
+    int ct  = 0; // nonzero: the compile-time kernel of this length is used
     fft_desc desc{};
     std::vector<int> radices;
     dbuf tw;
 
     // False if n cannot run in one CTA (size, registers or a large prime factor).
     static bool feasible(long long n);
-    void build(int n);
+    // `kind` selects the compile-time kernel list to look in (CT_NONE: always the runtime kernel).
+    void build(int n, int kind = CT_NONE);
     // Launch shape for `batch` signals (`spc_cap` bounds the signals per CTA, 0 = no bound).
     block_cfg cfg(long long batch, int spc_cap = 0) const;
     // Launch shape of a four-step tile: exactly `tile` signals per CTA.
@@ -150,6 +168,7 @@ public:
 private:
     long long n_, c_;
     complex_engine<T> ceng_;
+    block_program<T> prog_; // fused kernels: c-point program
     dbuf rtw_;
     bool fused_ = false;
 };
@@ -169,6 +188,7 @@ public:
 private:
     long long n_;
     complex_engine<T> ceng_;
+    block_program<T> prog_; // fused kernels: n-point program
     dbuf dtw_;
     bool fused_ = false;
 };

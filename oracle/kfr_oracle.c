@@ -303,8 +303,8 @@ static void orc_parallel(orc_job_fn fn, void* ctx, size_t count, int threads)
             ORC_CAT(filt_process, SFXT)(f, (C*)out, (const C*)in, n);                                    \
             return;                                                                                      \
         }                                                                                                \
-        C* ci = (C*)malloc(sizeof(C) * (n + 1));                                                         \
-        C* co = (C*)malloc(sizeof(C) * (n + 1));                                                         \
+        C* ci = (C*)calloc(n + 1, sizeof(C));                                                            \
+        C* co = (C*)calloc(n + 1, sizeof(C));                                                            \
         for (size_t i = 0; i < n; i++)                                                                   \
             ci[i] = ORC_CAT(cmk, SFXT)(in[i], 0);                                                        \
         ORC_CAT(filt_process, SFXT)(f, co, ci, n);                                                       \
