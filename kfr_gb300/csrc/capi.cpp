@@ -247,6 +247,8 @@ void exec_dft(void* h, size_t batch, void* out, const void* in, uint8_t* temp, b
     run(*p, out, bytes, in, bytes, temp, scr, stream, false,
         [&](void* o, const void* i, void* s, cudaStream_t st)
         { p->eng.execute(o, i, (long long)batch, (long long)p->n, (long long)p->n, inverse, s, st); });
+    if (!stream)
+        p->eng.check_device_error();
 }
 
 template <typename T>
@@ -525,7 +527,10 @@ void run_static_scratch_f32(void* plan, size_t batch, void* out, const void* in,
             p->eng.execute(out, in, (long long)batch, (long long)p->n, (long long)p->n, inverse, scr, st);
             check(cudaGetLastError(), "kernel launch");
             if (!stream)
+            {
                 check(cudaStreamSynchronize(st), "execute");
+                p->eng.check_device_error();
+            }
         });
 }
 } // namespace kfr_gpu

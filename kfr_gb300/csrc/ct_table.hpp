@@ -31,6 +31,11 @@
     X(8192, 512, 16, 16, 16, 2)                                                                              \
     X(16384, 1024, 16, 16, 16, 4)
 
+// convolution lengths L = n - 1 of the one-CTA Rader kernel for prime n (127, 8191)
+#define KFR_CT_RADER_F32(X)                                                                                 \
+    X(126, 16, 9, 7, 2)                                                                                      \
+    X(8190, 1024, 13, 9, 7, 5, 2)
+
 // four-step pass lengths (columns and rows): the factors of 30720 = 160 x 192 and of the power-of-two
 // lengths 2^15 .. 2^24
 #define KFR_CT_FOURSTEP_F32(X)                                                                              \

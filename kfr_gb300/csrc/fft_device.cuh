@@ -101,7 +101,7 @@ __device__ __forceinline__ int pidx(int i)
     return i + (i >> smem_pad<T>::shift);
 }
 template <typename T>
-__host__ __device__ inline int padded_len(int n)
+__host__ __device__ constexpr int padded_len(int n)
 {
     return n + (n >> smem_pad<T>::shift) + 1;
 }
@@ -561,6 +561,117 @@ __device__ __forceinline__ void ct_block_fft(cpx<T>* buf, const cpx<T>* __restri
     const int lta     = lt < TS ? lt : N;
     cpx<T> v[EPT];
     ct_passes<T, N, TS, EPT, 1, 0, Rs...>(v, buf, tw, lta);
+}
+
+// Compile-time block FFT whose first pass reads an unpadded source (a TMA-filled stage buffer) and whose
+// last pass writes straight to global memory (stride-one across threads, so the stores coalesce); the
+// passes in between work in the padded buffer `work`.  `cj` conjugates on read and on write (inverse).
+// Ends with a barrier, after which `src` and `work` may be reused.
+template <typename T, int N, int TS, int EPT, int R>
+__device__ __forceinline__ void ct_pass_first(cpx<T> (&v)[EPT], const cpx<T>* src, cpx<T>* work, const bool cj,
+                                              const int lt)
+{
+    constexpr int NBF = N / R;
+    constexpr int NB  = (NBF + TS - 1) / TS;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[b * R + r] = conj_if(src[j + r * NBF], cj);
+            dft_codelet<T, R>(&v[b * R]);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                work[pidx<T>(j * R + r)] = v[b * R + codelet_out<R>(r)];
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int N, int TS, int EPT, int R, int NS, int TWOFF>
+__device__ __forceinline__ void ct_pass_last(cpx<T> (&v)[EPT], const cpx<T>* work, cpx<T>* gout,
+                                             const cpx<T>* __restrict__ tw, const bool cj, const int lt)
+{
+    static_assert(NS * R == N, "last pass");
+    constexpr int NBF = N / R;
+    constexpr int NB  = (NBF + TS - 1) / TS;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[b * R + r] = work[pidx<T>(j + r * NBF)];
+            const cpx<T>* t = tw + TWOFF + j;
+#pragma unroll
+            for (int r = 1; r < R; r++)
+                v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * NS);
+            dft_codelet<T, R>(&v[b * R]);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                gout[j + r * NS] = conj_if(v[b * R + codelet_out<R>(r)], cj);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int N, int TS, int EPT, int R>
+__device__ __forceinline__ void ct_pass_only(cpx<T> (&v)[EPT], const cpx<T>* src, cpx<T>* gout, const bool cj,
+                                             const int lt)
+{
+    constexpr int NB = (1 + TS - 1) / TS;
+    static_assert(N == R, "single pass");
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < 1)
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[b * R + r] = conj_if(src[r], cj);
+            dft_codelet<T, R>(&v[b * R]);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                gout[r] = conj_if(v[b * R + codelet_out<R>(r)], cj);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int N, int TS, int EPT, int NS, int TWOFF, int R, int... Rest>
+__device__ __forceinline__ void ct_passes_io(cpx<T> (&v)[EPT], const cpx<T>* src, cpx<T>* work, cpx<T>* gout,
+                                             const cpx<T>* __restrict__ tw, const bool cj, const int lt)
+{
+    if constexpr (NS == 1 && sizeof...(Rest) == 0)
+        ct_pass_only<T, N, TS, EPT, R>(v, src, gout, cj, lt);
+    else if constexpr (NS == 1)
+    {
+        ct_pass_first<T, N, TS, EPT, R>(v, src, work, cj, lt);
+        ct_passes_io<T, N, TS, EPT, R, TWOFF, Rest...>(v, src, work, gout, tw, cj, lt);
+    }
+    else if constexpr (sizeof...(Rest) == 0)
+        ct_pass_last<T, N, TS, EPT, R, NS, TWOFF>(v, work, gout, tw, cj, lt);
+    else
+    {
+        ct_pass<T, N, TS, EPT, R, NS, TWOFF>(v, work, tw, lt);
+        ct_passes_io<T, N, TS, EPT, NS * R, TWOFF + NS * (R - 1), Rest...>(v, src, work, gout, tw, cj, lt);
+    }
+}
+
+template <typename T, int N, int TS, int... Rs>
+__device__ __forceinline__ void ct_block_fft_io(const cpx<T>* src, cpx<T>* work, cpx<T>* gout,
+                                                const cpx<T>* __restrict__ tw, const bool cj, const int lt)
+{
+    constexpr int EPT = ct_ept<N, TS, Rs...>();
+    const int lta     = lt < TS ? lt : N;
+    cpx<T> v[EPT];
+    ct_passes_io<T, N, TS, EPT, 1, 0, Rs...>(v, src, work, gout, tw, cj, lta);
 }
 
 // Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a

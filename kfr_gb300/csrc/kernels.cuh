@@ -11,6 +11,7 @@
 #include "ct_table.hpp"
 #include "fft_device.cuh"
 #include "launch.hpp"
+#include "tma.cuh"
 
 namespace kfr_gpu
 {
@@ -46,6 +47,11 @@ struct ct_fft
     __device__ __forceinline__ void run(cpx<T>* buf, const cpx<T>* __restrict__ tw, int lt) const
     {
         ct_block_fft<T, N, TS, Rs...>(buf, tw, lt);
+    }
+    __device__ __forceinline__ void run_io(const cpx<T>* src, cpx<T>* work, cpx<T>* gout, const cpx<T>* __restrict__ tw,
+                                           bool cj, int lt) const
+    {
+        ct_block_fft_io<T, N, TS, Rs...>(src, work, gout, tw, cj, lt);
     }
 };
 
@@ -105,6 +111,83 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2c(const c2c_args a, con
 }
 
 // ---------------------------------------------------------------------------------------------------
+// Complex DFT, contiguous batch, persistent and pipelined (compile-time lengths).  Each CTA walks tiles of
+// `spc` whole signals (tile t = signals [t*spc, t*spc + spc)).  One thread streams the next tile into the
+// other of two stage buffers with a bulk asynchronous copy (TMA) while the CTA transforms the current
+// one: the first pass reads the stage, the middle passes run in the padded work buffer, and the last pass
+// stores straight to global memory.  Only whole tiles are handled here; the host runs the remainder with
+// k_c2c.  A wait that runs out sets *err and the CTA returns.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1)
+    k_c2c_pipe(const c2c_args a, const long long ntiles, const int spc, int* err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int N      = F::n;
+    constexpr int STRIDE = padded_len<T>(N);
+    const F fft(nullptr, a.d, F::ts);
+    const int tile   = spc * N;
+    cpx<T>* stage0   = reinterpret_cast<cpx<T>*>(smem_raw);
+    cpx<T>* stage1   = stage0 + tile;
+    cpx<T>* work     = stage1 + tile;
+    uint64_t* bars   = reinterpret_cast<uint64_t*>(work + spc * STRIDE);
+    const uint32_t bytes = uint32_t(tile) * uint32_t(sizeof(cpx<T>));
+    const cpx<T>* in = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* out      = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
+    const bool inv   = a.inverse != 0;
+    const group_map gm(F::ts, spc);
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles)
+    {
+        mbar_arrive_expect_tx(&bars[0], bytes);
+        bulk_g2s(stage0, in + t * tile, bytes, &bars[0]);
+    }
+    uint32_t phase   = 0;                // bit s: parity to wait for on stage s
+    uint32_t pending = t < ntiles ? 1 : 0; // bit s: a copy into stage s is in flight
+    int it           = 0;
+    for (; t < ntiles; t += gridDim.x, it++)
+    {
+        const int sb   = it & 1;
+        cpx<T>* stage  = sb ? stage1 : stage0;
+        const bool got = mbar_wait(&bars[sb], (phase >> sb) & 1);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicExch(err, 1);
+                // give the other stage's copy (if any) a bounded chance to land before the CTA exits
+                if ((pending >> (sb ^ 1)) & 1)
+                    mbar_wait(&bars[sb ^ 1], (phase >> (sb ^ 1)) & 1);
+            }
+            return;
+        }
+        phase ^= 1u << sb;
+        pending &= ~(1u << sb);
+        const long long tn = t + gridDim.x;
+        if (tn < ntiles)
+        {
+            pending |= 1u << (sb ^ 1);
+            if (threadIdx.x == 0)
+            {
+                // the other stage was last read by the previous tile's first pass, which ended in a barrier
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bars[sb ^ 1], bytes);
+                bulk_g2s(sb ? stage0 : stage1, in + tn * tile, bytes, &bars[sb ^ 1]);
+            }
+        }
+        fft.run_io(stage + gm.g * N, work + gm.g * STRIDE, out + (t * spc + gm.g) * N, tw, inv, gm.lt);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
 // Bluestein (dft_arblen_stage_impl, src/dft/dft-impl.hpp:248-272), fused into one kernel:
 //   a = x * chirp (zero padded to M) -> FFT_M -> * bhat -> inverse FFT_M -> * chirp
 // ---------------------------------------------------------------------------------------------------
@@ -155,6 +238,156 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_bluestein(const bluestein
         const long long sig = s0 + s;
         if (sig < a.batch)
             out[sig * a.ostride + k] = conj_if(conj(sm[s * stride + pidx<T>(k)]) * ldg(chirp + k), inv);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Rader (prime n, L = n - 1 fits one CTA): permute on load, L-point DFT, times bhat, inverse L-point DFT,
+// gather on store.  x[0] and the DC term of the permuted input's DFT are kept per signal after the
+// signals' slots in shared memory.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a, const int ts, const int spc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ pass_desc sp[kMaxPasses];
+    const F fft(sp, a.d, ts);
+    cpx<T>* sm         = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int L        = fft.n;
+    const int n        = L + 1;
+    const int stride   = padded_len<T>(L);
+    cpx<T>* x0s        = sm + spc * stride; // spc values
+    cpx<T>* dcs        = x0s + spc;        // spc values
+    const long long s0 = (long long)blockIdx.x * spc;
+    const cpx<T>* __restrict__ in   = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* __restrict__ out        = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* __restrict__ bhat = reinterpret_cast<const cpx<T>*>(a.bhat);
+    const bool inv = a.inverse != 0;
+    for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int e = i - s * n;
+        const long long sig = s0 + s;
+        const cpx<T> v = sig < a.batch ? conj_if(in[sig * a.istride + e], inv) : mk<T>(0, 0);
+        if (e == 0)
+            x0s[s] = v;
+        else
+            sm[s * stride + pidx<T>(__ldg(a.pin + e))] = v;
+    }
+    __syncthreads();
+    const group_map gm(ts, spc);
+    const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
+    fft.run(sm + gm.g * stride, tw, gm.lt);
+    for (int i = threadIdx.x; i < spc * L; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_l));
+        const int q = i - s * L;
+        cpx<T>& r   = sm[s * stride + pidx<T>(q)];
+        const cpx<T> A = r;
+        if (q == 0)
+            dcs[s] = A;
+        r = conj(A * ldg(bhat + q));
+    }
+    __syncthreads();
+    fft.run(sm + gm.g * stride, tw, gm.lt);
+    for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
+    {
+        const int s = int(div_by(uint32_t(i), a.div_n));
+        const int k = i - s * n;
+        const long long sig = s0 + s;
+        if (sig >= a.batch)
+            continue;
+        const cpx<T> x0 = x0s[s];
+        const cpx<T> X  = k == 0 ? x0 + dcs[s] : x0 + conj(sm[s * stride + pidx<T>(__ldg(a.qof + k))]);
+        out[sig * a.ostride + k] = conj_if(X, inv);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Rader, persistent and pipelined (compile-time L, one signal per iteration).  The signal's bytes arrive in
+// a shared stage buffer by TMA; the bulk copy covers the enclosing 16-byte-aligned range, so an odd-length
+// signal sits one element into the stage.  The permutation into the convolution input reads the stage, after
+// which the next signal's copy is issued and overlaps the two L-point DFTs and the gathered store.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1)
+    k_rader_pipe(const rader_args a, const long long nsig, int* err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int L      = F::n;
+    constexpr int N      = L + 1;
+    constexpr int STRIDE = padded_len<T>(L);
+    constexpr int STAGE  = ((N * int(sizeof(cpx<T>)) + 31) / 16) * 16 / int(sizeof(cpx<T>));
+    const F fft(nullptr, a.d, F::ts);
+    cpx<T>* stage = reinterpret_cast<cpx<T>*>(smem_raw);
+    cpx<T>* work  = stage + STAGE;
+    cpx<T>* misc  = work + STRIDE; // x0, dc
+    uint64_t* bar = reinterpret_cast<uint64_t*>(misc + 2);
+    const char* inb = reinterpret_cast<const char*>(a.in);
+    cpx<T>* out     = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* __restrict__ bhat = reinterpret_cast<const cpx<T>*>(a.bhat);
+    const cpx<T>* tw                = reinterpret_cast<const cpx<T>*>(a.tw);
+    const bool inv = a.inverse != 0;
+    const int lt   = int(threadIdx.x) < F::ts ? int(threadIdx.x) : F::ts;
+    constexpr long long SIG_BYTES = (long long)N * sizeof(cpx<T>);
+    if (threadIdx.x == 0)
+    {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < nsig)
+    {
+        const long long s0 = t * SIG_BYTES, a0 = s0 & ~15LL, a1 = (s0 + SIG_BYTES + 15) & ~15LL;
+        mbar_arrive_expect_tx(bar, uint32_t(a1 - a0));
+        bulk_g2s(stage, inb + a0, uint32_t(a1 - a0), bar);
+    }
+    uint32_t phase = 0;
+    for (; t < nsig; t += gridDim.x)
+    {
+        const bool got = mbar_wait(bar, phase);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+                atomicExch(err, 1);
+            return;
+        }
+        phase ^= 1;
+        const int off = int(((t * SIG_BYTES) & 15) / int(sizeof(cpx<T>)));
+        for (int p = threadIdx.x; p < L; p += blockDim.x)
+            work[pidx<T>(p)] = conj_if(stage[off + __ldg(a.gp + p)], inv);
+        if (threadIdx.x == 0)
+            misc[0] = conj_if(stage[off], inv);
+        __syncthreads();
+        const long long tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < nsig)
+        {
+            fence_proxy_async_smem();
+            const long long s0 = tn * SIG_BYTES, a0 = s0 & ~15LL, a1 = (s0 + SIG_BYTES + 15) & ~15LL;
+            mbar_arrive_expect_tx(bar, uint32_t(a1 - a0));
+            bulk_g2s(stage, inb + a0, uint32_t(a1 - a0), bar);
+        }
+        fft.run(work, tw, lt);
+        for (int q = threadIdx.x; q < L; q += blockDim.x)
+        {
+            cpx<T>& r      = work[pidx<T>(q)];
+            const cpx<T> A = r;
+            if (q == 0)
+                misc[1] = A;
+            r = conj(A * ldg(bhat + q));
+        }
+        __syncthreads();
+        fft.run(work, tw, lt);
+        const cpx<T> x0 = misc[0];
+        const cpx<T> dc = misc[1];
+        cpx<T>* o       = out + t * N;
+        for (int k = threadIdx.x; k < N; k += blockDim.x)
+        {
+            const cpx<T> X = k == 0 ? x0 + dc : x0 + conj(work[pidx<T>(__ldg(a.qof + k))]);
+            o[k]           = conj_if(X, inv);
+        }
+        __syncthreads();
     }
 }
 
@@ -498,6 +731,12 @@ cudaError_t launch_bluestein(const bluestein_args& a, const block_cfg& c, cudaSt
     KFR_GPU_RUNTIME_DISPATCH(k_bluestein, KFR_GPU_GRID1, a, c.ts, c.spc)
 }
 template <typename T>
+cudaError_t launch_rader(const rader_args& a, const block_cfg& c, cudaStream_t st)
+{
+    KFR_GPU_CT_HOOK(launch_ct_rader_f32)
+    KFR_GPU_RUNTIME_DISPATCH(k_rader, KFR_GPU_GRID1, a, c.ts, c.spc)
+}
+template <typename T>
 cudaError_t launch_r2c(const real_args& a, const block_cfg& c, cudaStream_t st)
 {
     KFR_GPU_CT_HOOK(launch_ct_r2c_f32)
@@ -541,6 +780,7 @@ cudaError_t launch_fs_rows(const fourstep_args& a, const block_cfg& c, cudaStrea
 #define KFR_GPU_INSTANTIATE(T)                                                                             \
     template cudaError_t launch_c2c<T>(const c2c_args&, const block_cfg&, cudaStream_t);                   \
     template cudaError_t launch_bluestein<T>(const bluestein_args&, const block_cfg&, cudaStream_t);       \
+    template cudaError_t launch_rader<T>(const rader_args&, const block_cfg&, cudaStream_t);               \
     template cudaError_t launch_r2c<T>(const real_args&, const block_cfg&, cudaStream_t);                  \
     template cudaError_t launch_c2r<T>(const real_args&, const block_cfg&, cudaStream_t);                  \
     template cudaError_t launch_dct2<T>(const dct_args&, const block_cfg&, cudaStream_t);                  \

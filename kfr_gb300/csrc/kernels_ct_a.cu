@@ -1,6 +1,8 @@
 // Compile-time specialised single-precision kernels: complex DFT and one-CTA Bluestein (ct_table.hpp).
 #include "kernels.cuh"
 
+#include <algorithm>
+
 namespace kfr_gpu
 {
 
@@ -32,6 +34,76 @@ cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c,
 #undef CT_KERNEL
 #undef CT_GRID
 #undef CT_ARGS
+}
+
+cudaError_t launch_ct_rader_f32(const rader_args& a, const block_cfg& c, cudaStream_t st)
+{
+#define CT_KERNEL k_rader
+#define CT_GRID KFR_GPU_GRID1
+#define CT_ARGS a, c.ts, c.spc
+    switch (c.ct)
+    {
+        KFR_CT_RADER_F32(KFR_GPU_CT_CASE)
+    default: return cudaErrorInvalidValue;
+    }
+#undef CT_KERNEL
+#undef CT_GRID
+#undef CT_ARGS
+}
+
+static int sm_count()
+{
+    static int n = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+            v = 152;
+        return v;
+    }();
+    return n;
+}
+
+// Persistent launch: as many CTAs as fit on the device at once, capped by the number of tiles.
+template <typename K, typename... Args>
+static cudaError_t go_persistent(K kernel, const block_cfg& c, long long ntiles, cudaStream_t st, Args... args)
+{
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, c.threads, c.smem);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    const long long grid = std::min<long long>(ntiles, (long long)per_sm * sm_count());
+    kernel<<<unsigned(grid), c.threads, c.smem, st>>>(args...);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
+{
+#define KFR_GPU_PIPE_CASE(N, TS, ...)                                                                      \
+    case N:                                                                                                \
+        return go_persistent(k_c2c_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);
+    switch (c.ct)
+    {
+        KFR_CT_C2C_F32(KFR_GPU_PIPE_CASE)
+    default: return cudaErrorInvalidValue;
+    }
+#undef KFR_GPU_PIPE_CASE
+}
+
+cudaError_t launch_ct_rader_pipe_f32(const rader_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st)
+{
+#define KFR_GPU_RPIPE_CASE(N, TS, ...)                                                                     \
+    case N: return go_persistent(k_rader_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, nsig, st, a, nsig, err);
+    switch (c.ct)
+    {
+        KFR_CT_RADER_F32(KFR_GPU_RPIPE_CASE)
+    default: return cudaErrorInvalidValue;
+    }
+#undef KFR_GPU_RPIPE_CASE
 }
 
 } // namespace kfr_gpu

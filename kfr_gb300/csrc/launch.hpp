@@ -52,6 +52,26 @@ struct bluestein_args
     fft_desc d;
 };
 
+// Rader's algorithm for a prime length n whose cyclic convolution length L = n - 1 = d.n fits one CTA:
+// x[g^p] (p < L) is permuted into the convolution input on load, convolved with b[m] = W_n^{g^-m} through
+// two L-point DFTs, and X[g^-q] = x[0] + c[q] is gathered back on store (X[0] = x[0] + sum x).
+struct rader_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    long long istride, ostride;
+    int n;
+    int inverse;
+    const int* pin;   // pin[v] = p with g^p = v (mod n), v = 1..n-1
+    const int* qof;   // qof[k] = q with g^-q = k (mod n), k = 1..n-1
+    const int* gp;    // gp[p] = g^p (mod n), p = 0..L-1 (pipelined kernel)
+    const void* bhat; // L values: DFT_L(b) / L
+    const void* tw;
+    fast_div div_n, div_l;
+    fft_desc d;
+};
+
 // Real DFT of even length 2c through a c-point complex DFT (d.n = c).
 // Forward: in = reals (istride reals apart), out = c+1 (CCs) or c (Perm) complex (ostride complex apart).
 // Inverse: in = c+1 / c complex (istride complex apart), out = 2c reals (ostride reals apart).
@@ -108,6 +128,8 @@ cudaError_t launch_c2c(const c2c_args& a, const block_cfg& c, cudaStream_t st);
 template <typename T>
 cudaError_t launch_bluestein(const bluestein_args& a, const block_cfg& c, cudaStream_t st);
 template <typename T>
+cudaError_t launch_rader(const rader_args& a, const block_cfg& c, cudaStream_t st);
+template <typename T>
 cudaError_t launch_r2c(const real_args& a, const block_cfg& c, cudaStream_t st);
 template <typename T>
 cudaError_t launch_c2r(const real_args& a, const block_cfg& c, cudaStream_t st);
@@ -154,7 +176,16 @@ cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st);
 
 // Compile-time specialised kernels (single precision; lengths in ct_table.hpp).  kind: see ct_kind.
 cudaError_t launch_ct_c2c_f32(const c2c_args& a, const block_cfg& c, cudaStream_t st);
+// Persistent TMA-pipelined complex DFT over `ntiles` whole tiles of c.spc contiguous signals (c.smem must
+// hold two unpadded tiles, the padded work tile and two mbarriers; in must be 16-byte aligned).
+cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long long ntiles, int* err,
+                                   cudaStream_t st);
 cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c, cudaStream_t st);
+cudaError_t launch_ct_rader_f32(const rader_args& a, const block_cfg& c, cudaStream_t st);
+// Persistent Rader over signals [0, nsig) with the next signal's bytes streamed into a shared stage buffer
+// by TMA (in must be 16-byte aligned and signal nsig-1's enclosing 16-byte range must lie inside the batch).
+cudaError_t launch_ct_rader_pipe_f32(const rader_args& a, const block_cfg& c, long long nsig, int* err,
+                                     cudaStream_t st);
 cudaError_t launch_ct_r2c_f32(const real_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_c2r_f32(const real_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_dct2_f32(const dct_args& a, const block_cfg& c, cudaStream_t st);

@@ -119,6 +119,47 @@ void host_fft_pow2(std::vector<std::complex<double>>& b)
             }
 }
 
+void host_dft(std::vector<std::complex<double>>& a)
+{
+    const long long n = (long long)a.size();
+    if (n <= 1)
+        return;
+    long long p = 2;
+    while (p * p <= n && n % p)
+        p++;
+    if (n % p)
+        p = n;
+    if (p == n)
+    {
+        std::vector<std::complex<double>> r(n);
+        for (long long k = 0; k < n; k++)
+        {
+            std::complex<double> acc = 0;
+            for (long long j = 0; j < n; j++)
+                acc += a[j] * twiddle((j * k) % n, n);
+            r[k] = acc;
+        }
+        a.swap(r);
+        return;
+    }
+    // decimation in time by p: sub-sequences a[p*m + r], m < n/p
+    const long long m = n / p;
+    std::vector<std::vector<std::complex<double>>> sub(p, std::vector<std::complex<double>>(m));
+    for (long long r = 0; r < p; r++)
+    {
+        for (long long j = 0; j < m; j++)
+            sub[r][j] = a[j * p + r];
+        host_dft(sub[r]);
+    }
+    for (long long k = 0; k < n; k++)
+    {
+        std::complex<double> acc = 0;
+        for (long long r = 0; r < p; r++)
+            acc += sub[r][k % m] * twiddle((r * k) % n, n);
+        a[k] = acc;
+    }
+}
+
 std::vector<int> factor_radices(long long n)
 {
     std::vector<int> r;
@@ -195,11 +236,6 @@ static bool is_codelet(int r)
     }
 }
 
-// A generic radix-p pass costs about n*p complex multiply-adds; a one-CTA Bluestein transform about
-// 2 * M log2 M * 1.5 for M = next_pow2(2n - 1).  Prefer Bluestein where it is cheaper and fits one CTA.
-template <typename T>
-static bool bluestein_cheaper_impl(long long n);
-
 // Threads per signal needed by a radix sequence at `ept` elements per thread (0 = infeasible).
 static int threads_needed(long long n, const std::vector<int>& radices, int ept)
 {
@@ -256,6 +292,7 @@ bool ct_lookup(int kind, int n, int& ts, std::vector<int>& radices)
     {
     case CT_C2C: KFR_CT_C2C_F32(KFR_CT_HOST) break;
     case CT_BLUESTEIN: KFR_CT_BLUESTEIN_F32(KFR_CT_HOST) break;
+    case CT_RADER: KFR_CT_RADER_F32(KFR_CT_HOST) break;
     case CT_FOURSTEP: KFR_CT_FOURSTEP_F32(KFR_CT_HOST) break;
     case CT_REAL: KFR_CT_REAL_F32(KFR_CT_HOST) break;
     case CT_DCT: KFR_CT_DCT_F32(KFR_CT_HOST) break;
@@ -290,24 +327,6 @@ bool block_program<T>::feasible(long long n)
             return true;
     }
     return false;
-}
-
-template <typename T>
-static bool bluestein_cheaper_impl(long long n)
-{
-    const auto rad = factor_radices(n);
-    double generic = 0;
-    for (int r : rad)
-        if (!is_codelet(r))
-            generic += double(n) * r;
-    if (generic == 0)
-        return false;
-    long long m = 1;
-    while (m < 2 * n - 1)
-        m <<= 1;
-    if (!block_program<T>::feasible(m))
-        return false;
-    return generic > 3.0 * double(m) * std::log2(double(m));
 }
 
 template <typename T>
@@ -435,10 +454,27 @@ std::string block_program<T>::describe() const
 // complex_engine
 // ------------------------------------------------------------------------------------------------------
 
-template <typename T>
-static bool bluestein_cheaper(long long n)
+static bool is_prime(long long n)
 {
-    return bluestein_cheaper_impl<T>(n);
+    if (n < 2)
+        return false;
+    for (long long p = 2; p * p <= n; p++)
+        if (n % p == 0)
+            return false;
+    return true;
+}
+
+// Relative cost of a one-CTA FFT of length n: one unit per element per codelet pass, R/4 per element for a
+// generic radix-R pass (a length-R dot product per output).
+static double fft_cost(long long n)
+{
+    const auto rad = factor_radices(n);
+    if (rad.empty())
+        return 1e30;
+    double c = 0;
+    for (int r : rad)
+        c += is_codelet(r) ? 1.0 : r / 4.0;
+    return double(n) * c;
 }
 
 template <typename T>
@@ -449,27 +485,167 @@ complex_engine<T>::complex_engine(long long n) : n_(n)
         k_ = kind::trivial;
         return;
     }
-    if (block_program<T>::feasible(n) && !bluestein_cheaper<T>(n))
+    // one-CTA candidates: the direct mixed-radix plan, Rader (prime n) and Bluestein
+    long long m = 1;
+    while (m < 2 * n - 1)
+        m <<= 1;
+    const bool direct_ok    = block_program<T>::feasible(n);
+    const bool rader_ok     = is_prime(n) && n > 13 && block_program<T>::feasible(n - 1);
+    const bool bluestein_ok = block_program<T>::feasible(m);
+    const double c_direct   = direct_ok ? fft_cost(n) : 1e30;
+    const double c_rader    = rader_ok ? 2.0 * fft_cost(n - 1) + 2.0 * n : 1e30;
+    const double c_blue     = bluestein_ok ? 2.0 * fft_cost(m) + 3.0 * n : 1e30;
+    if (direct_ok && c_direct <= c_rader && c_direct <= c_blue)
     {
         k_ = kind::smem;
         prog_.build(int(n), CT_C2C);
+        plan_pipe();
         return;
     }
-    const auto rad = factor_radices(n);
-    if (!rad.empty() && bluestein_cheaper<T>(n))
+    if (rader_ok && c_rader <= c_blue)
+    {
+        init_rader(n);
+        return;
+    }
+    if (bluestein_ok)
     {
         init_bluestein(n);
         return;
     }
-    if (rad.empty())
-    {
-        // a prime factor above kGenericMax: Bluestein
-        init_bluestein(n);
-        return;
-    }
-    if (plan_fourstep(n))
+    if (!factor_radices(n).empty() && plan_fourstep(n))
         return;
     init_bluestein(n);
+}
+
+template <typename T>
+void complex_engine<T>::init_rader(long long n)
+{
+    const long long L = n - 1;
+    // smallest primitive root g of the prime n
+    std::vector<long long> fac;
+    {
+        long long x = L;
+        for (long long p = 2; p * p <= x; p++)
+            if (x % p == 0)
+            {
+                fac.push_back(p);
+                while (x % p == 0)
+                    x /= p;
+            }
+        if (x > 1)
+            fac.push_back(x);
+    }
+    auto powmod = [](long long b, long long e, long long md)
+    {
+        long long r = 1;
+        b %= md;
+        while (e)
+        {
+            if (e & 1)
+                r = r * b % md;
+            b = b * b % md;
+            e >>= 1;
+        }
+        return r;
+    };
+    long long g = 2;
+    for (;; g++)
+    {
+        bool ok = true;
+        for (long long f : fac)
+            if (powmod(g, L / f, n) == 1)
+            {
+                ok = false;
+                break;
+            }
+        if (ok)
+            break;
+    }
+    std::vector<int> pin(n, 0), qof(n, 0);
+    std::vector<std::complex<double>> b(L);
+    long long gp = 1; // g^p
+    for (long long p = 0; p < L; p++)
+    {
+        pin[gp] = int(p);
+        gp      = gp * g % n;
+    }
+    for (long long k = 1; k < n; k++)
+        qof[k] = int((L - pin[k]) % L);
+    // b[m] = W_n^{g^-m}; g^-m = g^{(L - m) mod L}
+    for (long long mm = 0; mm < L; mm++)
+        b[mm] = twiddle(powmod(g, (L - mm) % L, n), n);
+    host_dft(b);
+    std::vector<std::complex<T>> bh(L);
+    for (long long q = 0; q < L; q++)
+        bh[q] = std::complex<T>(T(b[q].real() / double(L)), T(b[q].imag() / double(L)));
+    std::vector<int> gpow(L);
+    for (long long p = 0, v = 1; p < L; p++, v = v * g % n)
+        gpow[p] = int(v);
+    pin_.upload(pin.data(), pin.size() * sizeof(int));
+    qof_.upload(qof.data(), qof.size() * sizeof(int));
+    gp_.upload(gpow.data(), gpow.size() * sizeof(int));
+    if (sizeof(T) == 4)
+    {
+        err_.alloc(sizeof(int));
+        check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
+    }
+    bhat_.upload(bh.data(), bh.size() * sizeof(std::complex<T>));
+    prog_.build(int(L), CT_RADER);
+    k_ = kind::rader_smem;
+}
+
+template <typename T>
+void complex_engine<T>::plan_pipe()
+{
+    pipe_spc_ = 0;
+    if (!prog_.ct || sizeof(T) != 4)
+        return;
+    const int n   = prog_.n;
+    const int esz = int(2 * sizeof(T));
+    // Signals per tile: the most resident threads per SM (at most 1024: the kernels use up to 64
+    // registers), then the smallest tile.  A tile must be a whole number of 16-byte units.
+    int best = 0, best_thr = 0;
+    for (int spc = 1; spc <= 16; spc++)
+    {
+        if ((spc * n) % 2)
+            continue;
+        const int threads = ((spc * prog_.ts + 31) / 32) * 32;
+        if (threads > 1024)
+            break;
+        const int smem = 2 * spc * n * esz + spc * padded_len_host<T>(n) * esz + 64;
+        if (smem > smem_budget())
+            break;
+        const int by_smem = (max_smem_bytes() + 1024) / (smem + 1024);
+        const int by_thr  = 1024 / threads;
+        const int ctas    = std::min(by_smem, by_thr);
+        if (ctas < 2)
+            continue;
+        const int resident = ctas * threads;
+        if (resident > best_thr)
+        {
+            best_thr = resident;
+            best     = spc;
+        }
+    }
+    if (!best)
+        return;
+    pipe_spc_ = best;
+    err_.alloc(sizeof(int));
+    check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
+}
+
+template <typename T>
+void complex_engine<T>::check_device_error() const
+{
+    if (!err_.get())
+        return;
+    int v = 0;
+    check(cudaMemcpy(&v, err_.get(), sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+    if (v)
+    {
+        cudaMemset(err_.get(), 0, sizeof(int));
+        throw cuda_error("a DFT kernel gave up waiting for its input copy (device error flag set)");
+    }
 }
 
 template <typename T>
@@ -629,10 +805,11 @@ int complex_engine<T>::launches(long long batch) const
     switch (k_)
     {
     case kind::trivial: return 1;
-    case kind::smem:
+    case kind::smem: return (pipe_spc_ && batch % pipe_spc_) ? 2 : 1;
     case kind::bluestein_smem: return 1;
     case kind::fourstep: return 2 * int((batch + 65534) / 65535);
     case kind::bluestein_multi: return 3 + 2 * inner_->launches(batch);
+    case kind::rader_smem: return (prog_.ct && prog_.cfg(batch).spc == 1 && batch > 1) ? 2 : 1;
     }
     return 0;
 }
@@ -671,7 +848,25 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.tw      = prog_.tw.get();
         a.div_n   = make_fast_div(uint32_t(n_));
         a.d       = prog_.desc;
-        check(launch_c2c<T>(a, prog_.cfg(batch), st), "launch c2c");
+        long long done = 0;
+        if (pipe_spc_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
+        {
+            const long long ntiles = batch / pipe_spc_;
+            if (ntiles > 0)
+            {
+                block_cfg pc = prog_.cfg_tile(pipe_spc_);
+                pc.smem = 2 * pipe_spc_ * int(n_) * int(esz) + pipe_spc_ * padded_len_host<T>(int(n_)) * int(esz) + 64;
+                check(launch_ct_c2c_pipe_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st), "launch c2c (pipelined)");
+                done = ntiles * pipe_spc_;
+            }
+        }
+        if (done < batch)
+        {
+            a.in    = static_cast<const char*>(in) + done * n_ * esz;
+            a.out   = static_cast<char*>(out) + done * n_ * esz;
+            a.batch = batch - done;
+            check(launch_c2c<T>(a, prog_.cfg(batch - done), st), "launch c2c");
+        }
         return;
     }
     case kind::bluestein_smem:
@@ -691,6 +886,49 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.div_m   = make_fast_div(uint32_t(m_));
         a.d       = prog_.desc;
         check(launch_bluestein<T>(a, prog_.cfg(batch), st), "launch bluestein");
+        return;
+    }
+    case kind::rader_smem:
+    {
+        rader_args a;
+        a.in      = in;
+        a.out     = out;
+        a.batch   = batch;
+        a.istride = istride;
+        a.ostride = ostride;
+        a.n       = int(n_);
+        a.inverse = inverse;
+        a.pin     = static_cast<const int*>(pin_.get());
+        a.qof     = static_cast<const int*>(qof_.get());
+        a.gp      = static_cast<const int*>(gp_.get());
+        a.bhat    = bhat_.get();
+        a.tw      = prog_.tw.get();
+        a.div_n   = make_fast_div(uint32_t(n_));
+        a.div_l   = make_fast_div(uint32_t(n_ - 1));
+        a.d       = prog_.desc;
+        long long done = 0;
+        // Large transforms (one signal per CTA): persistent TMA-pipelined kernel over all but the last
+        // signal, whose enclosing 16-byte range may end past the batch.
+        const block_cfg c1 = prog_.cfg(batch);
+        if (prog_.ct && c1.spc == 1 && err_.get() && istride == n_ && ostride == n_ && batch > 1 &&
+            (reinterpret_cast<uintptr_t>(in) % 16) == 0)
+        {
+            const int stage = int(((n_ * esz + 31) / 16) * 16);
+            block_cfg pc    = prog_.cfg_tile(1);
+            pc.smem         = stage + padded_len_host<T>(int(n_ - 1)) * int(esz) + 2 * int(esz) + 16;
+            if (pc.smem <= smem_budget())
+            {
+                check(launch_ct_rader_pipe_f32(a, pc, batch - 1, static_cast<int*>(err_.get()), st),
+                      "launch rader (pipelined)");
+                done = batch - 1;
+            }
+        }
+        a.in    = static_cast<const char*>(in) + done * n_ * esz;
+        a.out   = static_cast<char*>(out) + done * n_ * esz;
+        a.batch = batch - done;
+        block_cfg c = prog_.cfg(batch - done);
+        c.smem += 2 * c.spc * int(esz);
+        check(launch_rader<T>(a, c, st), "launch rader");
         return;
     }
     case kind::fourstep:
@@ -792,6 +1030,7 @@ std::string complex_engine<T>::describe() const
           << "] rows[" << prows_.describe() << " tile=" << tile_r_ << "]";
         break;
     case kind::bluestein_multi: s << "bluestein_multi n=" << n_ << " m=" << m_ << " inner{" << inner_->describe() << "}"; break;
+    case kind::rader_smem: s << "rader n=" << n_ << " [" << prog_.describe() << "]"; break;
     }
     return s.str();
 }

@@ -10,6 +10,8 @@
 //                    chirp-z transform in one kernel.
 //   fourstep         N = n1 * n2, both one-CTA lengths: a column pass (FFT_n1, twiddle, transpose-store)
 //                    and a row pass (FFT_n2, transpose-store), each one HBM round trip.
+//   rader_smem       a prime N whose cyclic convolution length N - 1 fits one CTA: Rader's permutation
+//                    into an (N-1)-point convolution, computed in one kernel (half the work of Bluestein).
 //   bluestein_multi  anything else: chirp pre-multiply, M-point engine, spectral product, M-point engine,
 //                    chirp post-multiply.
 #pragma once
@@ -61,6 +63,8 @@ std::complex<double> twiddle(long long k, long long n);
 
 // In-place forward DFT of a power-of-two length in double precision (host; used for precomputed spectra).
 void host_fft_pow2(std::vector<std::complex<double>>& a);
+// Forward DFT of any length in double precision (host; recursive mixed radix, O(N * sum of prime factors)).
+void host_dft(std::vector<std::complex<double>>& a);
 
 // Radix sequence for a one-CTA length; empty if a prime factor exceeds kGenericMax.
 std::vector<int> factor_radices(long long n);
@@ -71,6 +75,7 @@ enum ct_kind
     CT_NONE = -1,
     CT_C2C,
     CT_BLUESTEIN,
+    CT_RADER,
     CT_FOURSTEP,
     CT_REAL,
     CT_DCT,
@@ -114,7 +119,8 @@ public:
         smem,
         bluestein_smem,
         fourstep,
-        bluestein_multi
+        bluestein_multi,
+        rader_smem
     };
 
     explicit complex_engine(long long n);
@@ -132,6 +138,8 @@ public:
     long long size() const { return n_; }
     // Kernel launches one execute() issues (for the launch count reported by the benchmark).
     int launches(long long batch) const;
+    // Throws if a kernel of this engine recorded a device-side error (a bounded wait that ran out).
+    void check_device_error() const;
 
 private:
     long long n_;
@@ -147,9 +155,16 @@ private:
     int tile_c_ = 1, tile_r_ = 1;
     dbuf twA_, twB_;
     int lbits_ = 0;
+    // pipelined smem path (compile-time lengths): signals per tile, 0 = not used
+    int pipe_spc_ = 0;
+    dbuf err_;
 
     void init_bluestein(long long n);
+    void init_rader(long long n);
     bool plan_fourstep(long long n);
+    void plan_pipe();
+    // Rader
+    dbuf pin_, qof_, gp_;
 };
 
 // dft_plan_real<T>: N even, N/2-point complex engine plus the CCs/Perm split / merge.
