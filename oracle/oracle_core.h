@@ -195,7 +195,7 @@ static PLAN* FN(plan_create)(size_t n)
         free(bs);
         return p;
     }
-    /* Mixed radix: prime-power radices (8, 4, 2, 3, 5, 7, then the prime cofactor < 101). */
+    /* Mixed radix: radices 8, 4, 2, 9, 3, 5, 7, then the prime cofactor < 101. */
     size_t ns = 1;
     cur       = n;
     while (cur % 8 == 0)
@@ -213,8 +213,8 @@ static PLAN* FN(plan_create)(size_t n)
         FN(add_pass)(p, 2, &ns);
         cur /= 2;
     }
-    const int small[3] = { 3, 5, 7 };
-    for (int i = 0; i < 3; i++)
+    const int small[4] = { 9, 3, 5, 7 };
+    for (int i = 0; i < 4; i++)
         while (cur % (size_t)small[i] == 0)
         {
             FN(add_pass)(p, small[i], &ns);
@@ -278,6 +278,81 @@ static inline void FN(bfly3)(CPX* v)
     v[2]   = FN(csub)(m1, m2);
 }
 
+static inline void FN(bfly5)(CPX* v)
+{
+    const REAL c1 = (REAL)0.30901699437494742410, c2 = (REAL)-0.80901699437494742410;
+    const REAL s1 = (REAL)0.95105651629515357212, s2 = (REAL)0.58778525229247312917;
+    const CPX t1 = FN(cadd)(v[1], v[4]), t2 = FN(cadd)(v[2], v[3]);
+    const CPX t3 = FN(csub)(v[1], v[4]), t4 = FN(csub)(v[2], v[3]);
+    const CPX x0 = v[0];
+    const CPX a1 = FN(cmk)(x0.re + c1 * t1.re + c2 * t2.re, x0.im + c1 * t1.im + c2 * t2.im);
+    const CPX a2 = FN(cmk)(x0.re + c2 * t1.re + c1 * t2.re, x0.im + c2 * t1.im + c1 * t2.im);
+    const CPX b1 = FN(cmk)(s1 * t3.re + s2 * t4.re, s1 * t3.im + s2 * t4.im);
+    const CPX b2 = FN(cmk)(s2 * t3.re - s1 * t4.re, s2 * t3.im - s1 * t4.im);
+    v[0]         = FN(cadd)(x0, FN(cadd)(t1, t2));
+    v[1]         = FN(cmk)(a1.re + b1.im, a1.im - b1.re);
+    v[4]         = FN(cmk)(a1.re - b1.im, a1.im + b1.re);
+    v[2]         = FN(cmk)(a2.re + b2.im, a2.im - b2.re);
+    v[3]         = FN(cmk)(a2.re - b2.im, a2.im + b2.re);
+}
+
+/* odd radix by the symmetric pairing x_m +/- x_{r-m}; cs[k-1], sn[k-1] = cos, sin of 2 pi k / r */
+static inline void FN(bfly_odd)(CPX* v, int r, const double* cs, const double* sn)
+{
+    const int h = (r - 1) / 2;
+    CPX s[8], d[8];
+    CPX x0 = v[0], sum = v[0];
+    for (int m = 1; m <= h; m++)
+    {
+        s[m - 1] = FN(cadd)(v[m], v[r - m]);
+        d[m - 1] = FN(csub)(v[m], v[r - m]);
+        sum      = FN(cadd)(sum, s[m - 1]);
+    }
+    for (int k = 1; k <= h; k++)
+    {
+        REAL ar = x0.re, ai = x0.im, br = 0, bi = 0;
+        for (int m = 1; m <= h; m++)
+        {
+            int km = (k * m) % r;
+            REAL c, sg;
+            if (km == 0) /* composite r (9): k*m can be a multiple of r */
+            {
+                c  = 1;
+                sg = 0;
+            }
+            else if (km <= h)
+            {
+                c  = (REAL)cs[km - 1];
+                sg = (REAL)sn[km - 1];
+            }
+            else
+            {
+                c  = (REAL)cs[r - km - 1];
+                sg = -(REAL)sn[r - km - 1];
+            }
+            ar += c * s[m - 1].re;
+            ai += c * s[m - 1].im;
+            br += sg * d[m - 1].re;
+            bi += sg * d[m - 1].im;
+        }
+        /* X_k = a - i b, X_{r-k} = a + i b */
+        v[k]     = FN(cmk)(ar + bi, ai - br);
+        v[r - k] = FN(cmk)(ar - bi, ai + br);
+    }
+    v[0] = sum;
+}
+
+#ifndef ORC_ODD_CONSTANTS
+#define ORC_ODD_CONSTANTS
+static const double ORC_COS5[2] = { 0.30901699437494742410, -0.80901699437494742410 };
+static const double ORC_SIN5[2] = { 0.95105651629515357212, 0.58778525229247312917 };
+static const double ORC_COS7[3] = { 0.62348980185873353053, -0.22252093395631440429, -0.90096886790241912624 };
+static const double ORC_SIN7[3] = { 0.78183148246802980871, 0.97492791218182360702, 0.43388373911755812048 };
+static const double ORC_COS9[4] = { 0.76604444311897803520, 0.17364817766693034885, -0.5, -0.93969262078590838405 };
+static const double ORC_SIN9[4] = { 0.64278760968653932632, 0.98480775301220805937, 0.86602540378443864676,
+                                    0.34202014332566873304 };
+#endif
+
 static inline void FN(bfly_generic)(CPX* v, int r, const CPX* wr)
 {
     CPX tmp[128];
@@ -320,6 +395,9 @@ static void FN(pass)(const PLAN* p, int pi, CPX* dst, const CPX* src)
             case 3: FN(bfly3)(v); break;
             case 4: FN(bfly4)(v); break;
             case 8: FN(bfly8)(v); break;
+            case 5: FN(bfly5)(v); break;
+            case 7: FN(bfly_odd)(v, 7, ORC_COS7, ORC_SIN7); break;
+            case 9: FN(bfly_odd)(v, 9, ORC_COS9, ORC_SIN9); break;
             default: FN(bfly_generic)(v, r, p->wr[pi]); break;
             }
             const size_t d = j0 * (size_t)r + k;
