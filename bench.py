@@ -40,8 +40,13 @@ METRIC = "batched c32 DFT GB/s (% of HBM roofline), chosen vs plain form at ≤1
 FALLBACK_HBM_GBS = 6800.0
 
 # DRAM bytes per signal measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided
-# by the signals it processed); see profiles/ for the captures.  None = not captured.
-NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float | None] = {}
+# by the signals it processed) at the full 256 MiB batch; the captures are summarised in
+# profiles/k_rader_pipe_8191.md and profiles/k_fs_cols_rows_30720_k_rader_127.md.
+NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float] = {
+    8191: (271_920_896 + 229_835_264) / 4095,
+    127: (268_492_800 + 222_380_800) / 264208,
+    30720: (268_423_680 + 222_224_896 + 268_483_584 + 220_418_560) / 1092,
+}
 
 
 def batch_for(n: int) -> int:
@@ -278,12 +283,12 @@ def main():
         gbs = 16 * n * batch_for(n) / (ms * 1e-3) / 1e9
         per[n] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / hbm, 4),
                   "gflops": round(5 * n * np.log2(n) * batch_for(n) / (ms * 1e-3) / 1e9, 1),
-                  "rel_rms": float(f"{errs[n]:.3e}"), "plan": None}
+                  "rel_rms": float(f"{errs[n]:.3e}"), "plan": plans[n].describe()}
     dom = max(SIZES, key=lambda n: per[n]["ms"])
     traffic = NCU_TRAFFIC_BYTES_PER_SIGNAL.get(dom)
     roof = {"bound": "hbm", "achieved": per[dom]["gbs"], "peak": hbm, "unit": "GB/s",
             "frac": per[dom]["frac"], "traffic": (traffic * batch_for(dom)) if traffic else None,
-            "kernel": f"N={dom} ({'four-step' if dom == 30720 else 'block FFT'})", "peak_kind": peak_kind,
+            "kernel": f"N={dom}: {plans[dom].describe()}", "peak_kind": peak_kind,
             "step_frac": round(value / world / hbm, 4)}
     launches = args.steps * sum(plans[n].launch_count(batch_for(n)) for n in SIZES)
 

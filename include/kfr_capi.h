@@ -236,6 +236,10 @@ KFR_API_SPEC void kfr_dct_execute_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch
 KFR_API_SPEC void kfr_dct_execute_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch, kfr_f64* out, const kfr_f64* in,
                                             uint8_t* temp, kfr_bool inverse, void* stream);
 
+/* Text description of the plan's GPU strategy (kernel kind, radices, launch shape), as kfr_dft_dump_f32 prints
+ * it; copies at most size-1 bytes plus a terminating zero and returns the full length. */
+KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size);
+
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
 

@@ -97,6 +97,7 @@ _SIGS.update({
     "kfr_allocate_aligned": (_P, [_S, _S]),
     "kfr_deallocate": (None, [_P]),
     "kfr_dft_get_launch_count_f32": (_S, [_P, _S]),
+    "kfr_dft_describe_f32": (_S, [_P, ctypes.c_char_p, _S]),
     "kfr_dft_execute_static_scratch_f32": (None, [_P, _S, _P, _P, _B, _P]),
 })
 
@@ -225,6 +226,13 @@ class dft_plan(_plan):
     def execute_batch(self, out, inp, batch, temp=None, inverse=False, stream=None):
         _call(self._fn("execute_batch"), self.handle, batch, _addr(out), _addr(inp), _addr(temp), bool(inverse),
               _stream_addr(stream))
+
+    def describe(self) -> str:
+        if self.sfx != "f32":
+            return ""
+        buf = ctypes.create_string_buffer(512)
+        _call("kfr_dft_describe_f32", self.handle, buf, 512)
+        return buf.value.decode()
 
     def launch_count(self, batch=1):
         return _call("kfr_dft_get_launch_count_f32", self.handle, batch) if self.sfx == "f32" else None

@@ -495,6 +495,22 @@ KFR_API_SPEC void kfr_dft_execute_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch
 {
     try_void([&] { exec_dft<double>(plan, batch, out, in, temp, inverse, stream); });
 }
+KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size)
+{
+    return try_fn(
+        [&]
+        {
+            const std::string d = as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.describe();
+            if (buf && size)
+            {
+                const size_t n = std::min(size - 1, d.size());
+                std::memcpy(buf, d.data(), n);
+                buf[n] = 0;
+            }
+            return d.size();
+        },
+        size_t(0));
+}
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch)
 {
     return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.launches(batch)); }, size_t(0));
