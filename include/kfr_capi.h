@@ -236,6 +236,29 @@ KFR_API_SPEC void kfr_dct_execute_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch
 KFR_API_SPEC void kfr_dct_execute_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch, kfr_f64* out, const kfr_f64* in,
                                             uint8_t* temp, kfr_bool inverse, void* stream);
 
+/* Whole-signal convolution, correlation and autocorrelation: the reference's C++ convolve / correlate /
+ * autocorrelate (include/kfr/dft/convolution.hpp:53-76) as C entry points.  out receives na + nb - 1 values
+ * (autocorrelate: n values, lags 0 .. n-1); the return value is that count.  The result is the reference's:
+ * the linear convolution computed through DFTs of size next_pow2(na + nb - 1) and scaled by 1/size; for
+ * complex inputs only the real part is kept (the imaginary parts of out are zero), as the reference does
+ * (src/dft/convolution-impl.cpp:127).  correlate reverses b without conjugating it.  Pointers may be host
+ * or device memory; the call is synchronous. */
+KFR_API_SPEC size_t kfr_convolve_f32(kfr_f32* out, const kfr_f32* a, size_t na, const kfr_f32* b, size_t nb);
+KFR_API_SPEC size_t kfr_convolve_f64(kfr_f64* out, const kfr_f64* a, size_t na, const kfr_f64* b, size_t nb);
+KFR_API_SPEC size_t kfr_convolve_c32(kfr_c32* out, const kfr_c32* a, size_t na, const kfr_c32* b, size_t nb);
+KFR_API_SPEC size_t kfr_convolve_c64(kfr_c64* out, const kfr_c64* a, size_t na, const kfr_c64* b, size_t nb);
+KFR_API_SPEC size_t kfr_correlate_f32(kfr_f32* out, const kfr_f32* a, size_t na, const kfr_f32* b, size_t nb);
+KFR_API_SPEC size_t kfr_correlate_f64(kfr_f64* out, const kfr_f64* a, size_t na, const kfr_f64* b, size_t nb);
+KFR_API_SPEC size_t kfr_correlate_c32(kfr_c32* out, const kfr_c32* a, size_t na, const kfr_c32* b, size_t nb);
+KFR_API_SPEC size_t kfr_correlate_c64(kfr_c64* out, const kfr_c64* a, size_t na, const kfr_c64* b, size_t nb);
+KFR_API_SPEC size_t kfr_autocorrelate_f32(kfr_f32* out, const kfr_f32* a, size_t n);
+KFR_API_SPEC size_t kfr_autocorrelate_f64(kfr_f64* out, const kfr_f64* a, size_t n);
+
+/* The plan cache behind the convolution entry points (dft_cache, include/kfr/dft/cache.hpp:45-171): number
+ * of cached plans, and release of all of them. */
+KFR_API_SPEC size_t kfr_dft_cache_size(void);
+KFR_API_SPEC void kfr_dft_cache_clear(void);
+
 /* Text description of the plan's GPU strategy (kernel kind, radices, launch shape), as kfr_dft_dump_f32 prints
  * it; copies at most size-1 bytes plus a terminating zero and returns the full length. */
 KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size);

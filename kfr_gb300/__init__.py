@@ -25,8 +25,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libkfr_capi.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "kfr_capi.h")
 
-__all__ = ["KfrError", "lib", "dft_plan", "dft_plan_real", "dct_plan", "convolve_filter", "declared_symbols",
-           "CCs", "Perm"]
+__all__ = ["KfrError", "lib", "dft_plan", "dft_plan_md", "dft_plan_real", "dft_plan_md_real", "dct_plan",
+           "convolve_filter", "declared_symbols", "CCs", "Perm"]
 
 CCs = 1
 Perm = 0
@@ -87,6 +87,9 @@ for sfx in ("f32", "f64"):
         f"kfr_filter_reset_{sfx}": (None, [_P]),
         f"kfr_filter_delete_plan_{sfx}": (None, [_P]),
     })
+for fn in ("convolve", "correlate"):
+    for sfx in ("f32", "f64", "c32", "c64"):
+        _SIGS[f"kfr_{fn}_{sfx}"] = (_S, [_P, _P, _S, _P, _S])
 _SIGS.update({
     "kfr_version_string": (ctypes.c_char_p, []),
     "kfr_version": (ctypes.c_uint32, []),
@@ -99,6 +102,10 @@ _SIGS.update({
     "kfr_dft_get_launch_count_f32": (_S, [_P, _S]),
     "kfr_dft_describe_f32": (_S, [_P, ctypes.c_char_p, _S]),
     "kfr_dft_execute_static_scratch_f32": (None, [_P, _S, _P, _P, _B, _P]),
+    "kfr_dft_cache_size": (_S, []),
+    "kfr_dft_cache_clear": (None, []),
+    "kfr_autocorrelate_f32": (_S, [_P, _P, _S]),
+    "kfr_autocorrelate_f64": (_S, [_P, _P, _S]),
 })
 
 
@@ -238,6 +245,39 @@ class dft_plan(_plan):
         return _call("kfr_dft_get_launch_count_f32", self.handle, batch) if self.sfx == "f32" else None
 
 
+class dft_plan_md(dft_plan):
+    """Multi-dimensional complex DFT over a row-major array (dft_plan_md<T>, include/kfr/dft/fft.hpp:568-702)."""
+
+    def __init__(self, shape, dtype="f32"):
+        sfx = _sfx(dtype)
+        self.shape = tuple(int(v) for v in shape)
+        arr = (ctypes.c_uint * len(self.shape))(*self.shape)
+        _plan.__init__(self, _call(f"kfr_dft_create_md_plan_{sfx}", len(self.shape), ctypes.cast(arr, _P)), sfx)
+
+
+class dft_plan_md_real(_plan):
+    """Multi-dimensional real DFT (dft_plan_md_real<T>, include/kfr/dft/fft.hpp:704-924): real array of
+    `shape` <-> CCs complex array whose last axis has shape[-1]//2 + 1 values."""
+
+    _prefix = "kfr_dft_real"
+
+    def __init__(self, shape, real_out_is_enough=False, dtype="f32"):
+        sfx = _sfx(dtype)
+        self.shape = tuple(int(v) for v in shape)
+        self.complex_shape = self.shape[:-1] + (self.shape[-1] // 2 + 1,)
+        arr = (ctypes.c_uint * len(self.shape))(*self.shape)
+        super().__init__(_call(f"kfr_dft_real_create_md_plan_{sfx}", len(self.shape), ctypes.cast(arr, _P),
+                               bool(real_out_is_enough)), sfx)
+
+    def execute(self, out, inp, temp=None, inverse=False):
+        op = "execute_inverse" if inverse else "execute"
+        _call(self._fn(op), self.handle, _addr(out), _addr(inp), _addr(temp))
+
+    def execute_batch(self, out, inp, batch, temp=None, inverse=False, stream=None):
+        op = "execute_inverse_batch" if inverse else "execute_batch"
+        _call(self._fn(op), self.handle, batch, _addr(out), _addr(inp), _addr(temp), _stream_addr(stream))
+
+
 class dft_plan_real(_plan):
     """Real DFT of even length `size` (dft_plan_real<T>), CCs (N/2+1 bins) or Perm (N/2 bins) packing."""
 
@@ -318,6 +358,49 @@ class convolve_filter(_plan):
 
     def reset(self):
         _call(self._fn("reset"), self.handle)
+
+
+def _conv_sfx(x):
+    d = str(getattr(x, "dtype", ""))
+    table = {"float32": "f32", "float64": "f64", "complex64": "c32", "complex128": "c64", "torch.float32": "f32",
+             "torch.float64": "f64", "torch.complex64": "c32", "torch.complex128": "c64"}
+    if d not in table:
+        raise ValueError(f"unsupported dtype {d}")
+    return table[d]
+
+
+def _numel(x):
+    return x.numel() if hasattr(x, "numel") else len(x)
+
+
+def _like(x, n):
+    if isinstance(x, np.ndarray):
+        return np.zeros(n, dtype=x.dtype)
+    import torch
+
+    return torch.zeros(n, dtype=x.dtype, device=x.device)
+
+
+def convolve(a, b):
+    """Linear convolution (convolve, include/kfr/dft/convolution.hpp:53-58); complex inputs keep only the
+    real part, as the reference does."""
+    out = _like(a, _numel(a) + _numel(b) - 1)
+    _call(f"kfr_convolve_{_conv_sfx(a)}", _addr(out), _addr(a), _numel(a), _addr(b), _numel(b))
+    return out
+
+
+def correlate(a, b):
+    """Correlation: convolution with b reversed (not conjugated) (include/kfr/dft/convolution.hpp:61-66)."""
+    out = _like(a, _numel(a) + _numel(b) - 1)
+    _call(f"kfr_correlate_{_conv_sfx(a)}", _addr(out), _addr(a), _numel(a), _addr(b), _numel(b))
+    return out
+
+
+def autocorrelate(a):
+    """Lags 0 .. n-1 of correlate(a, a) (include/kfr/dft/convolution.hpp:69-76); real inputs."""
+    out = _like(a, _numel(a))
+    _call(f"kfr_autocorrelate_{_conv_sfx(a)}", _addr(out), _addr(a), _numel(a))
+    return out
 
 
 def allocate(size: int, alignment: int = 64) -> int:

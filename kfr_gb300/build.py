@@ -29,9 +29,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = [
     "kernels_f32.cu", "kernels_f64.cu", "kernels_ct_a.cu", "kernels_ct_b.cu", "kernels_ct_c.cu", "elementwise.cu",
-    "conv.cu", "static_scratch.cu",
+    "conv.cu", "convolve.cu", "static_scratch.cu",
 ]
-CPP_SOURCES = ["plan.cpp", "capi.cpp"]
+CPP_SOURCES = ["plan.cpp", "md.cpp", "capi.cpp"]
 
 
 def _headers():

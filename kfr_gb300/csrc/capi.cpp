@@ -13,6 +13,8 @@
 #include <string>
 
 #include "conv.hpp"
+#include "convolve.hpp"
+#include "md.hpp"
 #include "plan.hpp"
 
 using namespace kfr_gpu;
@@ -107,28 +109,86 @@ struct tags<double>
     static constexpr uint32_t dft = TAG_DFT_F64, real = TAG_REAL_F64, dct = TAG_DCT_F64, flt = TAG_FLT_F64;
 };
 
+// A complex plan is one-dimensional (complex_engine) or multi-dimensional (md_engine), like the reference's
+// var_dft_plan over dft_plan / dft_plan_md (src/capi/capi.cpp:93-156).
 template <typename T>
 struct dft_obj : plan_base
 {
-    size_t n;
-    complex_engine<T> eng;
-    explicit dft_obj(size_t n_) : plan_base(tags<T>::dft), n(n_), eng((long long)n_) {}
+    size_t n; // total number of complex values
+    std::unique_ptr<complex_engine<T>> eng1;
+    std::unique_ptr<md_engine<T>> md;
+    explicit dft_obj(size_t n_) : plan_base(tags<T>::dft), n(n_), eng1(new complex_engine<T>((long long)n_)) {}
+    explicit dft_obj(const std::vector<long long>& shape) : plan_base(tags<T>::dft), n(0)
+    {
+        if (shape.size() == 1)
+            eng1.reset(new complex_engine<T>(shape[0]));
+        else
+            md.reset(new md_engine<T>(shape));
+        n = eng1 ? size_t(eng1->size()) : size_t(md->size());
+    }
+    long long scratch_elems(long long b) const { return eng1 ? eng1->scratch_elems(b) : md->scratch_elems(b); }
+    void execute(void* o, const void* i, long long b, bool inv, void* s, cudaStream_t st) const
+    {
+        if (eng1)
+            eng1->execute(o, i, b, (long long)n, (long long)n, inv, s, st);
+        else
+            md->execute(o, i, b, inv, s, st);
+    }
+    std::string describe() const { return eng1 ? eng1->describe() : md->describe(); }
+    int launches(long long b) const { return eng1 ? eng1->launches(b) : md->launches(b); }
+    void check_device_error() const
+    {
+        if (eng1)
+            eng1->check_device_error();
+    }
 };
 
+// A real plan: one-dimensional (real_engine, CCs or Perm) or multi-dimensional (md_real_engine, CCs).
 template <typename T>
 struct real_obj : plan_base
 {
-    size_t n;
+    size_t n; // total number of reals
     bool ccs;
-    real_engine<T> eng;
-    real_obj(size_t n_, bool ccs_) : plan_base(tags<T>::real), n(n_), ccs(ccs_), eng(check_even(n_)) {}
-    static long long check_even(size_t n)
+    std::unique_ptr<real_engine<T>> eng1;
+    std::unique_ptr<md_real_engine<T>> md;
+    real_obj(size_t n_, bool ccs_) : plan_base(tags<T>::real), n(n_), ccs(ccs_)
     {
-        if (n % 2 != 0)
+        if (n_ % 2 != 0)
             throw std::logic_error("dft_plan_real requires size to be even");
-        return (long long)n;
+        eng1.reset(new real_engine<T>((long long)n_));
     }
-    size_t clen() const { return ccs ? n / 2 + 1 : n / 2; }
+    real_obj(const std::vector<long long>& shape, bool real_out_is_enough) : plan_base(tags<T>::real), n(0), ccs(true)
+    {
+        if (shape.size() == 1)
+        {
+            if (shape[0] % 2 != 0)
+                throw std::logic_error("dft_plan_real requires size to be even");
+            eng1.reset(new real_engine<T>(shape[0]));
+            n = size_t(shape[0]);
+        }
+        else
+        {
+            md.reset(new md_real_engine<T>(shape, real_out_is_enough));
+            n = size_t(md->size());
+        }
+    }
+    size_t clen() const { return md ? size_t(md->complex_size()) : (ccs ? n / 2 + 1 : n / 2); }
+    long long scratch_elems(long long b) const { return eng1 ? eng1->scratch_elems(b) : md->scratch_elems(b); }
+    void forward(void* o, const void* i, long long b, void* s, cudaStream_t st) const
+    {
+        if (eng1)
+            eng1->forward(o, i, b, ccs, s, st);
+        else
+            md->forward(o, i, b, s, st);
+    }
+    void inverse(void* o, const void* i, long long b, void* s, cudaStream_t st) const
+    {
+        if (eng1)
+            eng1->inverse(o, i, b, ccs, s, st);
+        else
+            md->inverse(o, i, b, s, st);
+    }
+    std::string describe() const { return eng1 ? eng1->describe() : md->describe(); }
 };
 
 template <typename T>
@@ -243,12 +303,11 @@ void exec_dft(void* h, size_t batch, void* out, const void* in, uint8_t* temp, b
     if (batch == 0 || p->n == 0)
         return;
     const size_t bytes = batch * p->n * 2 * sizeof(T);
-    const size_t scr   = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(T);
+    const size_t scr   = size_t(p->scratch_elems((long long)batch)) * 2 * sizeof(T);
     run(*p, out, bytes, in, bytes, temp, scr, stream, false,
-        [&](void* o, const void* i, void* s, cudaStream_t st)
-        { p->eng.execute(o, i, (long long)batch, (long long)p->n, (long long)p->n, inverse, s, st); });
+        [&](void* o, const void* i, void* s, cudaStream_t st) { p->execute(o, i, (long long)batch, inverse, s, st); });
     if (!stream)
-        p->eng.check_device_error();
+        p->check_device_error();
 }
 
 template <typename T>
@@ -259,13 +318,14 @@ void exec_real(void* h, size_t batch, void* out, const void* in, uint8_t* temp, 
         return;
     const size_t rbytes = batch * p->n * sizeof(T);
     const size_t cbytes = batch * p->clen() * 2 * sizeof(T);
-    const size_t scr    = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(T);
+    const size_t scr    = size_t(p->scratch_elems((long long)batch)) * 2 * sizeof(T);
+    const bool alias    = batch > 1 || p->md != nullptr;
     if (!inverse)
-        run(*p, out, cbytes, in, rbytes, temp, scr, stream, batch > 1,
-            [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.forward(o, i, (long long)batch, p->ccs, s, st); });
+        run(*p, out, cbytes, in, rbytes, temp, scr, stream, alias,
+            [&](void* o, const void* i, void* s, cudaStream_t st) { p->forward(o, i, (long long)batch, s, st); });
     else
-        run(*p, out, rbytes, in, cbytes, temp, scr, stream, batch > 1,
-            [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.inverse(o, i, (long long)batch, p->ccs, s, st); });
+        run(*p, out, rbytes, in, cbytes, temp, scr, stream, alias,
+            [&](void* o, const void* i, void* s, cudaStream_t st) { p->inverse(o, i, (long long)batch, s, st); });
 }
 
 template <typename T>
@@ -364,6 +424,95 @@ void host_free(void* p)
     std::free(h->base);
 }
 
+// init_shape (src/capi/capi.cpp:106-114)
+std::vector<long long> to_shape(size_t dims, const unsigned* shape)
+{
+    if (dims && !shape)
+        throw std::invalid_argument("shape is NULL");
+    std::vector<long long> s(dims);
+    for (size_t i = 0; i < dims; i++)
+        s[i] = shape[i];
+    return s;
+}
+
+// Whole-signal convolution with host or device pointers: host inputs and outputs are staged through
+// stream-ordered device allocations on the legacy default stream, and the call synchronises.
+template <typename T>
+size_t convolve_any(void* out, const void* a, size_t na, const void* b, size_t nb, bool is_complex, int mode)
+{
+    if (na == 0 || nb == 0)
+        return 0;
+    if (!out || !a || !b)
+        throw std::invalid_argument("NULL data pointer");
+    const size_t esz  = (is_complex ? 2 : 1) * sizeof(T);
+    const size_t olen = na + nb - 1;
+    cudaStream_t st   = nullptr;
+    const void* da    = a;
+    const void* db    = b;
+    void* dout        = out;
+    std::vector<void*> owned;
+    struct guard_t
+    {
+        std::vector<void*>& v;
+        ~guard_t()
+        {
+            for (void* p : v)
+                cudaFreeAsync(p, nullptr);
+        }
+    } guard{ owned };
+    auto stage = [&](const void* src, size_t bytes) -> const void*
+    {
+        if (is_device_ptr(src))
+            return src;
+        void* d = nullptr;
+        check(cudaMallocAsync(&d, bytes, st), "cudaMallocAsync");
+        owned.push_back(d);
+        check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, st), "copy input to device");
+        return d;
+    };
+    da                 = stage(a, na * esz);
+    db                 = stage(b, nb * esz);
+    const bool out_dev = is_device_ptr(out);
+    if (!out_dev)
+    {
+        void* d = nullptr;
+        check(cudaMallocAsync(&d, olen * esz, st), "cudaMallocAsync");
+        owned.push_back(d);
+        dout = d;
+    }
+    convolve_device<T>(dout, da, (long long)na, db, (long long)nb, is_complex, mode, st);
+    if (!out_dev)
+        check(cudaMemcpyAsync(out, dout, olen * esz, cudaMemcpyDeviceToHost, st), "copy result to host");
+    check(cudaStreamSynchronize(st), "convolve");
+    return olen;
+}
+
+// autocorrelate: the upper half of correlate(a, a), lags 0 .. n-1 (include/kfr/dft/convolution.hpp:69-76)
+template <typename T>
+size_t autocorrelate_any(T* out, const T* a, size_t n)
+{
+    if (n == 0)
+        return 0;
+    std::vector<T> full;
+    const bool out_dev = is_device_ptr(out);
+    void* tmp          = nullptr;
+    if (out_dev)
+    {
+        check(cudaMallocAsync(&tmp, (2 * n - 1) * sizeof(T), nullptr), "cudaMallocAsync");
+        convolve_any<T>(tmp, a, n, a, n, false, 1);
+        check(cudaMemcpy(out, static_cast<T*>(tmp) + (n - 1), n * sizeof(T), cudaMemcpyDeviceToDevice), "copy");
+        cudaFreeAsync(tmp, nullptr);
+        check(cudaStreamSynchronize(nullptr), "autocorrelate");
+    }
+    else
+    {
+        full.resize(2 * n - 1);
+        convolve_any<T>(full.data(), a, n, a, n, false, 1);
+        std::memcpy(out, full.data() + (n - 1), n * sizeof(T));
+    }
+    return n;
+}
+
 [[noreturn]] void not_built(const char* what)
 {
     throw std::logic_error(std::string(what) + " is not part of the GPU DFT path in this build");
@@ -417,37 +566,43 @@ KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_plan_f64(size_t size)
     return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F64*>(create_dft<double>(size)); },
                   (KFR_DFT_PLAN_F64*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_2d_plan_f32(size_t, size_t)
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_2d_plan_f32(size_t size1, size_t size2)
 {
-    return try_fn([]() -> KFR_DFT_PLAN_F32* { not_built("kfr_dft_create_2d_plan_f32"); }, (KFR_DFT_PLAN_F32*)nullptr);
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F32*>(static_cast<plan_base*>(new dft_obj<float>(std::vector<long long>{ (long long)size1, (long long)size2 }))); },
+                  (KFR_DFT_PLAN_F32*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_3d_plan_f32(size_t, size_t, size_t)
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_3d_plan_f32(size_t size1, size_t size2, size_t size3)
 {
-    return try_fn([]() -> KFR_DFT_PLAN_F32* { not_built("kfr_dft_create_3d_plan_f32"); }, (KFR_DFT_PLAN_F32*)nullptr);
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F32*>(static_cast<plan_base*>(new dft_obj<float>(std::vector<long long>{ (long long)size1, (long long)size2, (long long)size3 }))); },
+                  (KFR_DFT_PLAN_F32*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_md_plan_f32(size_t, const unsigned*)
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_md_plan_f32(size_t dims, const unsigned* shape)
 {
-    return try_fn([]() -> KFR_DFT_PLAN_F32* { not_built("kfr_dft_create_md_plan_f32"); }, (KFR_DFT_PLAN_F32*)nullptr);
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F32*>(static_cast<plan_base*>(new dft_obj<float>(to_shape(dims, shape)))); },
+                  (KFR_DFT_PLAN_F32*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_2d_plan_f64(size_t, size_t)
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_2d_plan_f64(size_t size1, size_t size2)
 {
-    return try_fn([]() -> KFR_DFT_PLAN_F64* { not_built("kfr_dft_create_2d_plan_f64"); }, (KFR_DFT_PLAN_F64*)nullptr);
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F64*>(static_cast<plan_base*>(new dft_obj<double>(std::vector<long long>{ (long long)size1, (long long)size2 }))); },
+                  (KFR_DFT_PLAN_F64*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_3d_plan_f64(size_t, size_t, size_t)
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_3d_plan_f64(size_t size1, size_t size2, size_t size3)
 {
-    return try_fn([]() -> KFR_DFT_PLAN_F64* { not_built("kfr_dft_create_3d_plan_f64"); }, (KFR_DFT_PLAN_F64*)nullptr);
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F64*>(static_cast<plan_base*>(new dft_obj<double>(std::vector<long long>{ (long long)size1, (long long)size2, (long long)size3 }))); },
+                  (KFR_DFT_PLAN_F64*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_md_plan_f64(size_t, const unsigned*)
+KFR_API_SPEC KFR_DFT_PLAN_F64* kfr_dft_create_md_plan_f64(size_t dims, const unsigned* shape)
 {
-    return try_fn([]() -> KFR_DFT_PLAN_F64* { not_built("kfr_dft_create_md_plan_f64"); }, (KFR_DFT_PLAN_F64*)nullptr);
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F64*>(static_cast<plan_base*>(new dft_obj<double>(to_shape(dims, shape)))); },
+                  (KFR_DFT_PLAN_F64*)nullptr);
 }
 KFR_API_SPEC void kfr_dft_dump_f32(KFR_DFT_PLAN_F32* plan)
 {
-    try_void([&] { print_line(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.describe()); });
+    try_void([&] { print_line(as<dft_obj<float>>(plan, TAG_DFT_F32)->describe()); });
 }
 KFR_API_SPEC void kfr_dft_dump_f64(KFR_DFT_PLAN_F64* plan)
 {
-    try_void([&] { print_line(as<dft_obj<double>>(plan, TAG_DFT_F64)->eng.describe()); });
+    try_void([&] { print_line(as<dft_obj<double>>(plan, TAG_DFT_F64)->describe()); });
 }
 KFR_API_SPEC size_t kfr_dft_get_size_f32(KFR_DFT_PLAN_F32* plan)
 {
@@ -459,12 +614,12 @@ KFR_API_SPEC size_t kfr_dft_get_size_f64(KFR_DFT_PLAN_F64* plan)
 }
 KFR_API_SPEC size_t kfr_dft_get_temp_size_batch_f32(KFR_DFT_PLAN_F32* plan, size_t batch)
 {
-    return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.scratch_elems(batch)) * 8; },
+    return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->scratch_elems(batch)) * 8; },
                   size_t(0));
 }
 KFR_API_SPEC size_t kfr_dft_get_temp_size_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch)
 {
-    return try_fn([&] { return size_t(as<dft_obj<double>>(plan, TAG_DFT_F64)->eng.scratch_elems(batch)) * 16; },
+    return try_fn([&] { return size_t(as<dft_obj<double>>(plan, TAG_DFT_F64)->scratch_elems(batch)) * 16; },
                   size_t(0));
 }
 KFR_API_SPEC size_t kfr_dft_get_temp_size_f32(KFR_DFT_PLAN_F32* plan) { return kfr_dft_get_temp_size_batch_f32(plan, 1); }
@@ -495,12 +650,43 @@ KFR_API_SPEC void kfr_dft_execute_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch
 {
     try_void([&] { exec_dft<double>(plan, batch, out, in, temp, inverse, stream); });
 }
+#define KFR_CONV_ENTRY(NAME, CT, T, CPLX, MODE)                                                             \
+    KFR_API_SPEC size_t NAME(CT* out, const CT* a, size_t na, const CT* b, size_t nb)                        \
+    {                                                                                                       \
+        return try_fn([&] { return convolve_any<T>(out, a, na, b, nb, CPLX, MODE); }, size_t(0));           \
+    }
+KFR_CONV_ENTRY(kfr_convolve_f32, kfr_f32, float, false, 0)
+KFR_CONV_ENTRY(kfr_convolve_f64, kfr_f64, double, false, 0)
+KFR_CONV_ENTRY(kfr_convolve_c32, kfr_c32, float, true, 0)
+KFR_CONV_ENTRY(kfr_convolve_c64, kfr_c64, double, true, 0)
+KFR_CONV_ENTRY(kfr_correlate_f32, kfr_f32, float, false, 1)
+KFR_CONV_ENTRY(kfr_correlate_f64, kfr_f64, double, false, 1)
+KFR_CONV_ENTRY(kfr_correlate_c32, kfr_c32, float, true, 1)
+KFR_CONV_ENTRY(kfr_correlate_c64, kfr_c64, double, true, 1)
+#undef KFR_CONV_ENTRY
+KFR_API_SPEC size_t kfr_autocorrelate_f32(kfr_f32* out, const kfr_f32* a, size_t n)
+{
+    return try_fn([&] { return autocorrelate_any<float>(out, a, n); }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_autocorrelate_f64(kfr_f64* out, const kfr_f64* a, size_t n)
+{
+    return try_fn([&] { return autocorrelate_any<double>(out, a, n); }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_cache_size(void)
+{
+    return try_fn([&] { return plan_cache::instance().size(); }, size_t(0));
+}
+KFR_API_SPEC void kfr_dft_cache_clear(void)
+{
+    try_void([&] { plan_cache::instance().clear(); });
+}
+
 KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size)
 {
     return try_fn(
         [&]
         {
-            const std::string d = as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.describe();
+            const std::string d = as<dft_obj<float>>(plan, TAG_DFT_F32)->describe();
             if (buf && size)
             {
                 const size_t n = std::min(size - 1, d.size());
@@ -513,7 +699,7 @@ KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size
 }
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch)
 {
-    return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->eng.launches(batch)); }, size_t(0));
+    return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->launches(batch)); }, size_t(0));
 }
 
 } // extern "C"
@@ -533,19 +719,19 @@ void run_static_scratch_f32(void* plan, size_t batch, void* out, const void* in,
                 return;
             if (!is_device_ptr(in) || !is_device_ptr(out))
                 throw std::invalid_argument("kfr_dft_execute_static_scratch_f32 needs device pointers for in and out");
-            const size_t need = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(float);
+            const size_t need = size_t(p->scratch_elems((long long)batch)) * 2 * sizeof(float);
             if (need > scratch_limit)
                 throw std::invalid_argument("kfr_dft_execute_static_scratch_f32: this plan and batch need " +
                                             std::to_string(need) + " bytes of scratch, more than the " +
                                             std::to_string(scratch_limit) + "-byte static scratch");
             void* scr       = need ? scratch_of() : nullptr;
             cudaStream_t st = static_cast<cudaStream_t>(stream);
-            p->eng.execute(out, in, (long long)batch, (long long)p->n, (long long)p->n, inverse, scr, st);
+            p->execute(out, in, (long long)batch, inverse, scr, st);
             check(cudaGetLastError(), "kernel launch");
             if (!stream)
             {
                 check(cudaStreamSynchronize(st), "execute");
-                p->eng.check_device_error();
+                p->check_device_error();
             }
         });
 }
@@ -575,43 +761,43 @@ KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_plan_f64(size_t size, KF
         [&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F64*>(static_cast<plan_base*>(new real_obj<double>(size, fmt == CCs))); },
         (KFR_DFT_REAL_PLAN_F64*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_2d_plan_f32(size_t, size_t, kfr_bool)
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_2d_plan_f32(size_t size1, size_t size2, kfr_bool real_out_is_enough)
 {
-    return try_fn([]() -> KFR_DFT_REAL_PLAN_F32* { not_built("kfr_dft_real_create_2d_plan_f32"); },
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F32*>(static_cast<plan_base*>(new real_obj<float>(std::vector<long long>{ (long long)size1, (long long)size2 }, real_out_is_enough))); },
                   (KFR_DFT_REAL_PLAN_F32*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_3d_plan_f32(size_t, size_t, size_t, kfr_bool)
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_3d_plan_f32(size_t size1, size_t size2, size_t size3, kfr_bool real_out_is_enough)
 {
-    return try_fn([]() -> KFR_DFT_REAL_PLAN_F32* { not_built("kfr_dft_real_create_3d_plan_f32"); },
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F32*>(static_cast<plan_base*>(new real_obj<float>(std::vector<long long>{ (long long)size1, (long long)size2, (long long)size3 }, real_out_is_enough))); },
                   (KFR_DFT_REAL_PLAN_F32*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_md_plan_f32(size_t, const unsigned*, kfr_bool)
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F32* kfr_dft_real_create_md_plan_f32(size_t dims, const unsigned* shape, kfr_bool real_out_is_enough)
 {
-    return try_fn([]() -> KFR_DFT_REAL_PLAN_F32* { not_built("kfr_dft_real_create_md_plan_f32"); },
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F32*>(static_cast<plan_base*>(new real_obj<float>(to_shape(dims, shape), real_out_is_enough))); },
                   (KFR_DFT_REAL_PLAN_F32*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_2d_plan_f64(size_t, size_t, kfr_bool)
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_2d_plan_f64(size_t size1, size_t size2, kfr_bool real_out_is_enough)
 {
-    return try_fn([]() -> KFR_DFT_REAL_PLAN_F64* { not_built("kfr_dft_real_create_2d_plan_f64"); },
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F64*>(static_cast<plan_base*>(new real_obj<double>(std::vector<long long>{ (long long)size1, (long long)size2 }, real_out_is_enough))); },
                   (KFR_DFT_REAL_PLAN_F64*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_3d_plan_f64(size_t, size_t, size_t, kfr_bool)
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_3d_plan_f64(size_t size1, size_t size2, size_t size3, kfr_bool real_out_is_enough)
 {
-    return try_fn([]() -> KFR_DFT_REAL_PLAN_F64* { not_built("kfr_dft_real_create_3d_plan_f64"); },
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F64*>(static_cast<plan_base*>(new real_obj<double>(std::vector<long long>{ (long long)size1, (long long)size2, (long long)size3 }, real_out_is_enough))); },
                   (KFR_DFT_REAL_PLAN_F64*)nullptr);
 }
-KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_md_plan_f64(size_t, const unsigned*, kfr_bool)
+KFR_API_SPEC KFR_DFT_REAL_PLAN_F64* kfr_dft_real_create_md_plan_f64(size_t dims, const unsigned* shape, kfr_bool real_out_is_enough)
 {
-    return try_fn([]() -> KFR_DFT_REAL_PLAN_F64* { not_built("kfr_dft_real_create_md_plan_f64"); },
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_REAL_PLAN_F64*>(static_cast<plan_base*>(new real_obj<double>(to_shape(dims, shape), real_out_is_enough))); },
                   (KFR_DFT_REAL_PLAN_F64*)nullptr);
 }
 KFR_API_SPEC void kfr_dft_real_dump_f32(KFR_DFT_REAL_PLAN_F32* plan)
 {
-    try_void([&] { print_line(as<real_obj<float>>(plan, TAG_REAL_F32)->eng.describe()); });
+    try_void([&] { print_line(as<real_obj<float>>(plan, TAG_REAL_F32)->describe()); });
 }
 KFR_API_SPEC void kfr_dft_real_dump_f64(KFR_DFT_REAL_PLAN_F64* plan)
 {
-    try_void([&] { print_line(as<real_obj<double>>(plan, TAG_REAL_F64)->eng.describe()); });
+    try_void([&] { print_line(as<real_obj<double>>(plan, TAG_REAL_F64)->describe()); });
 }
 KFR_API_SPEC size_t kfr_dft_real_get_size_f32(KFR_DFT_REAL_PLAN_F32* plan)
 {
@@ -623,12 +809,12 @@ KFR_API_SPEC size_t kfr_dft_real_get_size_f64(KFR_DFT_REAL_PLAN_F64* plan)
 }
 KFR_API_SPEC size_t kfr_dft_real_get_temp_size_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch)
 {
-    return try_fn([&] { return size_t(as<real_obj<float>>(plan, TAG_REAL_F32)->eng.scratch_elems(batch)) * 8; },
+    return try_fn([&] { return size_t(as<real_obj<float>>(plan, TAG_REAL_F32)->scratch_elems(batch)) * 8; },
                   size_t(0));
 }
 KFR_API_SPEC size_t kfr_dft_real_get_temp_size_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch)
 {
-    return try_fn([&] { return size_t(as<real_obj<double>>(plan, TAG_REAL_F64)->eng.scratch_elems(batch)) * 16; },
+    return try_fn([&] { return size_t(as<real_obj<double>>(plan, TAG_REAL_F64)->scratch_elems(batch)) * 16; },
                   size_t(0));
 }
 KFR_API_SPEC size_t kfr_dft_real_get_temp_size_f32(KFR_DFT_REAL_PLAN_F32* plan)

@@ -629,6 +629,18 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_cols(const fourstep_ar
     __syncthreads();
     const group_map gm(ts, S);
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
+    if (a.same_layout)
+    {
+        // an axis of a multi-dimensional transform: no twiddle, back to the input's own layout
+        for (int i = threadIdx.x; i < total; i += blockDim.x)
+        {
+            const int k1 = i >> sh;
+            const int c  = i & (S - 1);
+            if (c0 + c < n2)
+                y[(long long)k1 * n2 + c0 + c] = conj_if(sm[c * stride + pidx<T>(k1)], a.conj_out != 0);
+        }
+        return;
+    }
     const cpx<T>* twA = reinterpret_cast<const cpx<T>*>(a.twA);
     const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
     for (int i = threadIdx.x; i < total; i += blockDim.x)

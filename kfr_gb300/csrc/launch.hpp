@@ -120,6 +120,7 @@ struct fourstep_args
     const void* twB;
     int lbits;
     int tile_shift;  // log2(tile)
+    int same_layout; // cols pass: store back to x's own layout (multi-dimensional axes) and skip the twiddle
     fast_div div_n;  // divides by the FFT length of this pass
 };
 

@@ -1,0 +1,78 @@
+// Multi-dimensional DFTs: dft_plan_md<T> and dft_plan_md_real<T> (include/kfr/dft/fft.hpp:568-924).
+//
+// The reference transforms the last axis of a row-major array, transposes, and repeats for every axis.  On
+// the GPU no transpose is needed: the last axis runs as a batched 1-D transform over contiguous rows, and
+// every other axis i runs in place as a column pass over the [outer][n_i][inner] view (tiles of adjacent
+// columns are staged in shared memory, transformed, and written back to the same places).  The real
+// variant does the CCs real DFT along the last axis first (forward) or last (inverse), like the reference,
+// so the complex array has the reference's complex_size() shape (last axis N/2 + 1).
+#pragma once
+
+#include "plan.hpp"
+
+namespace kfr_gpu
+{
+
+template <typename T>
+class md_axes
+{
+public:
+    // Axes 0 .. dims-2 of `cshape` (complex element shape) with length > 1.
+    explicit md_axes(const std::vector<long long>& cshape);
+    // In place on `data` (batch arrays of the complex shape back to back).
+    void run(void* data, long long batch, bool inverse, cudaStream_t st) const;
+    int launches() const { return int(axes_.size()); }
+    std::string describe() const;
+
+private:
+    struct axis
+    {
+        long long n, inner, outer;
+        int tile;
+        std::unique_ptr<block_program<T>> prog;
+    };
+    std::vector<axis> axes_;
+};
+
+template <typename T>
+class md_engine
+{
+public:
+    explicit md_engine(const std::vector<long long>& shape);
+    long long size() const { return total_; }
+    const std::vector<long long>& shape() const { return shape_; }
+    long long scratch_elems(long long batch) const;
+    void execute(void* out, const void* in, long long batch, bool inverse, void* scratch, cudaStream_t st) const;
+    std::string describe() const;
+    int launches(long long batch) const;
+
+private:
+    std::vector<long long> shape_;
+    long long total_ = 0;
+    std::unique_ptr<complex_engine<T>> last_;
+    md_axes<T> axes_;
+};
+
+template <typename T>
+class md_real_engine
+{
+public:
+    md_real_engine(const std::vector<long long>& shape, bool real_out_is_enough);
+    long long size() const { return total_real_; }
+    long long complex_size() const { return total_cplx_; }
+    const std::vector<long long>& shape() const { return shape_; }
+    long long scratch_elems(long long batch) const;
+    void forward(void* out, const void* in, long long batch, void* scratch, cudaStream_t st) const;
+    void inverse(void* out, const void* in, long long batch, void* scratch, cudaStream_t st) const;
+    std::string describe() const;
+    int launches(long long batch) const;
+
+private:
+    std::vector<long long> shape_, cshape_;
+    long long total_real_ = 0, total_cplx_ = 0;
+    bool real_out_is_enough_;
+    std::unique_ptr<real_engine<T>> last_;
+    md_axes<T> axes_;
+};
+
+} // namespace kfr_gpu

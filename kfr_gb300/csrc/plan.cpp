@@ -265,7 +265,7 @@ static int ilog2(int x)
     return s;
 }
 
-static int smem_budget()
+int smem_budget()
 {
     // dynamic shared memory left after the static pass-descriptor array and a small reserve
     static const int budget = max_smem_bytes() - int(sizeof(pass_desc)) * kMaxPasses - 1024;
@@ -700,7 +700,7 @@ void complex_engine<T>::init_bluestein(long long n)
 }
 
 template <typename T>
-static int tile_for(const block_program<T>& p)
+int tile_for(const block_program<T>& p)
 {
     const int per_sig = padded_len_host<T>(p.n) * int(2 * sizeof(T));
     const int max_thr = p.ct ? (sizeof(T) == 4 ? 1024 : 512) : max_threads_for(int(sizeof(T)), p.ept);
@@ -946,6 +946,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             a.sig_stride = n_;
             a.n1         = int(n1_);
             a.n2         = int(n2_);
+            a.same_layout = 0;
             a.twA        = twA_.get();
             a.twB        = twB_.get();
             a.lbits      = lbits_;
@@ -1266,6 +1267,8 @@ std::string dct_engine<T>::describe() const
     return s.str();
 }
 
+template int tile_for<float>(const block_program<float>&);
+template int tile_for<double>(const block_program<double>&);
 template struct block_program<float>;
 template struct block_program<double>;
 template class complex_engine<float>;

@@ -109,6 +109,13 @@ struct block_program
     std::string describe() const;
 };
 
+// Dynamic shared memory a block FFT kernel may use (device limit less the static pass list and a reserve).
+int smem_budget();
+// Largest power-of-two number of signals (<= 16) of `p` that fit one CTA: the column / row tile of the
+// strided passes.  0 if not even one fits.
+template <typename T>
+int tile_for(const block_program<T>& p);
+
 template <typename T>
 class complex_engine
 {

@@ -144,6 +144,34 @@ class Oracle:
         n = self._fn("convolve", rdt)(_p(out), _p(a), len(a), _p(b), len(b), int(correlate), int(is_complex))
         return out[:n]
 
+    # ---- multi-dimensional (reference library only) ---------------------------------------------------
+    def dft_md(self, x, inverse=False):
+        """dft_plan_md<double> over the whole array (reference build only)."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        shp = (ctypes.c_uint * x.ndim)(*x.shape)
+        out = np.empty_like(x)
+        f = self.lib.ref_dft_md_f64
+        f.restype = _c_int
+        f.argtypes = [_ptr, _ptr, _c_size, _ptr, _c_int]
+        f(_p(out), _p(x), x.ndim, ctypes.cast(shp, _ptr), int(inverse))
+        return out
+
+    def dft_md_real(self, x, inverse=False, shape=None, real_out_is_enough=False):
+        """dft_plan_md_real<double>: forward real -> CCs complex (last axis N/2+1), inverse back (reference only)."""
+        f = self.lib.ref_dft_md_real_f64
+        f.restype = _c_int
+        f.argtypes = [_ptr, _ptr, _c_size, _ptr, _c_int, _c_int]
+        if not inverse:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            shape = x.shape
+            out = np.zeros(shape[:-1] + (shape[-1] // 2 + 1,), dtype=np.complex128)
+        else:
+            x = np.ascontiguousarray(x, dtype=np.complex128)
+            out = np.zeros(shape, dtype=np.float64)
+        shp = (ctypes.c_uint * len(shape))(*shape)
+        f(_p(out), _p(x), len(shape), ctypes.cast(shp, _ptr), int(inverse), int(real_out_is_enough))
+        return out
+
     def filter(self, taps, block=1024, precision="f64"):
         return _Filter(self, taps, block, precision)
 

@@ -119,6 +119,34 @@ size_t run_convolve(T* out, const T* a, size_t na, const T* b, size_t nb, int co
     return r.size();
 }
 
+template <typename T>
+int run_md(T* out, const T* in, size_t dims, const unsigned* shp, int inverse)
+{
+    shape<dynamic_shape> sh(dims);
+    for (size_t i = 0; i < dims; i++)
+        sh[i] = shp[i];
+    dft_plan_md<T, dynamic_shape> plan(sh);
+    univector<u8> temp(plan.temp_size);
+    plan.execute(reinterpret_cast<complex<T>*>(out), reinterpret_cast<const complex<T>*>(in), temp.data(),
+                 inverse != 0);
+    return 0;
+}
+
+template <typename T>
+int run_md_real(T* out, const T* in, size_t dims, const unsigned* shp, int inverse, int real_out_is_enough)
+{
+    shape<dynamic_shape> sh(dims);
+    for (size_t i = 0; i < dims; i++)
+        sh[i] = shp[i];
+    dft_plan_md_real<T, dynamic_shape> plan(sh, real_out_is_enough != 0);
+    univector<u8> temp(plan.temp_size);
+    if (!inverse)
+        plan.execute(reinterpret_cast<complex<T>*>(out), in, temp.data(), cdirect_t{});
+    else
+        plan.execute(out, reinterpret_cast<const complex<T>*>(in), temp.data(), cinvert_t{});
+    return 0;
+}
+
 struct any_filter
 {
     int is_complex;
@@ -229,6 +257,18 @@ void filter_delete(void* vh)
 
 REF_API(double, _f64)
 REF_API(float, _f32)
+
+extern "C" __attribute__((visibility("default"))) int ref_dft_md_f64(double* out, const double* in, size_t dims,
+                                                                     const unsigned* shape, int inverse)
+{
+    return run_md<double>(out, in, dims, shape, inverse);
+}
+extern "C" __attribute__((visibility("default"))) int ref_dft_md_real_f64(double* out, const double* in, size_t dims,
+                                                                          const unsigned* shape, int inverse,
+                                                                          int real_out_is_enough)
+{
+    return run_md_real<double>(out, in, dims, shape, inverse, real_out_is_enough);
+}
 
 extern "C" __attribute__((visibility("default"))) void ref_dft_dump_f32(size_t n)
 {

@@ -126,6 +126,27 @@ def main() -> None:
             fc[f"fnchunks_{kind}_{i}"] = np.array(len(chunks))
     fc["nfilters"] = np.array(len(cases))
     np.savez_compressed(os.path.join(HERE, "convolution.npz"), **fc)
+
+    # ---- multi-dimensional complex and real DFT (dft_plan_md / dft_plan_md_real) ---------------------
+    fm = {}
+    md_shapes = [(4, 8), (3, 5, 7), (16, 16), (6, 10), (2, 3, 4, 5), (1, 7), (8, 1), (32, 6), (5, 2, 2, 3, 2)]
+    for i, shp in enumerate(md_shapes):
+        x = rng.uniform(-1, 1, shp) + 1j * rng.uniform(-1, 1, shp)
+        fm[f"x_{i}"] = x
+        fm[f"fwd_{i}"] = ref.dft_md(x)
+        fm[f"inv_{i}"] = ref.dft_md(x, inverse=True)
+    fm["n"] = np.array(len(md_shapes))
+    md_real_shapes = [(4, 8), (3, 5, 6), (16, 16), (6, 10), (2, 3, 4, 6), (7, 2), (1, 12)]
+    for i, shp in enumerate(md_real_shapes):
+        x = rng.standard_normal(shp)
+        fm[f"rx_{i}"] = x
+        X = ref.dft_md_real(x)
+        fm[f"rfwd_{i}"] = X
+        S = rng.standard_normal(X.shape) + 1j * rng.standard_normal(X.shape)
+        fm[f"rspec_{i}"] = S
+        fm[f"rinv_{i}"] = ref.dft_md_real(S, inverse=True, shape=shp)
+    fm["nr"] = np.array(len(md_real_shapes))
+    np.savez_compressed(os.path.join(HERE, "dft_md.npz"), **fm)
     print("golden fixtures written to", HERE)
 
 
