@@ -86,3 +86,28 @@ def test_host_allocation_without_gpu(L):
 def test_out_of_scope_filters_report_errors(L):
     assert not L.kfr_filter_create_fir_plan_f32(None, 0)
     assert b"not part of the GPU DFT path" in L.kfr_last_error()
+
+
+def test_cpp_api_header_compiles_against_reference_style_code():
+    """include/kfr_dft.hpp mirrors KFR's C++ DFT interface; tests/cpp/test_cpp_api.cpp is written against it
+    the way reference users write against kfr/dft.hpp.  Compile-only here (no GPU)."""
+    import subprocess
+
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "test_cpp_api.cpp")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_c_header_compiles_as_c():
+    """The C ABI header is valid C (C99, _Complex element types)."""
+    import subprocess
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        with open(src, "w") as f:
+            f.write('#include "kfr_capi.h"\nint main(void) { KFR_DFT_PLAN_F32* p = kfr_dft_create_plan_f32(8);'
+                    ' kfr_dft_delete_plan_f32(p); return 0; }\n')
+        r = subprocess.run(["gcc", "-std=c99", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), src],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
