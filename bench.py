@@ -40,8 +40,8 @@ METRIC = "batched c32 DFT GB/s (% of HBM roofline), chosen vs plain form at ≤1
 FALLBACK_HBM_GBS = 6800.0
 
 # DRAM bytes per signal measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided
-# by the signals it processed) at the full 256 MiB batch; the captures are summarised in
-# profiles/k_rader_pipe_8191.md and profiles/k_fs_cols_rows_30720_k_rader_127.md.
+# by the signals it processed) at the full 256 MiB batch, from the --set full captures of the k_rader_pipe,
+# k_rader and k_fs_cols / k_fs_rows launches summarised under profiles/.
 NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float] = {
     8191: (271_920_896 + 229_835_264) / 4095,
     127: (268_492_800 + 222_380_800) / 264208,
