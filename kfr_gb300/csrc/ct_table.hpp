@@ -1,6 +1,6 @@
 // Lengths with compile-time specialised block FFTs (single precision).  Each entry is
 //   X(N, TS, radices...)   N = product of the radices, TS = threads per signal
-// chosen so that no thread holds more than 16 complex values in any pass.  The planner uses an entry when
+// chosen so that no thread holds more than 18 complex values in any pass.  The planner uses an entry when
 // the kernel kind and length match (block_program::build then lays the twiddles out in this radix order);
 // every other length runs the runtime-radix kernel.  Lists are per kernel kind to bound compile time:
 // they cover the parity and benchmark configurations and the power-of-two lengths up to 16384.
@@ -31,10 +31,11 @@
     X(8192, 512, 16, 16, 16, 2)                                                                              \
     X(16384, 1024, 16, 16, 16, 4)
 
-// convolution lengths L = n - 1 of the one-CTA Rader kernel for prime n (127, 8191)
+// convolution lengths L = n - 1 of the one-CTA Rader kernels for prime n (127, 8191); 14 and 10 are the
+// Good-Thomas composite codelets
 #define KFR_CT_RADER_F32(X)                                                                                 \
-    X(126, 16, 9, 7, 2)                                                                                      \
-    X(8190, 1024, 13, 9, 7, 5, 2)
+    X(126, 9, 14, 9)                                                                                         \
+    X(8190, 1024, 13, 9, 7, 10)
 
 // four-step pass lengths (columns and rows): the factors of 30720 = 160 x 192 and of the power-of-two
 // lengths 2^15 .. 2^24

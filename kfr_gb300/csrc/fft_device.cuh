@@ -287,6 +287,55 @@ __device__ __forceinline__ constexpr int codelet_out(int r)
 }
 
 template <typename T, int R>
+__device__ __forceinline__ void dft_codelet(cpx<T>* v);
+
+// Composite radices with coprime factors R = R1 * R2 (6, 10, 12, 14, 15, 18), by the Good-Thomas prime
+// factor algorithm: no twiddles between the two stages, only index maps that fold to register moves.
+//   input  n = (R2 n1 + R1 n2) mod R
+//   output k = (R2 e2 k1 + R1 e1 k2) mod R,  e2 = R2^-1 mod R1, e1 = R1^-1 mod R2
+template <int R1, int R2>
+struct pfa_split
+{
+    static constexpr int inv_mod(int a, int m)
+    {
+        for (int x = 1; x < m; x++)
+            if ((a * x) % m == 1)
+                return x;
+        return 1;
+    }
+    static constexpr int e2 = inv_mod(R2 % R1, R1);
+    static constexpr int e1 = inv_mod(R1 % R2, R2);
+};
+
+template <typename T, int R1, int R2>
+__device__ __forceinline__ void dft_pfa(cpx<T>* v)
+{
+    constexpr int R = R1 * R2;
+    using S         = pfa_split<R1, R2>;
+    cpx<T> u[R1][R2];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; n1++)
+    {
+#pragma unroll
+        for (int n2 = 0; n2 < R2; n2++)
+            u[n1][n2] = v[(R2 * n1 + R1 * n2) % R];
+        dft_codelet<T, R2>(u[n1]);
+    }
+#pragma unroll
+    for (int k2 = 0; k2 < R2; k2++)
+    {
+        cpx<T> w[R1];
+#pragma unroll
+        for (int n1 = 0; n1 < R1; n1++)
+            w[n1] = u[n1][codelet_out<R2>(k2)];
+        dft_codelet<T, R1>(w);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++)
+            v[(R2 * S::e2 * k1 + R1 * S::e1 * k2) % R] = w[codelet_out<R1>(k1)];
+    }
+}
+
+template <typename T, int R>
 __device__ __forceinline__ void dft_codelet(cpx<T>* v)
 {
     if constexpr (R == 2)
@@ -297,6 +346,18 @@ __device__ __forceinline__ void dft_codelet(cpx<T>* v)
         dft8(v);
     else if constexpr (R == 16)
         dft16(v);
+    else if constexpr (R == 6)
+        dft_pfa<T, 2, 3>(v);
+    else if constexpr (R == 10)
+        dft_pfa<T, 2, 5>(v);
+    else if constexpr (R == 12)
+        dft_pfa<T, 4, 3>(v);
+    else if constexpr (R == 14)
+        dft_pfa<T, 2, 7>(v);
+    else if constexpr (R == 15)
+        dft_pfa<T, 3, 5>(v);
+    else if constexpr (R == 18)
+        dft_pfa<T, 2, 9>(v);
     else
         dft_odd<T, R>(v);
 }
@@ -672,6 +733,165 @@ __device__ __forceinline__ void ct_block_fft_io(const cpx<T>* src, cpx<T>* work,
     const int lta     = lt < TS ? lt : N;
     cpx<T> v[EPT];
     ct_passes_io<T, N, TS, EPT, 1, 0, Rs...>(v, src, work, gout, tw, cj, lta);
+}
+
+// Compile-time block FFT with caller-supplied access to the transform's input and output: ld(p) fetches
+// input p of the first pass, st(q, x) stores output q of the last pass, and the passes in between work in
+// the padded buffer `work`.  hook() runs once, after the first pass's closing barrier (the input has been
+// consumed by then).  SEP_IN: ld reads memory that the first pass does not write; SEP_OUT: st writes
+// memory that the last pass does not read; each saves the barrier between that pass's loads and stores.
+// Ends with a barrier.
+template <typename T, int N, int TS, int EPT, int R, int NS, int TWOFF, bool SYNC_MID, class LD, class ST>
+__device__ __forceinline__ void ct_pass_fx(cpx<T> (&v)[EPT], const LD& ld, const ST& st,
+                                           const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int NBF = N / R;
+    constexpr int NB  = (NBF + TS - 1) / TS;
+    static_assert(NB * R <= EPT, "register array too small");
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[b * R + r] = ld(j + r * NBF);
+            if constexpr (NS > 1)
+            {
+                const int k     = j % NS;
+                const cpx<T>* t = tw + TWOFF + k;
+#pragma unroll
+                for (int r = 1; r < R; r++)
+                    v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * NS);
+            }
+            dft_codelet<T, R>(&v[b * R]);
+        }
+    }
+    if constexpr (SYNC_MID)
+        __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+            const int k = NS > 1 ? j % NS : 0;
+            const int d = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                st(d + r * NS, v[b * R + codelet_out<R>(r)]);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int N, int TS, int EPT, int NS, int TWOFF, bool SEP_IN, bool SEP_OUT, class LD, class ST,
+          class H, int R, int... Rest>
+__device__ __forceinline__ void ct_chain_fx(cpx<T> (&v)[EPT], const LD& ld, const ST& st, const H& hook,
+                                            cpx<T>* work, const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int TWNEXT = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
+    const auto wld       = [work](int p) { return work[pidx<T>(p)]; };
+    const auto wst       = [work](int q, cpx<T> x) { work[pidx<T>(q)] = x; };
+    if constexpr (NS == 1 && sizeof...(Rest) == 0)
+    {
+        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, !(SEP_IN || SEP_OUT)>(v, ld, st, tw, lt);
+        hook();
+    }
+    else if constexpr (NS == 1)
+    {
+        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, !SEP_IN>(v, ld, wst, tw, lt);
+        hook();
+        ct_chain_fx<T, N, TS, EPT, R, TWNEXT, false, SEP_OUT, decltype(wld), ST, H, Rest...>(v, wld, st, hook, work,
+                                                                                            tw, lt);
+    }
+    else if constexpr (sizeof...(Rest) == 0)
+        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, !SEP_OUT>(v, ld, st, tw, lt);
+    else
+    {
+        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, true>(v, ld, wst, tw, lt);
+        ct_chain_fx<T, N, TS, EPT, NS * R, TWNEXT, false, SEP_OUT, LD, ST, H, Rest...>(v, ld, st, hook, work, tw, lt);
+    }
+}
+
+template <typename T, int N, int TS, bool SEP_IN, bool SEP_OUT, int... Rs, class LD, class ST, class H>
+__device__ __forceinline__ void ct_block_fft_fx(const LD& ld, const ST& st, const H& hook, cpx<T>* work,
+                                                const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int EPT = ct_ept<N, TS, Rs...>();
+    const int lta     = lt < TS ? lt : N;
+    cpx<T> v[EPT];
+    ct_chain_fx<T, N, TS, EPT, 1, 0, SEP_IN, SEP_OUT, LD, ST, H, Rs...>(v, ld, st, hook, work, tw, lta);
+}
+
+// Ping-pong compile-time block FFT: pass i reads buffer A (i even) or B (i odd) and writes the other, so a
+// pass needs one barrier and each butterfly's outputs are stored as soon as they are computed (no register
+// array spans the pass).  ld(p) fetches input p of the first pass, st(q, x) stores output q of the last
+// pass (which writes A when the number of passes is even, else B); the passes in between use the padded
+// layouts of A and B.  hook() runs once, after the first pass's closing barrier.  Ends with a barrier.
+template <typename T, int N, int TS, int R, int NS, int TWOFF, class LD, class ST>
+__device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int NBF = N / R;
+    constexpr int NB  = (NBF + TS - 1) / TS;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+            cpx<T> v[R];
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[r] = ld(j + r * NBF);
+            const int k = NS > 1 ? j % NS : 0;
+            if constexpr (NS > 1)
+            {
+                const cpx<T>* t = tw + TWOFF + k;
+#pragma unroll
+                for (int r = 1; r < R; r++)
+                    v[r] = v[r] * ldg(t + (r - 1) * NS);
+            }
+            dft_codelet<T, R>(v);
+            const int d = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                st(d + r * NS, v[codelet_out<R>(r)]);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int N, int TS, int NS, int TWOFF, int I, class LD, class ST, class H, int R, int... Rest>
+__device__ __forceinline__ void pp_chain(const LD& ld, const ST& st, const H& hook, cpx<T>* A, cpx<T>* B,
+                                         const cpx<T>* __restrict__ tw, const int lt)
+{
+    if constexpr (sizeof...(Rest) == 0)
+    {
+        pp_pass<T, N, TS, R, NS, TWOFF>(ld, st, tw, lt);
+        if constexpr (NS == 1)
+            hook();
+    }
+    else
+    {
+        cpx<T>* dst      = (I % 2 == 0) ? B : A;
+        const auto d_st  = [dst](int q, cpx<T> x) { dst[pidx<T>(q)] = x; };
+        const auto d_ld  = [dst](int p) { return dst[pidx<T>(p)]; };
+        constexpr int TN = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
+        pp_pass<T, N, TS, R, NS, TWOFF>(ld, d_st, tw, lt);
+        if constexpr (NS == 1)
+            hook();
+        pp_chain<T, N, TS, NS * R, TN, I + 1, decltype(d_ld), ST, H, Rest...>(d_ld, st, hook, A, B, tw, lt);
+    }
+}
+
+template <typename T, int N, int TS, int... Rs, class LD, class ST, class H>
+__device__ __forceinline__ void ct_block_fft_pp(const LD& ld, const ST& st, const H& hook, cpx<T>* A, cpx<T>* B,
+                                                const cpx<T>* __restrict__ tw, const int lt)
+{
+    const int lta = lt < TS ? lt : N;
+    pp_chain<T, N, TS, 1, 0, 0, LD, ST, H, Rs...>(ld, st, hook, A, B, tw, lta);
 }
 
 // Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a

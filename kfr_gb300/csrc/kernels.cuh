@@ -53,6 +53,19 @@ struct ct_fft
     {
         ct_block_fft_io<T, N, TS, Rs...>(src, work, gout, tw, cj, lt);
     }
+    static constexpr int npass = sizeof...(Rs);
+    template <class LD, class ST, class H>
+    __device__ __forceinline__ void run_pp(const LD& ld, const ST& st, const H& hook, cpx<T>* A, cpx<T>* B,
+                                           const cpx<T>* __restrict__ tw, int lt) const
+    {
+        ct_block_fft_pp<T, N, TS, Rs...>(ld, st, hook, A, B, tw, lt);
+    }
+    template <bool SEP_IN, bool SEP_OUT, class LD, class ST, class H>
+    __device__ __forceinline__ void run_fx(const LD& ld, const ST& st, const H& hook, cpx<T>* work,
+                                           const cpx<T>* __restrict__ tw, int lt) const
+    {
+        ct_block_fft_fx<T, N, TS, SEP_IN, SEP_OUT, Rs...>(ld, st, hook, work, tw, lt);
+    }
 };
 
 __device__ __forceinline__ uint32_t div_by(uint32_t x, const fast_div f) { return fdiv(x, f); }
@@ -304,91 +317,148 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Rader, persistent and pipelined (compile-time L, one signal per iteration).  The signal's bytes arrive in
-// a shared stage buffer by TMA; the bulk copy covers the enclosing 16-byte-aligned range, so an odd-length
-// signal sits one element into the stage.  The permutation into the convolution input reads the stage, after
-// which the next signal's copy is issued and overlaps the two L-point DFTs and the gathered store.
+// Rader over tiles of `spc` whole signals, persistent and pipelined (compile-time L).  A tile's bytes are
+// contiguous: one bulk copy (TMA) brings the enclosing 16-byte-aligned range into one of two stage buffers,
+// and the tile's output leaves the same way from the same buffer.  The two L-point DFTs run ping-pong
+// between the stage buffer and a work buffer (one barrier per pass).  Per signal:
+//   first DFT:  pass 1 gathers a[p] = x[g^p] straight from the staged input; the last pass stores
+//               conj(A[q] * bhat[q]) and keeps A[0] (= sum of x[1..n-1]);
+//   second DFT: the last pass scatters X[g^-q] = x[0] + conj(C[q]) into the stage in the input's layout
+//               (g^-q = gp[L - q]);
+//   X[0] = x[0] + A[0].
+// The next tile's load goes to the other stage buffer as soon as the first pass is done (once the bulk
+// store that last read that buffer has finished reading it) and overlaps both DFTs of the current tile.
 // ---------------------------------------------------------------------------------------------------
 template <typename T, class F>
+__host__ __device__ constexpr int rader_stage_elems(int spc)
+{
+    return rader_stage_len(spc, F::n + 1, padded_len<T>(F::n));
+}
+
+template <typename T, class F>
 __global__ void __launch_bounds__(F::max_threads, 1)
-    k_rader_pipe(const rader_args a, const long long nsig, int* err)
+    k_rader_tile(const rader_args a, const long long ntiles, const int spc, int* err)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int L      = F::n;
     constexpr int N      = L + 1;
     constexpr int STRIDE = padded_len<T>(L);
-    constexpr int STAGE  = ((N * int(sizeof(cpx<T>)) + 31) / 16) * 16 / int(sizeof(cpx<T>));
+    constexpr int ESZ    = int(sizeof(cpx<T>));
+    const int stage_elems = rader_stage_elems<T, F>(spc);
+    cpx<T>* st0    = reinterpret_cast<cpx<T>*>(smem_raw);
+    cpx<T>* st1    = st0 + stage_elems;
+    cpx<T>* work   = st1 + stage_elems;
+    cpx<T>* x0s    = work + spc * STRIDE;
+    cpx<T>* dcs    = x0s + spc;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(dcs + spc);
     const F fft(nullptr, a.d, F::ts);
-    cpx<T>* stage = reinterpret_cast<cpx<T>*>(smem_raw);
-    cpx<T>* work  = stage + STAGE;
-    cpx<T>* misc  = work + STRIDE; // x0, dc
-    uint64_t* bar = reinterpret_cast<uint64_t*>(misc + 2);
-    const char* inb = reinterpret_cast<const char*>(a.in);
-    cpx<T>* out     = reinterpret_cast<cpx<T>*>(a.out);
+    const long long tile_bytes      = (long long)spc * N * ESZ;
+    const char* inb                 = reinterpret_cast<const char*>(a.in);
+    char* outb                      = reinterpret_cast<char*>(a.out);
     const cpx<T>* __restrict__ bhat = reinterpret_cast<const cpx<T>*>(a.bhat);
-    const cpx<T>* tw                = reinterpret_cast<const cpx<T>*>(a.tw);
-    const bool inv = a.inverse != 0;
-    const int lt   = int(threadIdx.x) < F::ts ? int(threadIdx.x) : F::ts;
-    constexpr long long SIG_BYTES = (long long)N * sizeof(cpx<T>);
+    const cpx<T>* __restrict__ tw   = reinterpret_cast<const cpx<T>*>(a.tw);
+    const int* __restrict__ gp      = a.gp;
+    const bool inv                  = a.inverse != 0;
+    const group_map gm(F::ts, spc);
     if (threadIdx.x == 0)
     {
-        mbar_init(bar, 1);
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
         mbar_fence_init();
     }
     __syncthreads();
     long long t = blockIdx.x;
-    if (threadIdx.x == 0 && t < nsig)
+    if (threadIdx.x == 0 && t < ntiles)
     {
-        const long long s0 = t * SIG_BYTES, a0 = s0 & ~15LL, a1 = (s0 + SIG_BYTES + 15) & ~15LL;
-        mbar_arrive_expect_tx(bar, uint32_t(a1 - a0));
-        bulk_g2s(stage, inb + a0, uint32_t(a1 - a0), bar);
+        const long long s0 = t * tile_bytes, a0 = s0 & ~15LL, a1 = (s0 + tile_bytes + 15) & ~15LL;
+        mbar_arrive_expect_tx(&bars[0], uint32_t(a1 - a0));
+        bulk_g2s(st0, inb + a0, uint32_t(a1 - a0), &bars[0]);
     }
-    uint32_t phase = 0;
-    for (; t < nsig; t += gridDim.x)
+    uint32_t phase   = 0;
+    uint32_t pending = t < ntiles ? 1 : 0;
+    int it           = 0;
+    for (; t < ntiles; t += gridDim.x, it++)
     {
-        const bool got = mbar_wait(bar, phase);
+        const int sb   = it & 1;
+        cpx<T>* stage  = sb ? st1 : st0;
+        const bool got = mbar_wait(&bars[sb], (phase >> sb) & 1);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
+            {
                 atomicExch(err, 1);
+                if ((pending >> (sb ^ 1)) & 1)
+                    mbar_wait(&bars[sb ^ 1], (phase >> (sb ^ 1)) & 1);
+                bulk_wait_all();
+            }
             return;
         }
-        phase ^= 1;
-        const int off = int(((t * SIG_BYTES) & 15) / int(sizeof(cpx<T>)));
-        for (int p = threadIdx.x; p < L; p += blockDim.x)
-            work[pidx<T>(p)] = conj_if(stage[off + __ldg(a.gp + p)], inv);
-        if (threadIdx.x == 0)
-            misc[0] = conj_if(stage[off], inv);
-        __syncthreads();
+        phase ^= 1u << sb;
+        pending &= ~(1u << sb);
+        const long long s0 = t * tile_bytes;
+        const long long a0 = s0 & ~15LL;
+        const int off      = int((s0 - a0) / ESZ);
+        cpx<T>* sig        = stage + off + gm.g * N; // this signal in the input / output layout
+        cpx<T>* sp         = stage + gm.g * STRIDE;  // this signal in the padded layout
+        cpx<T>* wk         = work + gm.g * STRIDE;
+        if (gm.lt == 0)
+            x0s[gm.g] = conj_if(sig[0], inv);
         const long long tn = t + gridDim.x;
-        if (threadIdx.x == 0 && tn < nsig)
+        const auto prefetch = [&]()
         {
-            fence_proxy_async_smem();
-            const long long s0 = tn * SIG_BYTES, a0 = s0 & ~15LL, a1 = (s0 + SIG_BYTES + 15) & ~15LL;
-            mbar_arrive_expect_tx(bar, uint32_t(a1 - a0));
-            bulk_g2s(stage, inb + a0, uint32_t(a1 - a0), bar);
-        }
-        fft.run(work, tw, lt);
-        for (int q = threadIdx.x; q < L; q += blockDim.x)
-        {
-            cpx<T>& r      = work[pidx<T>(q)];
-            const cpx<T> A = r;
-            if (q == 0)
-                misc[1] = A;
-            r = conj(A * ldg(bhat + q));
-        }
+            if (tn < ntiles)
+            {
+                pending |= 1u << (sb ^ 1);
+                if (threadIdx.x == 0)
+                {
+                    // the other stage was last read by the previous tile's bulk store
+                    bulk_wait_read();
+                    fence_proxy_async_smem();
+                    const long long n0 = tn * tile_bytes, b0 = n0 & ~15LL, b1 = (n0 + tile_bytes + 15) & ~15LL;
+                    mbar_arrive_expect_tx(&bars[sb ^ 1], uint32_t(b1 - b0));
+                    bulk_g2s(sb ? st0 : st1, inb + b0, uint32_t(b1 - b0), &bars[sb ^ 1]);
+                }
+            }
+        };
+        const auto nothing = []() {};
+        // first L-point DFT of the permuted input, times bhat; it ends in the stage (even pass count) or
+        // in the work buffer (odd)
+        constexpr bool even = F::npass % 2 == 0;
+        cpx<T>* mid         = even ? sp : wk;
+        fft.run_pp([&](int p) { return conj_if(sig[__ldg(gp + p)], inv); },
+                   [&](int q, cpx<T> x)
+                   {
+                       if (q == 0)
+                           dcs[gm.g] = x;
+                       mid[pidx<T>(q)] = conj(x * ldg(bhat + q));
+                   },
+                   prefetch, sp, wk, tw, gm.lt);
+        // second L-point DFT from there, scattered to the output order in the stage
+        const cpx<T> x0 = x0s[gm.g];
+        fft.run_pp([&](int p) { return mid[pidx<T>(p)]; },
+                   [&](int q, cpx<T> x) { sig[__ldg(gp + (q == 0 ? 0 : L - q))] = conj_if(x0 + conj(x), inv); },
+                   nothing, mid, even ? wk : sp, tw, gm.lt);
+        if (gm.lt == 0)
+            sig[0] = conj_if(x0 + dcs[gm.g], inv);
+        fence_proxy_async_smem();
         __syncthreads();
-        fft.run(work, tw, lt);
-        const cpx<T> x0 = misc[0];
-        const cpx<T> dc = misc[1];
-        cpx<T>* o       = out + t * N;
-        for (int k = threadIdx.x; k < N; k += blockDim.x)
+        // the tile's output: its 16-byte-aligned interior by a bulk store, the (at most two) 8-byte edge
+        // elements by plain stores
+        const long long e1 = s0 + tile_bytes;
+        const long long c0 = (s0 + 15) & ~15LL, c1 = e1 & ~15LL;
+        if (threadIdx.x == 0)
         {
-            const cpx<T> X = k == 0 ? x0 + dc : x0 + conj(work[pidx<T>(__ldg(a.qof + k))]);
-            o[k]           = conj_if(X, inv);
+            if (c1 > c0)
+                bulk_s2g(outb + c0, reinterpret_cast<const char*>(stage) + (c0 - a0), uint32_t(c1 - c0));
+            bulk_commit();
         }
-        __syncthreads();
+        if (threadIdx.x == 32 % blockDim.x && c0 != s0)
+            *reinterpret_cast<cpx<T>*>(outb + s0) = stage[off];
+        if (threadIdx.x == 64 % blockDim.x && c1 != e1)
+            *reinterpret_cast<cpx<T>*>(outb + e1 - ESZ) = stage[off + spc * N - 1];
     }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
 }
 
 // ---------------------------------------------------------------------------------------------------

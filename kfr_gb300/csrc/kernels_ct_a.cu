@@ -94,16 +94,18 @@ cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long l
 #undef KFR_GPU_PIPE_CASE
 }
 
-cudaError_t launch_ct_rader_pipe_f32(const rader_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st)
+cudaError_t launch_ct_rader_tile_f32(const rader_args& a, const block_cfg& c, long long ntiles, int* err,
+                                     cudaStream_t st)
 {
-#define KFR_GPU_RPIPE_CASE(N, TS, ...)                                                                     \
-    case N: return go_persistent(k_rader_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, nsig, st, a, nsig, err);
+#define KFR_GPU_RTILE_CASE(N, TS, ...)                                                                     \
+    case N:                                                                                                \
+        return go_persistent(k_rader_tile<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);
     switch (c.ct)
     {
-        KFR_CT_RADER_F32(KFR_GPU_RPIPE_CASE)
+        KFR_CT_RADER_F32(KFR_GPU_RTILE_CASE)
     default: return cudaErrorInvalidValue;
     }
-#undef KFR_GPU_RPIPE_CASE
+#undef KFR_GPU_RTILE_CASE
 }
 
 } // namespace kfr_gpu

@@ -183,9 +183,10 @@ cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long l
                                    cudaStream_t st);
 cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_rader_f32(const rader_args& a, const block_cfg& c, cudaStream_t st);
-// Persistent Rader over signals [0, nsig) with the next signal's bytes streamed into a shared stage buffer
-// by TMA (in must be 16-byte aligned and signal nsig-1's enclosing 16-byte range must lie inside the batch).
-cudaError_t launch_ct_rader_pipe_f32(const rader_args& a, const block_cfg& c, long long nsig, int* err,
+// Persistent Rader over `ntiles` tiles of c.spc contiguous signals, each tile streamed in and out of shared
+// memory by bulk copies (in and out 16-byte aligned; the last tile's enclosing 16-byte range must lie
+// inside the batch; c.smem as rader_tile_smem).
+cudaError_t launch_ct_rader_tile_f32(const rader_args& a, const block_cfg& c, long long ntiles, int* err,
                                      cudaStream_t st);
 cudaError_t launch_ct_r2c_f32(const real_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_c2r_f32(const real_args& a, const block_cfg& c, cudaStream_t st);

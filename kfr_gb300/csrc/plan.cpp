@@ -232,6 +232,13 @@ static bool is_codelet(int r)
     case 11:
     case 13:
     case 16: return true;
+    // Good-Thomas composites: only in compile-time radix lists (factor_radices never produces them)
+    case 6:
+    case 10:
+    case 12:
+    case 14:
+    case 15:
+    case 18: return true;
     default: return false;
     }
 }
@@ -592,6 +599,30 @@ void complex_engine<T>::init_rader(long long n)
     bhat_.upload(bh.data(), bh.size() * sizeof(std::complex<T>));
     prog_.build(int(L), CT_RADER);
     k_ = kind::rader_smem;
+    // Signals per tile of the pipelined kernel: one signal when it takes half a CTA's threads or more,
+    // otherwise as many as leave room for two CTAs per SM (each holding two stage tiles and a work tile).
+    rader_spc_ = 0;
+    if (prog_.ct && sizeof(T) == 4)
+    {
+        int spc = 1;
+        if (prog_.ts < 512)
+        {
+            spc = 1024 / prog_.ts;
+            while (spc > 1 && rader_tile_smem(spc) > smem_budget() / 2)
+                spc--;
+        }
+        if (rader_tile_smem(spc) <= smem_budget())
+            rader_spc_ = spc;
+    }
+}
+
+template <typename T>
+int complex_engine<T>::rader_tile_smem(int spc) const
+{
+    // two stage tiles, the padded work tile, x[0] and A[0] per signal, two mbarriers
+    const int esz   = int(2 * sizeof(T));
+    const int stage = rader_stage_len(spc, int(n_), padded_len_host<T>(int(n_ - 1)));
+    return (2 * stage + spc * padded_len_host<T>(int(n_ - 1)) + 2 * spc) * esz + 16;
 }
 
 template <typename T>
@@ -809,7 +840,7 @@ int complex_engine<T>::launches(long long batch) const
     case kind::bluestein_smem: return 1;
     case kind::fourstep: return 2 * int((batch + 65534) / 65535);
     case kind::bluestein_multi: return 3 + 2 * inner_->launches(batch);
-    case kind::rader_smem: return (prog_.ct && prog_.cfg(batch).spc == 1 && batch > 1) ? 2 : 1;
+    case kind::rader_smem: return (rader_spc_ && (batch - 1) / rader_spc_ > 0) ? 2 : 1;
     }
     return 0;
 }
@@ -907,20 +938,19 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.div_l   = make_fast_div(uint32_t(n_ - 1));
         a.d       = prog_.desc;
         long long done = 0;
-        // Large transforms (one signal per CTA): persistent TMA-pipelined kernel over all but the last
-        // signal, whose enclosing 16-byte range may end past the batch.
-        const block_cfg c1 = prog_.cfg(batch);
-        if (prog_.ct && c1.spc == 1 && err_.get() && istride == n_ && ostride == n_ && batch > 1 &&
-            (reinterpret_cast<uintptr_t>(in) % 16) == 0)
+        // Persistent tiled kernel over whole tiles that end before the last signal (whose enclosing
+        // 16-byte range may end past the batch); the rest runs in the plain kernel.
+        if (rader_spc_ && err_.get() && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 &&
+            (reinterpret_cast<uintptr_t>(out) % 16) == 0)
         {
-            const int stage = int(((n_ * esz + 31) / 16) * 16);
-            block_cfg pc    = prog_.cfg_tile(1);
-            pc.smem         = stage + padded_len_host<T>(int(n_ - 1)) * int(esz) + 2 * int(esz) + 16;
-            if (pc.smem <= smem_budget())
+            const long long ntiles = (batch - 1) / rader_spc_;
+            if (ntiles > 0)
             {
-                check(launch_ct_rader_pipe_f32(a, pc, batch - 1, static_cast<int*>(err_.get()), st),
-                      "launch rader (pipelined)");
-                done = batch - 1;
+                block_cfg pc = prog_.cfg_tile(rader_spc_);
+                pc.smem      = rader_tile_smem(rader_spc_);
+                check(launch_ct_rader_tile_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st),
+                      "launch rader (tiled)");
+                done = ntiles * rader_spc_;
             }
         }
         a.in    = static_cast<const char*>(in) + done * n_ * esz;
@@ -1031,7 +1061,11 @@ std::string complex_engine<T>::describe() const
           << "] rows[" << prows_.describe() << " tile=" << tile_r_ << "]";
         break;
     case kind::bluestein_multi: s << "bluestein_multi n=" << n_ << " m=" << m_ << " inner{" << inner_->describe() << "}"; break;
-    case kind::rader_smem: s << "rader n=" << n_ << " [" << prog_.describe() << "]"; break;
+    case kind::rader_smem:
+        s << "rader n=" << n_ << " [" << prog_.describe() << "]";
+        if (rader_spc_)
+            s << " tiled spc=" << rader_spc_;
+        break;
     }
     return s.str();
 }

@@ -172,6 +172,8 @@ private:
     void plan_pipe();
     // Rader
     dbuf pin_, qof_, gp_;
+    int rader_spc_ = 0; // signals per tile of the pipelined kernel, 0 = not used
+    int rader_tile_smem(int spc) const;
 };
 
 // dft_plan_real<T>: N even, N/2-point complex engine plus the CCs/Perm split / merge.

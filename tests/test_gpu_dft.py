@@ -97,6 +97,37 @@ def test_complex_dft_batched_against_oracle(orc, n, batch, sfx):
     assert rel_rms(zd.cpu().numpy(), ref) <= tol(n, sfx), n
 
 
+@pytest.mark.parametrize("n,batch", [(127, 40000), (8191, 500)])
+def test_rader_tiles_many_per_cta(orc, n, batch):
+    """Prime lengths through the persistent tiled Rader kernel with several tiles per CTA (stage buffers
+    reused, output bulk stores overlapping the next tile's load), forward, inverse, in place, and from an
+    8-byte-misaligned pointer (which takes the plain kernel)."""
+    rng = np.random.default_rng(n + batch)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    pick = np.r_[0:3, batch // 2, batch - 3:batch]
+    ref = orc.dft(x[pick].astype(np.complex128), threads=8)
+    refi = orc.dft(x[pick].astype(np.complex128), inverse=True, threads=8)
+    plan = k.dft_plan(n, "f32")
+    assert "tiled" in plan.describe()
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    plan.execute_batch(yd, xd, batch)
+    assert rel_rms(yd.cpu().numpy()[pick], ref) <= tol(n, "f32")
+    full = yd.clone()
+    plan.execute_batch(yd, xd, batch, inverse=True)
+    assert rel_rms(yd.cpu().numpy()[pick], refi) <= tol(n, "f32")
+    zd = xd.clone()
+    plan.execute_batch(zd, zd, batch)
+    assert torch.equal(zd, full)
+    # misaligned by one element: same results through the plain kernel
+    buf = torch.empty(batch * n + 1, dtype=torch.complex64, device="cuda")
+    buf[1:].copy_(xd.reshape(-1))
+    out = torch.empty_like(buf)
+    plan.execute_batch(out[1:], buf[1:], batch)
+    got = out[1:].reshape(batch, n).cpu().numpy()
+    assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
+
+
 @pytest.mark.parametrize("n", [1 << 24, 30720000])
 def test_complex_dft_large_single(orc, n):
     """The large single transforms of the mixed-radix parity set (c32)."""
