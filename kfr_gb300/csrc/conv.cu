@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_conv_os(const conv_args a
     T* out           = reinterpret_cast<T*>(a.out) + (long long)ch * a.n;
     const long long base  = b * a.bo;
     const long long limit = a.m1 + a.n;
+#pragma unroll 4
     for (int m = threadIdx.x; m < c; m += blockDim.x)
     {
         const long long i0 = base + 2 * m;
@@ -47,7 +48,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_conv_os(const conv_args a
             v0 = i0 < a.m1 ? hist[i0] : in[i0 - a.m1];
         if (i0 + 1 < limit)
             v1 = i0 + 1 < a.m1 ? hist[i0 + 1] : in[i0 + 1 - a.m1];
-        sm[pidx<T>(m)] = mk(v0, v1);
+        sm[F::pi(m)] = mk(v0, v1);
     }
     __syncthreads();
     const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
@@ -67,15 +68,15 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_conv_os(const conv_args a
         else
         {
             const int kk      = c - k;
-            const cpx<T> zk   = sm[pidx<T>(k)];
-            const cpx<T> zkk  = sm[pidx<T>(kk)];
+            const cpx<T> zk   = sm[F::pi(k)];
+            const cpx<T> zkk  = sm[F::pi(kk)];
             const cpx<T> wk   = ldg(rtw + k);
             const cpx<T> wkk  = ldg(rtw + kk);
             const cpx<T> yk   = rsplit(zk, zkk, wk) * ldg(H + k);
             const cpx<T> ykk  = rsplit(zkk, zk, wkk) * ldg(H + kk);
-            sm[pidx<T>(k)]    = conj(rmerge(yk, ykk, wk));
+            sm[F::pi(k)]    = conj(rmerge(yk, ykk, wk));
             if (kk != k)
-                sm[pidx<T>(kk)] = conj(rmerge(ykk, yk, wkk));
+                sm[F::pi(kk)] = conj(rmerge(ykk, yk, wkk));
         }
     }
     __syncthreads();
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_conv_os(const conv_args a
         if (no < a.n)
         {
             const long long j = a.m1 + t;
-            const cpx<T> v    = sm[pidx<T>(int(j >> 1))];
+            const cpx<T> v    = sm[F::pi(int(j >> 1))];
             out[no]           = (j & 1) ? -v.y : v.x;
         }
     }

@@ -67,3 +67,40 @@
     X(1024, 64, 16, 16, 4)                                                                                   \
     X(2048, 128, 16, 16, 8)                                                                                  \
     X(4096, 256, 16, 16, 16)
+
+// Shared-memory layout of a compile-time length (single precision): X(N, TS, pad shift, extra group stride).
+// Element i of a signal sits at i + (i >> shift) (shift 0: unpadded), signals of a CTA lie `stride` elements
+// apart, stride = N + (N >> shift) + 1 + extra.  The default (shift 4, extra 0) suits power-of-two strides;
+// these entries were chosen with a wavefront model of every pass's accesses (odd radices do best unpadded).
+#define KFR_CT_LAYOUT_F32(X)                                                                                \
+    X(126, 9, 0, 10)                                                                                         \
+    X(2187, 243, 0, 0)                                                                                       \
+    X(8190, 1024, 0, 0)
+
+#if defined(__CUDACC__)
+#define KFR_CT_HD __host__ __device__
+#else
+#define KFR_CT_HD
+#endif
+
+namespace kfr_gpu
+{
+KFR_CT_HD constexpr int ct_pad_shift_f32(int n, int ts)
+{
+#define KFR_CT_LAYOUT_SHIFT(N, TS, S, E)                                                                   \
+    if (n == N && ts == TS)                                                                                \
+        return S;
+    KFR_CT_LAYOUT_F32(KFR_CT_LAYOUT_SHIFT)
+#undef KFR_CT_LAYOUT_SHIFT
+    return 4;
+}
+KFR_CT_HD constexpr int ct_group_stride_f32(int n, int ts)
+{
+#define KFR_CT_LAYOUT_STRIDE(N, TS, S, E)                                                                  \
+    if (n == N && ts == TS)                                                                                \
+        return n + (S ? (n >> S) : 0) + 1 + E;
+    KFR_CT_LAYOUT_F32(KFR_CT_LAYOUT_STRIDE)
+#undef KFR_CT_LAYOUT_STRIDE
+    return n + (n >> 4) + 1;
+}
+} // namespace kfr_gpu

@@ -11,6 +11,8 @@
 // synchronises, and writes them back, so a signal needs only N (+1/16 padding) slots of shared memory.
 #pragma once
 
+#include "ct_table.hpp"
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -99,6 +101,12 @@ template <typename T>
 __device__ __forceinline__ int pidx(int i)
 {
     return i + (i >> smem_pad<T>::shift);
+}
+// padding with an explicit shift (0: none), used by the compile-time lengths
+template <int PS>
+__device__ __forceinline__ int pidx_s(int i)
+{
+    return PS ? i + (i >> PS) : i;
 }
 template <typename T>
 __host__ __device__ constexpr int padded_len(int n)
@@ -551,6 +559,12 @@ __device__ __forceinline__ void block_fft(cpx<T>* buf, const pass_desc* sp, cons
 // the same radix order.
 // --------------------------------------------------------------------------------------------------
 
+template <typename T>
+__host__ __device__ constexpr int ct_ps(int n, int ts)
+{
+    return sizeof(T) == 4 ? ct_pad_shift_f32(n, ts) : smem_pad<T>::shift;
+}
+
 template <int N, int TS, int R>
 __host__ __device__ constexpr int ct_nb()
 {
@@ -578,7 +592,7 @@ __device__ __forceinline__ void ct_pass(cpx<T> (&v)[EPT], cpx<T>* buf, const cpx
         {
 #pragma unroll
             for (int r = 0; r < R; r++)
-                v[b * R + r] = buf[pidx<T>(j + r * NBF)];
+                v[b * R + r] = buf[pidx_s<ct_ps<T>(N, TS)>(j + r * NBF)];
             if constexpr (NS > 1)
             {
                 const int k     = j % NS;
@@ -601,7 +615,7 @@ __device__ __forceinline__ void ct_pass(cpx<T> (&v)[EPT], cpx<T>* buf, const cpx
             const int d = (j - k) * R + k;
 #pragma unroll
             for (int r = 0; r < R; r++)
-                buf[pidx<T>(d + r * NS)] = v[b * R + codelet_out<R>(r)];
+                buf[pidx_s<ct_ps<T>(N, TS)>(d + r * NS)] = v[b * R + codelet_out<R>(r)];
         }
     }
     __syncthreads();
@@ -646,7 +660,7 @@ __device__ __forceinline__ void ct_pass_first(cpx<T> (&v)[EPT], const cpx<T>* sr
             dft_codelet<T, R>(&v[b * R]);
 #pragma unroll
             for (int r = 0; r < R; r++)
-                work[pidx<T>(j * R + r)] = v[b * R + codelet_out<R>(r)];
+                work[pidx_s<ct_ps<T>(N, TS)>(j * R + r)] = v[b * R + codelet_out<R>(r)];
         }
     }
     __syncthreads();
@@ -667,7 +681,7 @@ __device__ __forceinline__ void ct_pass_last(cpx<T> (&v)[EPT], const cpx<T>* wor
         {
 #pragma unroll
             for (int r = 0; r < R; r++)
-                v[b * R + r] = work[pidx<T>(j + r * NBF)];
+                v[b * R + r] = work[pidx_s<ct_ps<T>(N, TS)>(j + r * NBF)];
             const cpx<T>* t = tw + TWOFF + j;
 #pragma unroll
             for (int r = 1; r < R; r++)
@@ -792,8 +806,8 @@ __device__ __forceinline__ void ct_chain_fx(cpx<T> (&v)[EPT], const LD& ld, cons
                                             cpx<T>* work, const cpx<T>* __restrict__ tw, const int lt)
 {
     constexpr int TWNEXT = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
-    const auto wld       = [work](int p) { return work[pidx<T>(p)]; };
-    const auto wst       = [work](int q, cpx<T> x) { work[pidx<T>(q)] = x; };
+    const auto wld       = [work](int p) { return work[pidx_s<ct_ps<T>(N, TS)>(p)]; };
+    const auto wst       = [work](int q, cpx<T> x) { work[pidx_s<ct_ps<T>(N, TS)>(q)] = x; };
     if constexpr (NS == 1 && sizeof...(Rest) == 0)
     {
         ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, !(SEP_IN || SEP_OUT)>(v, ld, st, tw, lt);
@@ -863,12 +877,14 @@ __device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>
     __syncthreads();
 }
 
-template <typename T, int N, int TS, int NS, int TWOFF, int I, class LD, class ST, class H, int R, int... Rest>
-__device__ __forceinline__ void pp_chain(const LD& ld, const ST& st, const H& hook, cpx<T>* A, cpx<T>* B,
-                                         const cpx<T>* __restrict__ tw, const int lt)
+template <typename T, int N, int TS, int NS, int TWOFF, int I, class LD, class ST, class H, class P, int R,
+          int... Rest>
+__device__ __forceinline__ void pp_chain(const LD& ld, const ST& st, const H& hook, const P& pre_last, cpx<T>* A,
+                                         cpx<T>* B, const cpx<T>* __restrict__ tw, const int lt)
 {
     if constexpr (sizeof...(Rest) == 0)
     {
+        pre_last();
         pp_pass<T, N, TS, R, NS, TWOFF>(ld, st, tw, lt);
         if constexpr (NS == 1)
             hook();
@@ -876,22 +892,24 @@ __device__ __forceinline__ void pp_chain(const LD& ld, const ST& st, const H& ho
     else
     {
         cpx<T>* dst      = (I % 2 == 0) ? B : A;
-        const auto d_st  = [dst](int q, cpx<T> x) { dst[pidx<T>(q)] = x; };
-        const auto d_ld  = [dst](int p) { return dst[pidx<T>(p)]; };
+        const auto d_st  = [dst](int q, cpx<T> x) { dst[pidx_s<ct_ps<T>(N, TS)>(q)] = x; };
+        const auto d_ld  = [dst](int p) { return dst[pidx_s<ct_ps<T>(N, TS)>(p)]; };
         constexpr int TN = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
         pp_pass<T, N, TS, R, NS, TWOFF>(ld, d_st, tw, lt);
         if constexpr (NS == 1)
             hook();
-        pp_chain<T, N, TS, NS * R, TN, I + 1, decltype(d_ld), ST, H, Rest...>(d_ld, st, hook, A, B, tw, lt);
+        pp_chain<T, N, TS, NS * R, TN, I + 1, decltype(d_ld), ST, H, P, Rest...>(d_ld, st, hook, pre_last, A, B, tw,
+                                                                                lt);
     }
 }
 
-template <typename T, int N, int TS, int... Rs, class LD, class ST, class H>
-__device__ __forceinline__ void ct_block_fft_pp(const LD& ld, const ST& st, const H& hook, cpx<T>* A, cpx<T>* B,
-                                                const cpx<T>* __restrict__ tw, const int lt)
+// hook() runs after the first pass, pre_last() before the last pass (all threads, uniformly).
+template <typename T, int N, int TS, int... Rs, class LD, class ST, class H, class P>
+__device__ __forceinline__ void ct_block_fft_pp(const LD& ld, const ST& st, const H& hook, const P& pre_last,
+                                                cpx<T>* A, cpx<T>* B, const cpx<T>* __restrict__ tw, const int lt)
 {
     const int lta = lt < TS ? lt : N;
-    pp_chain<T, N, TS, 1, 0, 0, LD, ST, H, Rs...>(ld, st, hook, A, B, tw, lta);
+    pp_chain<T, N, TS, 1, 0, 0, LD, ST, H, P, Rs...>(ld, st, hook, pre_last, A, B, tw, lta);
 }
 
 // Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a

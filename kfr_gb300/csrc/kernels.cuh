@@ -35,6 +35,9 @@ struct rt_fft
     {
         block_fft<T, EPT>(buf, sp, npass, n, tw, lt, ts);
     }
+    // shared-memory layout: signals gstride(n) elements apart, element i at pi(i)
+    static __host__ __device__ constexpr int gstride(int len) { return padded_len<T>(len); }
+    static __device__ __forceinline__ int pi(int i) { return pidx<T>(i); }
 };
 
 template <typename T, int N, int TS, int... Rs>
@@ -43,6 +46,13 @@ struct ct_fft
     static constexpr int max_threads = sizeof(T) == 4 ? 1024 : 512;
     static constexpr int n           = N;
     static constexpr int ts          = TS;
+    // shared-memory layout (ct_table.hpp): signals gstride() elements apart, element i at pi(i)
+    static constexpr int ps = ct_ps<T>(N, TS);
+    static __host__ __device__ constexpr int gstride(int = N)
+    {
+        return sizeof(T) == 4 ? ct_group_stride_f32(N, TS) : padded_len<T>(N);
+    }
+    static __device__ __forceinline__ int pi(int i) { return pidx_s<ps>(i); }
     __device__ __forceinline__ ct_fft(pass_desc*, const fft_desc&, int) {}
     __device__ __forceinline__ void run(cpx<T>* buf, const cpx<T>* __restrict__ tw, int lt) const
     {
@@ -54,11 +64,11 @@ struct ct_fft
         ct_block_fft_io<T, N, TS, Rs...>(src, work, gout, tw, cj, lt);
     }
     static constexpr int npass = sizeof...(Rs);
-    template <class LD, class ST, class H>
-    __device__ __forceinline__ void run_pp(const LD& ld, const ST& st, const H& hook, cpx<T>* A, cpx<T>* B,
-                                           const cpx<T>* __restrict__ tw, int lt) const
+    template <class LD, class ST, class H, class P>
+    __device__ __forceinline__ void run_pp(const LD& ld, const ST& st, const H& hook, const P& pre_last, cpx<T>* A,
+                                           cpx<T>* B, const cpx<T>* __restrict__ tw, int lt) const
     {
-        ct_block_fft_pp<T, N, TS, Rs...>(ld, st, hook, A, B, tw, lt);
+        ct_block_fft_pp<T, N, TS, Rs...>(ld, st, hook, pre_last, A, B, tw, lt);
     }
     template <bool SEP_IN, bool SEP_OUT, class LD, class ST, class H>
     __device__ __forceinline__ void run_fx(const LD& ld, const ST& st, const H& hook, cpx<T>* work,
@@ -69,6 +79,31 @@ struct ct_fft
 };
 
 __device__ __forceinline__ uint32_t div_by(uint32_t x, const fast_div f) { return fdiv(x, f); }
+
+// Block-wide strided copy i = threadIdx.x + k * blockDim.x, i < total: U loads ld(i) are issued before
+// their U stores st(i, v), so each thread keeps U global loads in flight.
+template <int U, class LD, class ST>
+__device__ __forceinline__ void copy_batched(const int total, const LD& ld, const ST& st)
+{
+    for (int base = threadIdx.x; base < total; base += U * int(blockDim.x))
+    {
+        decltype(ld(0)) v[U];
+#pragma unroll
+        for (int e = 0; e < U; e++)
+        {
+            const int i = base + e * int(blockDim.x);
+            if (i < total)
+                v[e] = ld(i);
+        }
+#pragma unroll
+        for (int e = 0; e < U; e++)
+        {
+            const int i = base + e * int(blockDim.x);
+            if (i < total)
+                st(i, v[e]);
+        }
+    }
+}
 
 // thread -> (signal slot, lane within the signal's thread group)
 struct group_map
@@ -94,7 +129,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2c(const c2c_args a, con
     const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
     const int n       = fft.n;
-    const int stride  = padded_len<T>(n);
+    const int stride  = F::gstride(n);
     const long long s0 = (long long)blockIdx.x * spc;
     const cpx<T>* __restrict__ in = reinterpret_cast<const cpx<T>*>(a.in);
     cpx<T>* __restrict__ out      = reinterpret_cast<cpx<T>*>(a.out);
@@ -107,7 +142,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2c(const c2c_args a, con
         const int e = i - s * n;
         const long long sig = s0 + s;
         if (sig < a.batch)
-            sm[s * stride + pidx<T>(e)] = conj_if(in[sig * a.istride + e], inv);
+            sm[s * stride + F::pi(e)] = conj_if(in[sig * a.istride + e], inv);
     }
     __syncthreads();
     const group_map gm(ts, spc);
@@ -119,7 +154,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2c(const c2c_args a, con
         const int e = i - s * n;
         const long long sig = s0 + s;
         if (sig < a.batch)
-            out[sig * a.ostride + e] = conj_if(sm[s * stride + pidx<T>(e)], inv);
+            out[sig * a.ostride + e] = conj_if(sm[s * stride + F::pi(e)], inv);
     }
 }
 
@@ -137,7 +172,7 @@ __global__ void __launch_bounds__(F::max_threads, 1)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int N      = F::n;
-    constexpr int STRIDE = padded_len<T>(N);
+    constexpr int STRIDE = F::gstride(N);
     const F fft(nullptr, a.d, F::ts);
     const int tile   = spc * N;
     cpx<T>* stage0   = reinterpret_cast<cpx<T>*>(smem_raw);
@@ -214,13 +249,14 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_bluestein(const bluestein
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
     const int m       = fft.n;
     const int n       = a.n;
-    const int stride  = padded_len<T>(m);
+    const int stride  = F::gstride(m);
     const long long s0 = (long long)blockIdx.x * spc;
     const cpx<T>* __restrict__ in    = reinterpret_cast<const cpx<T>*>(a.in);
     cpx<T>* __restrict__ out         = reinterpret_cast<cpx<T>*>(a.out);
     const cpx<T>* __restrict__ chirp = reinterpret_cast<const cpx<T>*>(a.chirp);
     const cpx<T>* __restrict__ bhat  = reinterpret_cast<const cpx<T>*>(a.bhat);
     const bool inv = a.inverse != 0;
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * m; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_m));
@@ -229,28 +265,30 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_bluestein(const bluestein
         cpx<T> v = mk<T>(0, 0);
         if (e < n && sig < a.batch)
             v = conj_if(in[sig * a.istride + e], inv) * ldg(chirp + e);
-        sm[s * stride + pidx<T>(e)] = v;
+        sm[s * stride + F::pi(e)] = v;
     }
     __syncthreads();
     const group_map gm(ts, spc);
     const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
     fft.run(sm + gm.g * stride, tw, gm.lt);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * m; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_m));
         const int e = i - s * m;
-        cpx<T>& r   = sm[s * stride + pidx<T>(e)];
+        cpx<T>& r   = sm[s * stride + F::pi(e)];
         r           = conj(r * ldg(bhat + e));
     }
     __syncthreads();
     fft.run(sm + gm.g * stride, tw, gm.lt);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
         const int k = i - s * n;
         const long long sig = s0 + s;
         if (sig < a.batch)
-            out[sig * a.ostride + k] = conj_if(conj(sm[s * stride + pidx<T>(k)]) * ldg(chirp + k), inv);
+            out[sig * a.ostride + k] = conj_if(conj(sm[s * stride + F::pi(k)]) * ldg(chirp + k), inv);
     }
 }
 
@@ -268,7 +306,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
     cpx<T>* sm         = reinterpret_cast<cpx<T>*>(smem_raw);
     const int L        = fft.n;
     const int n        = L + 1;
-    const int stride   = padded_len<T>(L);
+    const int stride   = F::gstride(L);
     cpx<T>* x0s        = sm + spc * stride; // spc values
     cpx<T>* dcs        = x0s + spc;        // spc values
     const long long s0 = (long long)blockIdx.x * spc;
@@ -276,6 +314,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
     cpx<T>* __restrict__ out        = reinterpret_cast<cpx<T>*>(a.out);
     const cpx<T>* __restrict__ bhat = reinterpret_cast<const cpx<T>*>(a.bhat);
     const bool inv = a.inverse != 0;
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -285,17 +324,18 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
         if (e == 0)
             x0s[s] = v;
         else
-            sm[s * stride + pidx<T>(__ldg(a.pin + e))] = v;
+            sm[s * stride + F::pi(__ldg(a.pin + e))] = v;
     }
     __syncthreads();
     const group_map gm(ts, spc);
     const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
     fft.run(sm + gm.g * stride, tw, gm.lt);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * L; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_l));
         const int q = i - s * L;
-        cpx<T>& r   = sm[s * stride + pidx<T>(q)];
+        cpx<T>& r   = sm[s * stride + F::pi(q)];
         const cpx<T> A = r;
         if (q == 0)
             dcs[s] = A;
@@ -303,6 +343,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
     }
     __syncthreads();
     fft.run(sm + gm.g * stride, tw, gm.lt);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -311,7 +352,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
         if (sig >= a.batch)
             continue;
         const cpx<T> x0 = x0s[s];
-        const cpx<T> X  = k == 0 ? x0 + dcs[s] : x0 + conj(sm[s * stride + pidx<T>(__ldg(a.qof + k))]);
+        const cpx<T> X  = k == 0 ? x0 + dcs[s] : x0 + conj(sm[s * stride + F::pi(__ldg(a.qof + k))]);
         out[sig * a.ostride + k] = conj_if(X, inv);
     }
 }
@@ -332,7 +373,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
 template <typename T, class F>
 __host__ __device__ constexpr int rader_stage_elems(int spc)
 {
-    return rader_stage_len(spc, F::n + 1, padded_len<T>(F::n));
+    return rader_stage_len(spc, F::n + 1, F::gstride(F::n));
 }
 
 template <typename T, class F>
@@ -342,7 +383,7 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int L      = F::n;
     constexpr int N      = L + 1;
-    constexpr int STRIDE = padded_len<T>(L);
+    constexpr int STRIDE = F::gstride(L);
     constexpr int ESZ    = int(sizeof(cpx<T>));
     const int stage_elems = rader_stage_elems<T, F>(spc);
     cpx<T>* st0    = reinterpret_cast<cpx<T>*>(smem_raw);
@@ -430,14 +471,14 @@ __global__ void __launch_bounds__(F::max_threads, 1)
                    {
                        if (q == 0)
                            dcs[gm.g] = x;
-                       mid[pidx<T>(q)] = conj(x * ldg(bhat + q));
+                       mid[F::pi(q)] = conj(x * ldg(bhat + q));
                    },
-                   prefetch, sp, wk, tw, gm.lt);
+                   prefetch, nothing, sp, wk, tw, gm.lt);
         // second L-point DFT from there, scattered to the output order in the stage
         const cpx<T> x0 = x0s[gm.g];
-        fft.run_pp([&](int p) { return mid[pidx<T>(p)]; },
+        fft.run_pp([&](int p) { return mid[F::pi(p)]; },
                    [&](int q, cpx<T> x) { sig[__ldg(gp + (q == 0 ? 0 : L - q))] = conj_if(x0 + conj(x), inv); },
-                   nothing, mid, even ? wk : sp, tw, gm.lt);
+                   nothing, nothing, mid, even ? wk : sp, tw, gm.lt);
         if (gm.lt == 0)
             sig[0] = conj_if(x0 + dcs[gm.g], inv);
         fence_proxy_async_smem();
@@ -473,23 +514,25 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_r2c(const real_args a, co
     const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
     const int c       = fft.n;
-    const int stride  = padded_len<T>(c);
+    const int stride  = F::gstride(c);
     const long long s0 = (long long)blockIdx.x * spc;
     const T* __restrict__ inr      = reinterpret_cast<const T*>(a.in);
     cpx<T>* __restrict__ out       = reinterpret_cast<cpx<T>*>(a.out);
     const cpx<T>* __restrict__ rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * c; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
         const int e = i - s * c;
         const long long sig = s0 + s;
         if (sig < a.batch)
-            sm[s * stride + pidx<T>(e)] = reinterpret_cast<const cpx<T>*>(inr + sig * a.istride)[e];
+            sm[s * stride + F::pi(e)] = reinterpret_cast<const cpx<T>*>(inr + sig * a.istride)[e];
     }
     __syncthreads();
     const group_map gm(ts, spc);
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     const int olen = a.ccs ? c + 1 : c;
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * olen; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_out));
@@ -511,8 +554,8 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_r2c(const real_args a, co
         }
         else
         {
-            const cpx<T> zk  = z[pidx<T>(k)];
-            const cpx<T> znk = conj(z[pidx<T>(c - k)]);
+            const cpx<T> zk  = z[F::pi(k)];
+            const cpx<T> znk = conj(z[F::pi(c - k)]);
             const cpx<T> e   = scale(zk + znk, T(0.5));
             const cpx<T> o   = scale(mul_mi(zk - znk), T(0.5));
             v                = e + ldg(rtw + k) * o;
@@ -534,11 +577,12 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2r(const real_args a, co
     const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
     const int c       = fft.n;
-    const int stride  = padded_len<T>(c);
+    const int stride  = F::gstride(c);
     const long long s0 = (long long)blockIdx.x * spc;
     const cpx<T>* __restrict__ in  = reinterpret_cast<const cpx<T>*>(a.in);
     T* __restrict__ outr           = reinterpret_cast<T*>(a.out);
     const cpx<T>* __restrict__ rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * c; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -562,18 +606,19 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2r(const real_args a, co
             const cpx<T> f2  = xk - xnk;
             z                = f1 + mul_pi(conj(ldg(rtw + k)) * f2);
         }
-        sm[s * stride + pidx<T>(k)] = conj(z);
+        sm[s * stride + F::pi(k)] = conj(z);
     }
     __syncthreads();
     const group_map gm(ts, spc);
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * c; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
         const int e = i - s * c;
         const long long sig = s0 + s;
         if (sig < a.batch)
-            reinterpret_cast<cpx<T>*>(outr + sig * a.ostride)[e] = conj(sm[s * stride + pidx<T>(e)]);
+            reinterpret_cast<cpx<T>*>(outr + sig * a.ostride)[e] = conj(sm[s * stride + F::pi(e)]);
     }
 }
 
@@ -589,11 +634,12 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_dct2(const dct_args a, co
     const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
     const int n       = fft.n;
-    const int stride  = padded_len<T>(n);
+    const int stride  = F::gstride(n);
     const long long s0 = (long long)blockIdx.x * spc;
     const T* __restrict__ in       = reinterpret_cast<const T*>(a.in);
     T* __restrict__ out            = reinterpret_cast<T*>(a.out);
     const cpx<T>* __restrict__ dtw = reinterpret_cast<const cpx<T>*>(a.dtw);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s   = int(div_by(uint32_t(i), a.div_n));
@@ -602,11 +648,12 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_dct2(const dct_args a, co
         if (sig >= a.batch)
             continue;
         const int pos = (src & 1) ? n - 1 - (src >> 1) : (src >> 1);
-        sm[s * stride + pidx<T>(pos)] = mk<T>(in[sig * a.stride + src], T(0));
+        sm[s * stride + F::pi(pos)] = mk<T>(in[sig * a.stride + src], T(0));
     }
     __syncthreads();
     const group_map gm(ts, spc);
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -614,7 +661,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_dct2(const dct_args a, co
         const long long sig = s0 + s;
         if (sig >= a.batch)
             continue;
-        const cpx<T> y = sm[s * stride + pidx<T>(k)];
+        const cpx<T> y = sm[s * stride + F::pi(k)];
         const cpx<T> w = ldg(dtw + k);
         out[sig * a.stride + k] = y.x * w.x + y.y * w.y;
     }
@@ -630,11 +677,12 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_dct3(const dct_args a, co
     const F fft(sp, a.d, ts);
     cpx<T>* sm        = reinterpret_cast<cpx<T>*>(smem_raw);
     const int n       = fft.n;
-    const int stride  = padded_len<T>(n);
+    const int stride  = F::gstride(n);
     const long long s0 = (long long)blockIdx.x * spc;
     const T* __restrict__ in       = reinterpret_cast<const T*>(a.in);
     T* __restrict__ out            = reinterpret_cast<T*>(a.out);
     const cpx<T>* __restrict__ dtw = reinterpret_cast<const cpx<T>*>(a.dtw);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s = int(div_by(uint32_t(i), a.div_n));
@@ -647,11 +695,12 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_dct3(const dct_args a, co
         cpx<T> v       = mk<T>(x * w.x, -(x * w.y));
         if (k == 0)
             v = scale(v, T(0.5));
-        sm[s * stride + pidx<T>(k)] = v;
+        sm[s * stride + F::pi(k)] = v;
     }
     __syncthreads();
     const group_map gm(ts, spc);
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
+#pragma unroll 4
     for (int i = threadIdx.x; i < spc * n; i += blockDim.x)
     {
         const int s   = int(div_by(uint32_t(i), a.div_n));
@@ -660,7 +709,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_dct3(const dct_args a, co
         if (sig >= a.batch)
             continue;
         const int pos = (dst & 1) ? n - 1 - (dst >> 1) : (dst >> 1);
-        out[sig * a.stride + dst] = sm[s * stride + pidx<T>(pos)].x;
+        out[sig * a.stride + dst] = sm[s * stride + F::pi(pos)].x;
     }
 }
 
@@ -682,37 +731,46 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_cols(const fourstep_ar
     const F fft(sp, a.d, ts);
     cpx<T>* sm       = reinterpret_cast<cpx<T>*>(smem_raw);
     const int n1     = fft.n, n2 = a.n2, S = a.tile, sh = a.tile_shift;
-    const int stride = padded_len<T>(n1);
+    const int stride = F::gstride(n1);
     const int c0     = blockIdx.x * S;
     const long long sig = blockIdx.y;
     const cpx<T>* __restrict__ x = reinterpret_cast<const cpx<T>*>(a.in) + sig * a.sig_stride;
     cpx<T>* __restrict__ y       = reinterpret_cast<cpx<T>*>(a.out) + sig * a.sig_stride;
     const bool cin  = a.conj_in != 0;
     const int total = S * n1;
-    for (int i = threadIdx.x; i < total; i += blockDim.x)
-    {
-        const int n1i = i >> sh; // S is a power of two
-        const int c   = i & (S - 1);
-        if (c0 + c < n2)
-            sm[c * stride + pidx<T>(n1i)] = conj_if(x[(long long)n1i * n2 + c0 + c], cin);
-    }
+    copy_batched<8>(
+        total,
+        [&](int i)
+        {
+            const int n1i = i >> sh; // S is a power of two
+            const int c   = i & (S - 1);
+            return c0 + c < n2 ? x[(long long)n1i * n2 + c0 + c] : mk<T>(0, 0);
+        },
+        [&](int i, cpx<T> v)
+        {
+            const int n1i = i >> sh;
+            const int c   = i & (S - 1);
+            sm[c * stride + F::pi(n1i)] = conj_if(v, cin);
+        });
     __syncthreads();
     const group_map gm(ts, S);
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     if (a.same_layout)
     {
         // an axis of a multi-dimensional transform: no twiddle, back to the input's own layout
+#pragma unroll 4
         for (int i = threadIdx.x; i < total; i += blockDim.x)
         {
             const int k1 = i >> sh;
             const int c  = i & (S - 1);
             if (c0 + c < n2)
-                y[(long long)k1 * n2 + c0 + c] = conj_if(sm[c * stride + pidx<T>(k1)], a.conj_out != 0);
+                y[(long long)k1 * n2 + c0 + c] = conj_if(sm[c * stride + F::pi(k1)], a.conj_out != 0);
         }
         return;
     }
     const cpx<T>* twA = reinterpret_cast<const cpx<T>*>(a.twA);
     const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
+#pragma unroll 4
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {
         const int c  = int(div_by(uint32_t(i), a.div_n));
@@ -720,7 +778,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_cols(const fourstep_ar
         const int col = c0 + c;
         if (col < n2)
         {
-            cpx<T> v = sm[c * stride + pidx<T>(k1)];
+            cpx<T> v = sm[c * stride + F::pi(k1)];
             v        = v * twiddle_2level(twA, twB, (long long)col * k1, a.lbits);
             y[(long long)col * n1 + k1] = conj_if(v, a.conj_out != 0);
         }
@@ -735,30 +793,38 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_rows(const fourstep_ar
     const F fft(sp, a.d, ts);
     cpx<T>* sm       = reinterpret_cast<cpx<T>*>(smem_raw);
     const int n1     = a.n1, n2 = fft.n, S = a.tile, sh = a.tile_shift;
-    const int stride = padded_len<T>(n2);
+    const int stride = F::gstride(n2);
     const int r0     = blockIdx.x * S;
     const long long sig = blockIdx.y;
     const cpx<T>* __restrict__ y = reinterpret_cast<const cpx<T>*>(a.in) + sig * a.sig_stride;
     cpx<T>* __restrict__ X       = reinterpret_cast<cpx<T>*>(a.out) + sig * a.sig_stride;
     const int total = S * n2;
     const bool cin  = a.conj_in != 0;
-    for (int i = threadIdx.x; i < total; i += blockDim.x)
-    {
-        const int n2i = i >> sh;
-        const int r   = i & (S - 1);
-        if (r0 + r < n1)
-            sm[r * stride + pidx<T>(n2i)] = conj_if(y[(long long)n2i * n1 + r0 + r], cin);
-    }
+    copy_batched<8>(
+        total,
+        [&](int i)
+        {
+            const int n2i = i >> sh;
+            const int r   = i & (S - 1);
+            return r0 + r < n1 ? y[(long long)n2i * n1 + r0 + r] : mk<T>(0, 0);
+        },
+        [&](int i, cpx<T> v)
+        {
+            const int n2i = i >> sh;
+            const int r   = i & (S - 1);
+            sm[r * stride + F::pi(n2i)] = conj_if(v, cin);
+        });
     __syncthreads();
     const group_map gm(ts, S);
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     const bool cout = a.conj_out != 0;
+#pragma unroll 4
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {
         const int k2 = i >> sh;
         const int r  = i & (S - 1);
         if (r0 + r < n1)
-            X[(long long)(r0 + r) + (long long)n1 * k2] = conj_if(sm[r * stride + pidx<T>(k2)], cout);
+            X[(long long)(r0 + r) + (long long)n1 * k2] = conj_if(sm[r * stride + F::pi(k2)], cout);
     }
 }
 

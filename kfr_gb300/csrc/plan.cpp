@@ -369,6 +369,9 @@ void block_program<T>::build(int n_, int kind)
         if (ept == 0)
             throw std::invalid_argument("internal: length exceeds one CTA");
     }
+    gstride = padded_len_host<T>(n);
+    if (ct && sizeof(T) == 4)
+        gstride = ct_group_stride_f32(n, ts);
     std::memset(&desc, 0, sizeof(desc));
     desc.n     = n;
     desc.npass = int(radices.size());
@@ -410,7 +413,7 @@ block_cfg block_program<T>::cfg(long long batch, int spc_cap) const
     block_cfg c;
     c.ept              = ept;
     c.ts               = ts;
-    const int per_sig  = padded_len_host<T>(n) * int(2 * sizeof(T));
+    const int per_sig  = gstride * int(2 * sizeof(T));
     const int max_thr  = ct ? (sizeof(T) == 4 ? 1024 : 512) : max_threads_for(int(sizeof(T)), ept);
     int spc            = std::max(1, 256 / ts);
     spc                = std::min(spc, std::max(1, max_thr / ts));
@@ -437,7 +440,7 @@ block_cfg block_program<T>::cfg_tile(int tile) const
     c.ts      = ts;
     c.spc     = tile;
     c.threads = ((tile * ts + 31) / 32) * 32;
-    c.smem    = tile * padded_len_host<T>(n) * int(2 * sizeof(T));
+    c.smem    = tile * gstride * int(2 * sizeof(T));
     c.grid    = 1;
     c.ct      = ct;
     return c;
@@ -621,8 +624,8 @@ int complex_engine<T>::rader_tile_smem(int spc) const
 {
     // two stage tiles, the padded work tile, x[0] and A[0] per signal, two mbarriers
     const int esz   = int(2 * sizeof(T));
-    const int stage = rader_stage_len(spc, int(n_), padded_len_host<T>(int(n_ - 1)));
-    return (2 * stage + spc * padded_len_host<T>(int(n_ - 1)) + 2 * spc) * esz + 16;
+    const int stage = rader_stage_len(spc, int(n_), prog_.gstride);
+    return (2 * stage + spc * prog_.gstride + 2 * spc) * esz + 16;
 }
 
 template <typename T>
@@ -643,7 +646,7 @@ void complex_engine<T>::plan_pipe()
         const int threads = ((spc * prog_.ts + 31) / 32) * 32;
         if (threads > 1024)
             break;
-        const int smem = 2 * spc * n * esz + spc * padded_len_host<T>(n) * esz + 64;
+        const int smem = 2 * spc * n * esz + spc * prog_.gstride * esz + 64;
         if (smem > smem_budget())
             break;
         const int by_smem = (max_smem_bytes() + 1024) / (smem + 1024);
@@ -733,7 +736,7 @@ void complex_engine<T>::init_bluestein(long long n)
 template <typename T>
 int tile_for(const block_program<T>& p)
 {
-    const int per_sig = padded_len_host<T>(p.n) * int(2 * sizeof(T));
+    const int per_sig = (p.gstride ? p.gstride : padded_len_host<T>(p.n)) * int(2 * sizeof(T));
     const int max_thr = p.ct ? (sizeof(T) == 4 ? 1024 : 512) : max_threads_for(int(sizeof(T)), p.ept);
     int s             = 16;
     while (s > 1 && (s * per_sig > smem_budget() || s * p.ts > max_thr))
@@ -886,7 +889,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             if (ntiles > 0)
             {
                 block_cfg pc = prog_.cfg_tile(pipe_spc_);
-                pc.smem = 2 * pipe_spc_ * int(n_) * int(esz) + pipe_spc_ * padded_len_host<T>(int(n_)) * int(esz) + 64;
+                pc.smem = 2 * pipe_spc_ * int(n_) * int(esz) + pipe_spc_ * prog_.gstride * int(esz) + 64;
                 check(launch_ct_c2c_pipe_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st), "launch c2c (pipelined)");
                 done = ntiles * pipe_spc_;
             }

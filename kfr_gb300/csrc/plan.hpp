@@ -94,6 +94,7 @@ struct block_program
     int ept = 16;
     int ts  = 1;
     int ct  = 0; // nonzero: the compile-time kernel of this length is used
+    int gstride = 0; // elements between the shared-memory slots of consecutive signals
     fft_desc desc{};
     std::vector<int> radices;
     dbuf tw;
