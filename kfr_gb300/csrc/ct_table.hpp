@@ -12,9 +12,9 @@
     X(128, 8, 16, 8)                                                                                         \
     X(256, 16, 16, 16)                                                                                       \
     X(512, 64, 8, 8, 8)                                                                                      \
-    X(1000, 128, 8, 5, 5, 5)                                                                                 \
+    X(1000, 100, 10, 10, 10)                                                                                 \
     X(1024, 64, 16, 16, 4)                                                                                   \
-    X(1536, 192, 8, 8, 8, 3)                                                                                 \
+    X(1536, 96, 16, 16, 6)                                                                                   \
     X(2048, 128, 16, 16, 8)                                                                                  \
     X(2187, 243, 9, 9, 9, 3)                                                                                 \
     X(4096, 256, 16, 16, 16)                                                                                 \
@@ -74,7 +74,8 @@
 // these entries were chosen with a wavefront model of every pass's accesses (odd radices do best unpadded).
 #define KFR_CT_LAYOUT_F32(X)                                                                                \
     X(126, 9, 0, 10)                                                                                         \
-    X(2187, 243, 0, 0)                                                                                       \
+    X(1000, 100, 0, 11)                                                                                      \
+    X(2187, 243, 0, 7)                                                                                       \
     X(8190, 1024, 0, 0)
 
 #if defined(__CUDACC__)

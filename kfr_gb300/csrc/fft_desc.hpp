@@ -50,15 +50,15 @@ inline int padded_len_host(int n)
     return n + (n >> (sizeof(T) == 4 ? 4 : 3)) + 1;
 }
 
-// Elements of one stage buffer of the tiled Rader kernel: the enclosing 16-byte range of a tile of spc
-// signals of n elements, or the padded layout of spc (n - 1)-point work signals, whichever is larger,
-// rounded up to 128 bytes so that the second buffer stays aligned for bulk copies.
+// Elements of one stage buffer of the pipelined kernels: the enclosing 16-byte range of a tile of spc
+// signals of n elements, or the padded layout of spc work signals (`gstride` apart), whichever is larger,
+// rounded up to 128 bytes so that the next buffer stays aligned for bulk copies.
 #if defined(__CUDACC__)
 __host__ __device__
 #endif
-    inline constexpr int rader_stage_len(int spc, int n, int padded)
+    inline constexpr int pipe_stage_len(int spc, int n, int gstride)
 {
-    return ((((spc * n + 3) / 2 * 2) > spc * padded ? ((spc * n + 3) / 2 * 2) : spc * padded) + 15) / 16 * 16;
+    return ((((spc * n + 3) / 2 * 2) > spc * gstride ? ((spc * n + 3) / 2 * 2) : spc * gstride) + 15) / 16 * 16;
 }
 
 struct pass_desc

@@ -175,9 +175,10 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     constexpr int STRIDE = F::gstride(N);
     const F fft(nullptr, a.d, F::ts);
     const int tile   = spc * N;
+    const int slen   = pipe_stage_len(spc, N, STRIDE);
     cpx<T>* stage0   = reinterpret_cast<cpx<T>*>(smem_raw);
-    cpx<T>* stage1   = stage0 + tile;
-    cpx<T>* work     = stage1 + tile;
+    cpx<T>* stage1   = stage0 + slen;
+    cpx<T>* work     = stage1 + slen;
     uint64_t* bars   = reinterpret_cast<uint64_t*>(work + spc * STRIDE);
     const uint32_t bytes = uint32_t(tile) * uint32_t(sizeof(cpx<T>));
     const cpx<T>* in = reinterpret_cast<const cpx<T>*>(a.in);
@@ -225,13 +226,19 @@ __global__ void __launch_bounds__(F::max_threads, 1)
             pending |= 1u << (sb ^ 1);
             if (threadIdx.x == 0)
             {
-                // the other stage was last read by the previous tile's first pass, which ended in a barrier
+                // the other stage was last used by the previous tile's passes, which ended in a barrier
                 fence_proxy_async_smem();
                 mbar_arrive_expect_tx(&bars[sb ^ 1], bytes);
                 bulk_g2s(sb ? stage0 : stage1, in + tn * tile, bytes, &bars[sb ^ 1]);
             }
         }
-        fft.run_io(stage + gm.g * N, work + gm.g * STRIDE, out + (t * spc + gm.g) * N, tw, inv, gm.lt);
+        // ping-pong between the stage (its padded layout, once the first pass has read the tile) and the
+        // work buffer; the last pass stores straight to global memory (stride one across threads)
+        const cpx<T>* src  = stage + gm.g * N;
+        cpx<T>* gout       = out + (t * spc + gm.g) * N;
+        const auto nothing = []() {};
+        fft.run_pp([&](int p) { return conj_if(src[p], inv); }, [&](int q, cpx<T> x) { gout[q] = conj_if(x, inv); },
+                   nothing, nothing, stage + gm.g * STRIDE, work + gm.g * STRIDE, tw, gm.lt);
     }
 }
 
@@ -373,7 +380,7 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
 template <typename T, class F>
 __host__ __device__ constexpr int rader_stage_elems(int spc)
 {
-    return rader_stage_len(spc, F::n + 1, F::gstride(F::n));
+    return pipe_stage_len(spc, F::n + 1, F::gstride(F::n));
 }
 
 template <typename T, class F>
