@@ -41,8 +41,8 @@
 // lengths 2^15 .. 2^24
 #define KFR_CT_FOURSTEP_F32(X)                                                                              \
     X(128, 8, 16, 8)                                                                                         \
-    X(160, 32, 8, 4, 5)                                                                                      \
-    X(192, 16, 16, 4, 3)                                                                                     \
+    X(160, 16, 16, 10)                                                                                       \
+    X(192, 16, 16, 12)                                                                                       \
     X(256, 16, 16, 16)                                                                                       \
     X(512, 64, 8, 8, 8)                                                                                      \
     X(1024, 64, 16, 16, 4)                                                                                   \

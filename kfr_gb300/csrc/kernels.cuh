@@ -23,6 +23,7 @@ namespace kfr_gpu
 template <typename T, int EPT>
 struct rt_fft
 {
+    static constexpr bool compile_time = false;
     // the block FFT keeps EPT complex values per thread in registers
     static constexpr int max_threads = (sizeof(T) == 4 ? 1024 : 512) / (EPT / 16);
     const pass_desc* sp;
@@ -43,6 +44,7 @@ struct rt_fft
 template <typename T, int N, int TS, int... Rs>
 struct ct_fft
 {
+    static constexpr bool compile_time = true;
     static constexpr int max_threads = sizeof(T) == 4 ? 1024 : 512;
     static constexpr int n           = N;
     static constexpr int ts          = TS;
@@ -761,6 +763,29 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_cols(const fourstep_ar
         });
     __syncthreads();
     const group_map gm(ts, S);
+    const cpx<T>* twA = reinterpret_cast<const cpx<T>*>(a.twA);
+    const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
+    if constexpr (F::compile_time)
+    {
+        if (a.pingpong && !a.same_layout)
+        {
+            // ping-pong passes with a second buffer after the tile; the last pass applies W_N^{col k1} and
+            // stores the column contiguously (stride one across a signal's threads)
+            const int col      = c0 + gm.g;
+            const bool cout    = a.conj_out != 0;
+            const auto nothing = []() {};
+            fft.run_pp([&](int p) { return sm[gm.g * stride + F::pi(p)]; },
+                       [&](int k1, cpx<T> v)
+                       {
+                           if (col < n2)
+                               y[(long long)col * n1 + k1] =
+                                   conj_if(v * twiddle_2level(twA, twB, (long long)col * k1, a.lbits), cout);
+                       },
+                       nothing, nothing, sm + gm.g * stride, sm + (S + gm.g) * stride,
+                       reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
+            return;
+        }
+    }
     fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     if (a.same_layout)
     {
@@ -775,8 +800,6 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_cols(const fourstep_ar
         }
         return;
     }
-    const cpx<T>* twA = reinterpret_cast<const cpx<T>*>(a.twA);
-    const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
 #pragma unroll 4
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {
@@ -823,8 +846,31 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_rows(const fourstep_ar
         });
     __syncthreads();
     const group_map gm(ts, S);
-    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
     const bool cout = a.conj_out != 0;
+    if constexpr (F::compile_time)
+    {
+        if (a.pingpong)
+        {
+            // ping-pong passes with a second buffer after the tile; the last pass stages its output as
+            // [k2][row] (rows XOR-swizzled by k2) in the buffer it does not read, for row-contiguous stores
+            cpx<T>* B          = sm + S * stride;
+            cpx<T>* stg        = F::npass % 2 == 0 ? sm : B;
+            const auto nothing = []() {};
+            fft.run_pp([&](int p) { return sm[gm.g * stride + F::pi(p)]; },
+                       [&](int k2, cpx<T> v) { stg[k2 * S + (gm.g ^ (k2 & (S - 1)))] = v; }, nothing, nothing,
+                       sm + gm.g * stride, B + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
+#pragma unroll 4
+            for (int i = threadIdx.x; i < total; i += blockDim.x)
+            {
+                const int k2 = i >> sh;
+                const int r  = i & (S - 1);
+                if (r0 + r < n1)
+                    X[(long long)(r0 + r) + (long long)n1 * k2] = conj_if(stg[k2 * S + (r ^ (k2 & (S - 1)))], cout);
+            }
+            return;
+        }
+    }
+    fft.run(sm + gm.g * stride, reinterpret_cast<const cpx<T>*>(a.tw), gm.lt);
 #pragma unroll 4
     for (int i = threadIdx.x; i < total; i += blockDim.x)
     {

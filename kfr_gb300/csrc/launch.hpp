@@ -121,6 +121,7 @@ struct fourstep_args
     int lbits;
     int tile_shift;  // log2(tile)
     int same_layout; // cols pass: store back to x's own layout (multi-dimensional axes) and skip the twiddle
+    int pingpong;    // compile-time kernels: ping-pong passes over two buffers per signal (2x shared memory)
     fast_div div_n;  // divides by the FFT length of this pass
 };
 

@@ -66,6 +66,7 @@ void md_axes<T>::run(void* data, long long batch, bool inverse, cudaStream_t st)
                 sh++;
             a.tile_shift  = sh;
             a.same_layout = 1;
+            a.pingpong    = 0;
             a.conj_in     = inverse;
             a.conj_out    = inverse;
             a.tw          = ax.prog->tw.get();

@@ -734,9 +734,9 @@ void complex_engine<T>::init_bluestein(long long n)
 }
 
 template <typename T>
-int tile_for(const block_program<T>& p)
+int tile_for(const block_program<T>& p, int buffers)
 {
-    const int per_sig = (p.gstride ? p.gstride : padded_len_host<T>(p.n)) * int(2 * sizeof(T));
+    const int per_sig = buffers * (p.gstride ? p.gstride : padded_len_host<T>(p.n)) * int(2 * sizeof(T));
     const int max_thr = p.ct ? (sizeof(T) == 4 ? 1024 : 512) : max_threads_for(int(sizeof(T)), p.ept);
     int s             = 16;
     while (s > 1 && (s * per_sig > smem_budget() || s * p.ts > max_thr))
@@ -799,6 +799,27 @@ bool complex_engine<T>::plan_fourstep(long long n)
     prows_.build(int(n2_), CT_FOURSTEP);
     tile_c_ = tile_for(pcols_);
     tile_r_ = tile_for(prows_);
+    // compile-time passes run ping-pong (two buffers per signal) unless that would shrink a tile below 8
+    // signals (short row segments coalesce poorly)
+    pp_c_ = pp_r_ = false;
+    if (pcols_.ct)
+    {
+        const int t2 = tile_for(pcols_, 2);
+        if (t2 >= 8 || t2 == tile_c_)
+        {
+            tile_c_ = t2;
+            pp_c_   = true;
+        }
+    }
+    if (prows_.ct)
+    {
+        const int t2 = tile_for(prows_, 2);
+        if (t2 >= 8 || t2 == tile_r_)
+        {
+            tile_r_ = t2;
+            pp_r_   = true;
+        }
+    }
     // two-level table for W_N^m, m < N
     int lb = 0;
     while ((1LL << (2 * lb)) < n)
@@ -993,7 +1014,10 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             a.tw       = pcols_.tw.get();
             a.d        = pcols_.desc;
             a.div_n    = make_fast_div(uint32_t(n1_));
+            a.pingpong   = pp_c_;
             block_cfg cc = pcols_.cfg_tile(tile_c_);
+            if (pp_c_)
+                cc.smem *= 2; // ping-pong buffers
             cc.grid      = (n2_ + tile_c_ - 1) / tile_c_;
             check(launch_fs_cols<T>(a, cc, st), "launch four-step columns");
             // row pass: scratch -> out
@@ -1006,7 +1030,10 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             a.tw       = prows_.tw.get();
             a.d        = prows_.desc;
             a.div_n    = make_fast_div(uint32_t(n2_));
+            a.pingpong   = pp_r_;
             block_cfg cr = prows_.cfg_tile(tile_r_);
+            if (pp_r_)
+                cr.smem *= 2;
             cr.grid      = (n1_ + tile_r_ - 1) / tile_r_;
             check(launch_fs_rows<T>(a, cr, st), "launch four-step rows");
         }
@@ -1304,8 +1331,8 @@ std::string dct_engine<T>::describe() const
     return s.str();
 }
 
-template int tile_for<float>(const block_program<float>&);
-template int tile_for<double>(const block_program<double>&);
+template int tile_for<float>(const block_program<float>&, int);
+template int tile_for<double>(const block_program<double>&, int);
 template struct block_program<float>;
 template struct block_program<double>;
 template class complex_engine<float>;

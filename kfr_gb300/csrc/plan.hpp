@@ -112,10 +112,10 @@ struct block_program
 
 // Dynamic shared memory a block FFT kernel may use (device limit less the static pass list and a reserve).
 int smem_budget();
-// Largest power-of-two number of signals (<= 16) of `p` that fit one CTA: the column / row tile of the
-// strided passes.  0 if not even one fits.
+// Largest power-of-two number of signals (<= 16) of `p` that fit one CTA with `buffers` shared-memory
+// buffers per signal: the column / row tile of the strided passes.  0 if not even one fits.
 template <typename T>
-int tile_for(const block_program<T>& p);
+int tile_for(const block_program<T>& p, int buffers = 1);
 
 template <typename T>
 class complex_engine
@@ -161,6 +161,7 @@ private:
     long long n1_ = 0, n2_ = 0;
     block_program<T> pcols_, prows_;
     int tile_c_ = 1, tile_r_ = 1;
+    bool pp_c_ = false, pp_r_ = false; // ping-pong column / row passes
     dbuf twA_, twB_;
     int lbits_ = 0;
     // pipelined smem path (compile-time lengths): signals per tile, 0 = not used
