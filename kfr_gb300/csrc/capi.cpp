@@ -87,11 +87,31 @@ enum : uint32_t
     TAG_FLT_F64  = 0x32544c46u,
 };
 
+// Streams and per-stream buffers of the pipelined host-to-host path (see run_chunked).
+constexpr int kPipeStreams = 3;
+struct pipe_set
+{
+    cudaStream_t s[kPipeStreams] = {};
+    dbuf in[kPipeStreams], out[kPipeStreams], scr[kPipeStreams];
+    pipe_set()
+    {
+        for (auto& x : s)
+            check(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking), "create stream");
+    }
+    ~pipe_set()
+    {
+        for (auto x : s)
+            if (x)
+                cudaStreamDestroy(x);
+    }
+};
+
 struct plan_base
 {
     uint32_t tag;
     std::mutex mu;     // guards the plan-owned staging and scratch buffers
     dbuf stage_in, stage_out, scratch;
+    std::unique_ptr<pipe_set> pipes;
     explicit plan_base(uint32_t t) : tag(t) {}
     virtual ~plan_base() { tag = 0; }
 };
@@ -290,6 +310,55 @@ void run(plan_base& pl, void* out, size_t out_bytes, const void* in, size_t in_b
         check(cudaStreamSynchronize(st), "execute");
 }
 
+// Host buffers on both sides of a synchronous call of a batch-separable transform: the batch runs as a
+// pipeline of chunks (about 16 MiB of input each) over kPipeStreams streams, so that copying chunk c+1 in,
+// transforming chunk c and copying chunk c-1 out overlap (the two copy directions and the kernels run
+// concurrently).  exec(dout, din, nb, scratch, stream) transforms nb signals; scr_bytes(nb) is its scratch.
+// Returns false (nothing done) when the call does not qualify: device pointers, a caller stream, or a
+// batch too small to split.
+template <typename Exec, typename Scr>
+bool run_chunked(plan_base& pl, void* out, size_t out_per, const void* in, size_t in_per, size_t batch, void* stream,
+                 Scr&& scr_bytes, Exec&& exec)
+{
+    if (stream || !out || !in || batch < 2 || is_device_ptr(in) || is_device_ptr(out))
+        return false;
+    const size_t per   = std::max(in_per, out_per);
+    const size_t chunk = std::max<size_t>(1, std::min<size_t>(batch, (size_t(16) << 20) / std::max<size_t>(per, 1)));
+    const size_t nchunks = (batch + chunk - 1) / chunk;
+    if (nchunks < 2)
+        return false;
+    std::unique_lock<std::mutex> lock(pl.mu);
+    if (!pl.pipes)
+        pl.pipes.reset(new pipe_set());
+    pipe_set& P      = *pl.pipes;
+    const size_t scr = scr_bytes((long long)chunk);
+    for (int k = 0; k < kPipeStreams; k++)
+    {
+        P.in[k].ensure(chunk * in_per);
+        P.out[k].ensure(chunk * out_per);
+        if (scr)
+            P.scr[k].ensure(scr);
+    }
+    const char* hin = static_cast<const char*>(in);
+    char* hout      = static_cast<char*>(out);
+    for (size_t c = 0; c < nchunks; c++)
+    {
+        const int k       = int(c % kPipeStreams);
+        const size_t b0   = c * chunk;
+        const size_t nb   = std::min(chunk, batch - b0);
+        cudaStream_t st   = P.s[k];
+        check(cudaMemcpyAsync(P.in[k].get(), hin + b0 * in_per, nb * in_per, cudaMemcpyHostToDevice, st),
+              "copy input to device");
+        exec(P.out[k].get(), P.in[k].get(), (long long)nb, scr ? P.scr[k].get() : nullptr, st);
+        check(cudaGetLastError(), "kernel launch");
+        check(cudaMemcpyAsync(hout + b0 * out_per, P.out[k].get(), nb * out_per, cudaMemcpyDeviceToHost, st),
+              "copy result to host");
+    }
+    for (auto st : P.s)
+        check(cudaStreamSynchronize(st), "execute");
+    return true;
+}
+
 template <typename T>
 void* create_dft(size_t n)
 {
@@ -302,10 +371,15 @@ void exec_dft(void* h, size_t batch, void* out, const void* in, uint8_t* temp, b
     auto* p = as<dft_obj<T>>(h, tags<T>::dft);
     if (batch == 0 || p->n == 0)
         return;
-    const size_t bytes = batch * p->n * 2 * sizeof(T);
+    const size_t per   = p->n * 2 * sizeof(T);
+    const size_t bytes = batch * per;
     const size_t scr   = size_t(p->scratch_elems((long long)batch)) * 2 * sizeof(T);
-    run(*p, out, bytes, in, bytes, temp, scr, stream, false,
-        [&](void* o, const void* i, void* s, cudaStream_t st) { p->execute(o, i, (long long)batch, inverse, s, st); });
+    if (!run_chunked(
+            *p, out, per, in, per, batch, stream,
+            [&](long long nb) { return size_t(p->scratch_elems(nb)) * 2 * sizeof(T); },
+            [&](void* o, const void* i, long long nb, void* s, cudaStream_t st) { p->execute(o, i, nb, inverse, s, st); }))
+        run(*p, out, bytes, in, bytes, temp, scr, stream, false,
+            [&](void* o, const void* i, void* s, cudaStream_t st) { p->execute(o, i, (long long)batch, inverse, s, st); });
     if (!stream)
         p->check_device_error();
 }
@@ -320,12 +394,21 @@ void exec_real(void* h, size_t batch, void* out, const void* in, uint8_t* temp, 
     const size_t cbytes = batch * p->clen() * 2 * sizeof(T);
     const size_t scr    = size_t(p->scratch_elems((long long)batch)) * 2 * sizeof(T);
     const bool alias    = batch > 1 || p->md != nullptr;
+    const auto scr_of   = [&](long long nb) { return size_t(p->scratch_elems(nb)) * 2 * sizeof(T); };
     if (!inverse)
-        run(*p, out, cbytes, in, rbytes, temp, scr, stream, alias,
-            [&](void* o, const void* i, void* s, cudaStream_t st) { p->forward(o, i, (long long)batch, s, st); });
+    {
+        if (!run_chunked(*p, out, cbytes / batch, in, rbytes / batch, batch, stream, scr_of,
+                         [&](void* o, const void* i, long long nb, void* s, cudaStream_t st) { p->forward(o, i, nb, s, st); }))
+            run(*p, out, cbytes, in, rbytes, temp, scr, stream, alias,
+                [&](void* o, const void* i, void* s, cudaStream_t st) { p->forward(o, i, (long long)batch, s, st); });
+    }
     else
-        run(*p, out, rbytes, in, cbytes, temp, scr, stream, alias,
-            [&](void* o, const void* i, void* s, cudaStream_t st) { p->inverse(o, i, (long long)batch, s, st); });
+    {
+        if (!run_chunked(*p, out, rbytes / batch, in, cbytes / batch, batch, stream, scr_of,
+                         [&](void* o, const void* i, long long nb, void* s, cudaStream_t st) { p->inverse(o, i, nb, s, st); }))
+            run(*p, out, rbytes, in, cbytes, temp, scr, stream, alias,
+                [&](void* o, const void* i, void* s, cudaStream_t st) { p->inverse(o, i, (long long)batch, s, st); });
+    }
 }
 
 template <typename T>
@@ -334,10 +417,15 @@ void exec_dct(void* h, size_t batch, void* out, const void* in, uint8_t* temp, b
     auto* p = as<dct_obj<T>>(h, tags<T>::dct);
     if (batch == 0 || p->n == 0)
         return;
-    const size_t bytes = batch * p->n * sizeof(T);
+    const size_t per   = p->n * sizeof(T);
+    const size_t bytes = batch * per;
     const size_t scr   = size_t(p->eng.scratch_elems((long long)batch)) * 2 * sizeof(T);
-    run(*p, out, bytes, in, bytes, temp, scr, stream, false,
-        [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.execute(o, i, (long long)batch, inverse, s, st); });
+    if (!run_chunked(
+            *p, out, per, in, per, batch, stream,
+            [&](long long nb) { return size_t(p->eng.scratch_elems(nb)) * 2 * sizeof(T); },
+            [&](void* o, const void* i, long long nb, void* s, cudaStream_t st) { p->eng.execute(o, i, nb, inverse, s, st); }))
+        run(*p, out, bytes, in, bytes, temp, scr, stream, false,
+            [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.execute(o, i, (long long)batch, inverse, s, st); });
 }
 
 template <typename T>

@@ -128,6 +128,40 @@ def test_rader_tiles_many_per_cta(orc, n, batch):
     assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
 
 
+@pytest.mark.parametrize("n,batch", [(1000, 5000), (8191, 700), (4096, 1100)])
+def test_host_buffers_pipelined_match_device(n, batch):
+    """Host input and output (the reference's calling convention) split into chunks that overlap copies with
+    transforms: same results as the device-resident call, forward and inverse, for complex, real and DCT
+    plans."""
+    rng = np.random.default_rng(n)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    plan = k.dft_plan(n, "f32")
+    for inverse in (False, True):
+        y = np.empty_like(x)
+        plan.execute_batch(y, x, batch, inverse=inverse)
+        xd = dev(x)
+        yd = torch.empty_like(xd)
+        plan.execute_batch(yd, xd, batch, inverse=inverse)
+        assert rel_rms(y, yd.cpu().numpy()) <= tol(n, "f32") / 4, inverse
+    if n % 2 == 0:
+        r = rng.standard_normal((batch, n)).astype(np.float32)
+        rp = k.dft_plan_real(n)
+        c = np.empty((batch, n // 2 + 1), np.complex64)
+        rp.execute_batch(c, r, batch)
+        cd = torch.empty((batch, n // 2 + 1), dtype=torch.complex64, device="cuda")
+        rp.execute_batch(cd, dev(r), batch)
+        assert rel_rms(c, cd.cpu().numpy()) <= tol(n, "f32") / 4
+        back = np.empty_like(r)
+        rp.execute_batch(back, c, batch, inverse=True)
+        assert rel_rms(back / n, r) <= 2 * tol(n, "f32")
+        dp = k.dct_plan(n)
+        d = np.empty_like(r)
+        dp.execute_batch(d, r, batch)
+        dd = torch.empty_like(dev(r))
+        dp.execute_batch(dd, dev(r), batch)
+        assert rel_rms(d, dd.cpu().numpy()) <= tol(n, "f32") / 4
+
+
 @pytest.mark.parametrize("n", [1 << 24, 30720000])
 def test_complex_dft_large_single(orc, n):
     """The large single transforms of the mixed-radix parity set (c32)."""
