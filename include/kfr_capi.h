@@ -266,6 +266,47 @@ KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
 
+/* Adjoints (vector-Jacobian products) for gradient-based callers; no counterpart in the reference, which has
+ * no differentiation.  Each maps the gradient of a transform's output (grad_out) to the gradient of its input
+ * (grad_in), batch signals laid out as in the batched calls above, with the same pointer and stream rules
+ * (the real and DCT adjoints keep their scratch in the plan and ignore temp).  Complex gradients follow the complex-autograd convention: for a real loss L the gradient of a
+ * complex value z is dL/dRe(z) + i dL/dIm(z).
+ *   kfr_dft_adjoint_batch:              of execute (inverse = 0) or execute_inverse (inverse = 1): the
+ *                                       unscaled transform in the other direction;
+ *   kfr_dft_real_adjoint_batch:         of the forward real DFT: the inverse real DFT of grad_out with bins
+ *                                       1 .. N/2-1 halved (one-dimensional plans);
+ *   kfr_dft_real_adjoint_inverse_batch: of the inverse real DFT: the forward real DFT of grad_out with bins
+ *                                       1 .. N/2-1 doubled (one-dimensional plans);
+ *   kfr_dct_adjoint_batch:              of the DCT-II (inverse = 0: DCT-III of grad_out with its first value
+ *                                       doubled) or of the reference's DCT-III (inverse = 1: DCT-II, then the
+ *                                       first value halved). */
+KFR_API_SPEC void kfr_dft_adjoint_batch_f32(KFR_DFT_PLAN_F32* plan, size_t batch, kfr_c32* grad_in,
+                                            const kfr_c32* grad_out, uint8_t* temp, kfr_bool inverse, void* stream);
+KFR_API_SPEC void kfr_dft_adjoint_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch, kfr_c64* grad_in,
+                                            const kfr_c64* grad_out, uint8_t* temp, kfr_bool inverse, void* stream);
+KFR_API_SPEC void kfr_dft_real_adjoint_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_f32* grad_in,
+                                                 const kfr_c32* grad_out, uint8_t* temp, void* stream);
+KFR_API_SPEC void kfr_dft_real_adjoint_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_f64* grad_in,
+                                                 const kfr_c64* grad_out, uint8_t* temp, void* stream);
+KFR_API_SPEC void kfr_dft_real_adjoint_inverse_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_c32* grad_in,
+                                                         const kfr_f32* grad_out, uint8_t* temp, void* stream);
+KFR_API_SPEC void kfr_dft_real_adjoint_inverse_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_c64* grad_in,
+                                                         const kfr_f64* grad_out, uint8_t* temp, void* stream);
+KFR_API_SPEC void kfr_dct_adjoint_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch, kfr_f32* grad_in,
+                                            const kfr_f32* grad_out, uint8_t* temp, kfr_bool inverse, void* stream);
+KFR_API_SPEC void kfr_dct_adjoint_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch, kfr_f64* grad_in,
+                                            const kfr_f64* grad_out, uint8_t* temp, kfr_bool inverse, void* stream);
+
+/* Gradients of the causal FIR convolution that a convolution filter (kfr_filter_create_convolution_plan) applies
+ * from a reset state, y[c][t] = sum_{m<ntaps} taps[m] x[c][t-m], over `channels` signals of n samples each
+ * (channel-major): grad_x[c][t] = sum_m taps[m] grad_y[c][t+m] and grad_taps[m] = sum_c sum_t grad_y[c][t]
+ * x[c][t-m].  Device pointers only; grad_x or grad_taps may be NULL when not wanted.  stream: NULL = default
+ * stream; the call returns when the gradients are written. */
+KFR_API_SPEC void kfr_fir_backward_f32(const kfr_f32* taps, size_t ntaps, size_t channels, size_t n, const kfr_f32* x,
+                                       const kfr_f32* grad_y, kfr_f32* grad_x, kfr_f32* grad_taps, void* stream);
+KFR_API_SPEC void kfr_fir_backward_f64(const kfr_f64* taps, size_t ntaps, size_t channels, size_t n, const kfr_f64* x,
+                                       const kfr_f64* grad_y, kfr_f64* grad_x, kfr_f64* grad_taps, void* stream);
+
 /* Allocation-free execution (no counterpart in the reference).
  *
  * Same transform as kfr_dft_execute_batch_f32, for callers that must not allocate GPU memory while they

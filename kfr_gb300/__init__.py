@@ -86,6 +86,11 @@ for sfx in ("f32", "f64"):
         f"kfr_filter_process_{sfx}": (None, [_P, _P, _P, _S]),
         f"kfr_filter_reset_{sfx}": (None, [_P]),
         f"kfr_filter_delete_plan_{sfx}": (None, [_P]),
+        f"kfr_dft_adjoint_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _B, _P]),
+        f"kfr_dft_real_adjoint_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _P]),
+        f"kfr_dft_real_adjoint_inverse_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _P]),
+        f"kfr_dct_adjoint_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _B, _P]),
+        f"kfr_fir_backward_{sfx}": (None, [_P, _S, _S, _S, _P, _P, _P, _P, _P]),
     })
 for fn in ("convolve", "correlate"):
     for sfx in ("f32", "f64", "c32", "c64"):
@@ -234,6 +239,11 @@ class dft_plan(_plan):
         _call(self._fn("execute_batch"), self.handle, batch, _addr(out), _addr(inp), _addr(temp), bool(inverse),
               _stream_addr(stream))
 
+    def adjoint_batch(self, grad_in, grad_out, batch, inverse=False, stream=None):
+        """Gradient of the input of execute_batch(inverse) from the gradient of its output."""
+        _call(self._fn("adjoint_batch"), self.handle, batch, _addr(grad_in), _addr(grad_out), None, bool(inverse),
+              _stream_addr(stream))
+
     def describe(self) -> str:
         if self.sfx != "f32":
             return ""
@@ -309,6 +319,11 @@ class dft_plan_real(_plan):
         op = "execute_inverse_batch" if inverse else "execute_batch"
         _call(self._fn(op), self.handle, batch, _addr(out), _addr(inp), _addr(temp), _stream_addr(stream))
 
+    def adjoint_batch(self, grad_in, grad_out, batch, inverse=False, stream=None):
+        """Gradient of the input of execute_batch(inverse) from the gradient of its output."""
+        op = "adjoint_inverse_batch" if inverse else "adjoint_batch"
+        _call(self._fn(op), self.handle, batch, _addr(grad_in), _addr(grad_out), None, _stream_addr(stream))
+
 
 class dct_plan(_plan):
     """DCT-II (forward) / DCT-III with X0 halved (inverse), unscaled (dct_plan<T>)."""
@@ -334,6 +349,19 @@ class dct_plan(_plan):
     def execute_batch(self, out, inp, batch, temp=None, inverse=False, stream=None):
         _call(self._fn("execute_batch"), self.handle, batch, _addr(out), _addr(inp), _addr(temp), bool(inverse),
               _stream_addr(stream))
+
+    def adjoint_batch(self, grad_in, grad_out, batch, inverse=False, stream=None):
+        """Gradient of the input of execute_batch(inverse) from the gradient of its output."""
+        _call(self._fn("adjoint_batch"), self.handle, batch, _addr(grad_in), _addr(grad_out), None, bool(inverse),
+              _stream_addr(stream))
+
+
+def fir_backward(taps, x, grad_y, grad_x=None, grad_taps=None, channels=1, stream=None):
+    """Gradients of the causal FIR convolution a convolution filter applies from a reset state (device tensors;
+    x and grad_y hold `channels` signals back to back)."""
+    n = _numel(x) // channels
+    _call(f"kfr_fir_backward_{_conv_sfx(x)}", _addr(taps), _numel(taps), channels, n, _addr(x), _addr(grad_y),
+          _addr(grad_x), _addr(grad_taps), _stream_addr(stream))
 
 
 class convolve_filter(_plan):

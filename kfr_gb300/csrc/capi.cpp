@@ -12,6 +12,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "adjoint.hpp"
 #include "conv.hpp"
 #include "convolve.hpp"
 #include "md.hpp"
@@ -426,6 +427,92 @@ void exec_dct(void* h, size_t batch, void* out, const void* in, uint8_t* temp, b
             [&](void* o, const void* i, long long nb, void* s, cudaStream_t st) { p->eng.execute(o, i, nb, inverse, s, st); }))
         run(*p, out, bytes, in, bytes, temp, scr, stream, false,
             [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.execute(o, i, (long long)batch, inverse, s, st); });
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Adjoints (adjoint.hpp): the same kernels as the transforms plus elementwise weighting.
+// ---------------------------------------------------------------------------------------------------
+
+template <typename T>
+void adj_real(void* h, size_t batch, void* grad_in, const void* grad_out, bool of_inverse, void* stream)
+{
+    auto* p = as<real_obj<T>>(h, tags<T>::real);
+    if (batch == 0)
+        return;
+    if (!p->eng1)
+        throw std::invalid_argument("adjoints are provided for one-dimensional real plans");
+    const long long b    = (long long)batch;
+    const size_t rbytes  = batch * p->n * sizeof(T);
+    const size_t spec    = batch * p->clen() * 2 * sizeof(T);
+    const size_t escr    = size_t(p->scratch_elems(b)) * 2 * sizeof(T);
+    if (!of_inverse)
+    {
+        // adjoint of r2c: c2r of the gradient with the interior bins halved (into scratch: the caller's
+        // gradient stays untouched)
+        run(*p, grad_in, rbytes, grad_out, spec, nullptr, spec + escr, stream, false,
+            [&](void* o, const void* i, void* s, cudaStream_t st)
+            {
+                check(launch_spectrum_weight<T>(s, i, b, (long long)p->clen(), p->ccs, T(0.5), st), "weight spectrum");
+                p->inverse(o, s, b, escr ? static_cast<char*>(s) + spec : nullptr, st);
+            });
+    }
+    else
+    {
+        // adjoint of c2r: r2c of the gradient with the interior bins doubled
+        run(*p, grad_in, spec, grad_out, rbytes, nullptr, escr, stream, true,
+            [&](void* o, const void* i, void* s, cudaStream_t st)
+            {
+                p->forward(o, i, b, s, st);
+                check(launch_spectrum_weight<T>(o, o, b, (long long)p->clen(), p->ccs, T(2), st), "weight spectrum");
+            });
+    }
+}
+
+template <typename T>
+void adj_dct(void* h, size_t batch, T* grad_in, const T* grad_out, bool of_inverse, void* stream)
+{
+    auto* p = as<dct_obj<T>>(h, tags<T>::dct);
+    if (batch == 0 || p->n == 0)
+        return;
+    const long long b   = (long long)batch, n = (long long)p->n;
+    const size_t bytes  = batch * p->n * sizeof(T);
+    const size_t escr   = size_t(p->eng.scratch_elems(b)) * 2 * sizeof(T);
+    if (!of_inverse)
+    {
+        // DCT-II^T = DCT-III with X0 at full weight = the reference's inverse of g with g[0] doubled
+        const size_t wb = (bytes + 255) / 256 * 256;
+        run(*p, grad_in, bytes, grad_out, bytes, nullptr, wb + escr, stream, false,
+            [&](void* o, const void* i, void* s, cudaStream_t st)
+            {
+                T* w = static_cast<T*>(s);
+                check(launch_scale_first<T>(w, static_cast<const T*>(i), b, n, T(2), st), "scale X0");
+                p->eng.execute(o, w, b, true, escr ? static_cast<char*>(s) + wb : nullptr, st);
+            });
+    }
+    else
+    {
+        // (DCT-III with X0 halved)^T = DCT-II, then element 0 halved
+        run(*p, grad_in, bytes, grad_out, bytes, nullptr, escr, stream, false,
+            [&](void* o, const void* i, void* s, cudaStream_t st)
+            {
+                p->eng.execute(o, i, b, false, s, st);
+                check(launch_scale_first<T>(static_cast<T*>(o), static_cast<const T*>(o), b, n, T(0.5), st), "scale X0");
+            });
+    }
+}
+
+template <typename T>
+void fir_bwd(const T* taps, size_t ntaps, size_t channels, size_t n, const T* x, const T* grad_y, T* grad_x,
+             T* grad_taps, void* stream)
+{
+    if (!taps || !x || !grad_y)
+        throw std::invalid_argument("NULL data pointer");
+    for (const void* q : { (const void*)taps, (const void*)x, (const void*)grad_y, (const void*)grad_x,
+                           (const void*)grad_taps })
+        if (q && !is_device_ptr(q))
+            throw std::invalid_argument("FIR backward needs device pointers");
+    fir_backward<T>(taps, (long long)ntaps, (long long)channels, (long long)n, x, grad_y, grad_x, grad_taps,
+                    static_cast<cudaStream_t>(stream));
 }
 
 template <typename T>
@@ -1092,6 +1179,64 @@ KFR_API_SPEC void kfr_filter_delete_plan_f32(KFR_FILTER_F32* plan)
 KFR_API_SPEC void kfr_filter_delete_plan_f64(KFR_FILTER_F64* plan)
 {
     try_void([&] { if (plan) delete as<filter_obj<double>>(plan, TAG_FLT_F64); });
+}
+
+/* Adjoints (no counterpart in the reference) */
+KFR_API_SPEC void kfr_dft_adjoint_batch_f32(KFR_DFT_PLAN_F32* plan, size_t batch, kfr_c32* grad_in,
+                                            const kfr_c32* grad_out, uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    try_void([&] { exec_dft<float>(plan, batch, grad_in, grad_out, temp, !inverse, stream); });
+}
+KFR_API_SPEC void kfr_dft_adjoint_batch_f64(KFR_DFT_PLAN_F64* plan, size_t batch, kfr_c64* grad_in,
+                                            const kfr_c64* grad_out, uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    try_void([&] { exec_dft<double>(plan, batch, grad_in, grad_out, temp, !inverse, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_adjoint_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_f32* grad_in,
+                                                 const kfr_c32* grad_out, uint8_t* temp, void* stream)
+{
+    (void)temp;
+    try_void([&] { adj_real<float>(plan, batch, grad_in, grad_out, false, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_adjoint_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_f64* grad_in,
+                                                 const kfr_c64* grad_out, uint8_t* temp, void* stream)
+{
+    (void)temp;
+    try_void([&] { adj_real<double>(plan, batch, grad_in, grad_out, false, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_adjoint_inverse_batch_f32(KFR_DFT_REAL_PLAN_F32* plan, size_t batch, kfr_c32* grad_in,
+                                                         const kfr_f32* grad_out, uint8_t* temp, void* stream)
+{
+    (void)temp;
+    try_void([&] { adj_real<float>(plan, batch, grad_in, grad_out, true, stream); });
+}
+KFR_API_SPEC void kfr_dft_real_adjoint_inverse_batch_f64(KFR_DFT_REAL_PLAN_F64* plan, size_t batch, kfr_c64* grad_in,
+                                                         const kfr_f64* grad_out, uint8_t* temp, void* stream)
+{
+    (void)temp;
+    try_void([&] { adj_real<double>(plan, batch, grad_in, grad_out, true, stream); });
+}
+KFR_API_SPEC void kfr_dct_adjoint_batch_f32(KFR_DCT_PLAN_F32* plan, size_t batch, kfr_f32* grad_in,
+                                            const kfr_f32* grad_out, uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    (void)temp;
+    try_void([&] { adj_dct<float>(plan, batch, grad_in, grad_out, inverse, stream); });
+}
+KFR_API_SPEC void kfr_dct_adjoint_batch_f64(KFR_DCT_PLAN_F64* plan, size_t batch, kfr_f64* grad_in,
+                                            const kfr_f64* grad_out, uint8_t* temp, kfr_bool inverse, void* stream)
+{
+    (void)temp;
+    try_void([&] { adj_dct<double>(plan, batch, grad_in, grad_out, inverse, stream); });
+}
+KFR_API_SPEC void kfr_fir_backward_f32(const kfr_f32* taps, size_t ntaps, size_t channels, size_t n, const kfr_f32* x,
+                                       const kfr_f32* grad_y, kfr_f32* grad_x, kfr_f32* grad_taps, void* stream)
+{
+    try_void([&] { fir_bwd<float>(taps, ntaps, channels, n, x, grad_y, grad_x, grad_taps, stream); });
+}
+KFR_API_SPEC void kfr_fir_backward_f64(const kfr_f64* taps, size_t ntaps, size_t channels, size_t n, const kfr_f64* x,
+                                       const kfr_f64* grad_y, kfr_f64* grad_x, kfr_f64* grad_taps, void* stream)
+{
+    try_void([&] { fir_bwd<double>(taps, ntaps, channels, n, x, grad_y, grad_x, grad_taps, stream); });
 }
 
 } // extern "C"
