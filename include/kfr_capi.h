@@ -77,6 +77,7 @@ KFR_OPAQUE_STRUCT(KFR_FILTER_F32)
 KFR_OPAQUE_STRUCT(KFR_FILTER_F64)
 KFR_OPAQUE_STRUCT(KFR_FILTER_C32)
 KFR_OPAQUE_STRUCT(KFR_FILTER_C64)
+KFR_OPAQUE_STRUCT(KFR_DFT_UNEVEN_F32) /* uneven batch plan: extension, no counterpart in the reference */
 
 #define KFR_DEFAULT_ALIGNMENT 64 /* include/kfr/capi.h:165 */
 #define KFR_HEADERS_VERSION 70000
@@ -265,6 +266,23 @@ KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size
 
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
+
+/* Uneven batch (no counterpart in the reference, whose callers loop over one plan per length): `count` complex
+ * signals of the given lengths stored back to back, transformed by one persistent work-queue launch (plus
+ * regular launches for signals too long for one CTA), replayed as a CUDA graph after the first call with a
+ * given (out, in, direction).  autotune: time candidate radix orders and tiles per length class when the
+ * plan is created (the choice is cached for the process).  in and out are device pointers (count * total
+ * elements, see kfr_dft_uneven_get_size_f32); stream: NULL = default stream, synchronous.
+ * kfr_dft_uneven_execute_per_signal_f32 runs the same transforms as one regular plan execution per signal
+ * (the plain form, for comparison). */
+KFR_API_SPEC KFR_DFT_UNEVEN_F32* kfr_dft_create_uneven_plan_f32(const size_t* lengths, size_t count, kfr_bool autotune);
+KFR_API_SPEC size_t kfr_dft_uneven_get_size_f32(KFR_DFT_UNEVEN_F32* plan);
+KFR_API_SPEC void kfr_dft_uneven_execute_f32(KFR_DFT_UNEVEN_F32* plan, kfr_c32* out, const kfr_c32* in, kfr_bool inverse,
+                                             void* stream);
+KFR_API_SPEC void kfr_dft_uneven_execute_per_signal_f32(KFR_DFT_UNEVEN_F32* plan, kfr_c32* out, const kfr_c32* in,
+                                                        kfr_bool inverse, void* stream);
+KFR_API_SPEC size_t kfr_dft_uneven_describe_f32(KFR_DFT_UNEVEN_F32* plan, char* buf, size_t size);
+KFR_API_SPEC void kfr_dft_uneven_delete_plan_f32(KFR_DFT_UNEVEN_F32* plan);
 
 /* Adjoints (vector-Jacobian products) for gradient-based callers; no counterpart in the reference, which has
  * no differentiation.  Each maps the gradient of a transform's output (grad_out) to the gradient of its input

@@ -111,6 +111,12 @@ _SIGS.update({
     "kfr_dft_cache_clear": (None, []),
     "kfr_autocorrelate_f32": (_S, [_P, _P, _S]),
     "kfr_autocorrelate_f64": (_S, [_P, _P, _S]),
+    "kfr_dft_create_uneven_plan_f32": (_P, [_P, _S, _B]),
+    "kfr_dft_uneven_get_size_f32": (_S, [_P]),
+    "kfr_dft_uneven_execute_f32": (None, [_P, _P, _P, _B, _P]),
+    "kfr_dft_uneven_execute_per_signal_f32": (None, [_P, _P, _P, _B, _P]),
+    "kfr_dft_uneven_describe_f32": (_S, [_P, ctypes.c_char_p, _S]),
+    "kfr_dft_uneven_delete_plan_f32": (None, [_P]),
 })
 
 
@@ -362,6 +368,39 @@ def fir_backward(taps, x, grad_y, grad_x=None, grad_taps=None, channels=1, strea
     n = _numel(x) // channels
     _call(f"kfr_fir_backward_{_conv_sfx(x)}", _addr(taps), _numel(taps), channels, n, _addr(x), _addr(grad_y),
           _addr(grad_x), _addr(grad_taps), _stream_addr(stream))
+
+
+class dft_plan_uneven(_plan):
+    """Many complex signals of uneven lengths stored back to back, one persistent launch (c32)."""
+
+    _prefix = "kfr_dft_uneven"
+
+    def __init__(self, lengths, autotune=True):
+        arr = np.ascontiguousarray(np.asarray(lengths, dtype=np.uint64))
+        self._lengths = arr
+        h = _call("kfr_dft_create_uneven_plan_f32", arr.ctypes.data, len(arr), bool(autotune))
+        super().__init__(h, "f32")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().kfr_dft_uneven_delete_plan_f32(self.handle)
+            self.handle = None
+
+    @property
+    def size(self):
+        return _call("kfr_dft_uneven_get_size_f32", self.handle)
+
+    def execute(self, out, inp, inverse=False, stream=None):
+        _call("kfr_dft_uneven_execute_f32", self.handle, _addr(out), _addr(inp), bool(inverse), _stream_addr(stream))
+
+    def execute_per_signal(self, out, inp, inverse=False, stream=None):
+        _call("kfr_dft_uneven_execute_per_signal_f32", self.handle, _addr(out), _addr(inp), bool(inverse),
+              _stream_addr(stream))
+
+    def describe(self) -> str:
+        buf = ctypes.create_string_buffer(512)
+        _call("kfr_dft_uneven_describe_f32", self.handle, buf, 512)
+        return buf.value.decode()
 
 
 class convolve_filter(_plan):

@@ -16,6 +16,7 @@
 #include "conv.hpp"
 #include "convolve.hpp"
 #include "md.hpp"
+#include "uneven.hpp"
 #include "plan.hpp"
 
 using namespace kfr_gpu;
@@ -86,6 +87,7 @@ enum : uint32_t
     TAG_DCT_F64  = 0x32544344u,
     TAG_FLT_F32  = 0x31544c46u,
     TAG_FLT_F64  = 0x32544c46u,
+    TAG_UNEVEN   = 0x31564e55u,
 };
 
 // Streams and per-stream buffers of the pipelined host-to-host path (see run_chunked).
@@ -513,6 +515,33 @@ void fir_bwd(const T* taps, size_t ntaps, size_t channels, size_t n, const T* x,
             throw std::invalid_argument("FIR backward needs device pointers");
     fir_backward<T>(taps, (long long)ntaps, (long long)channels, (long long)n, x, grad_y, grad_x, grad_taps,
                     static_cast<cudaStream_t>(stream));
+}
+
+struct uneven_obj : plan_base
+{
+    uneven_plan plan;
+    uneven_obj(const std::vector<long long>& lengths, bool tune) : plan_base(TAG_UNEVEN), plan(lengths, tune) {}
+};
+
+void exec_uneven(void* h, void* out, const void* in, bool inverse, void* stream, bool per_signal)
+{
+    auto* p = as<uneven_obj>(h, TAG_UNEVEN);
+    if (p->plan.total() == 0)
+        return;
+    if (!out || !in || !is_device_ptr(out) || !is_device_ptr(in))
+        throw std::invalid_argument("uneven batch execution needs device pointers");
+    std::unique_lock<std::mutex> lock(p->mu);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (per_signal)
+        p->plan.execute_per_signal(out, in, inverse, st);
+    else
+        p->plan.execute(out, in, inverse, st);
+    check(cudaGetLastError(), "uneven batch");
+    if (!stream)
+    {
+        check(cudaStreamSynchronize(st), "uneven batch");
+        p->plan.check_device_error();
+    }
 }
 
 template <typename T>
@@ -1237,6 +1266,54 @@ KFR_API_SPEC void kfr_fir_backward_f64(const kfr_f64* taps, size_t ntaps, size_t
                                        const kfr_f64* grad_y, kfr_f64* grad_x, kfr_f64* grad_taps, void* stream)
 {
     try_void([&] { fir_bwd<double>(taps, ntaps, channels, n, x, grad_y, grad_x, grad_taps, stream); });
+}
+
+/* Uneven batch (extension) */
+KFR_API_SPEC KFR_DFT_UNEVEN_F32* kfr_dft_create_uneven_plan_f32(const size_t* lengths, size_t count, kfr_bool autotune)
+{
+    return try_fn(
+        [&]
+        {
+            if (!lengths && count)
+                throw std::invalid_argument("lengths is NULL");
+            std::vector<long long> l(lengths, lengths + count);
+            return reinterpret_cast<KFR_DFT_UNEVEN_F32*>(static_cast<plan_base*>(new uneven_obj(l, autotune != 0)));
+        },
+        (KFR_DFT_UNEVEN_F32*)nullptr);
+}
+KFR_API_SPEC size_t kfr_dft_uneven_get_size_f32(KFR_DFT_UNEVEN_F32* plan)
+{
+    return try_fn([&] { return size_t(as<uneven_obj>(plan, TAG_UNEVEN)->plan.total()); }, size_t(0));
+}
+KFR_API_SPEC void kfr_dft_uneven_execute_f32(KFR_DFT_UNEVEN_F32* plan, kfr_c32* out, const kfr_c32* in, kfr_bool inverse,
+                                             void* stream)
+{
+    try_void([&] { exec_uneven(plan, out, in, inverse != 0, stream, false); });
+}
+KFR_API_SPEC void kfr_dft_uneven_execute_per_signal_f32(KFR_DFT_UNEVEN_F32* plan, kfr_c32* out, const kfr_c32* in,
+                                                        kfr_bool inverse, void* stream)
+{
+    try_void([&] { exec_uneven(plan, out, in, inverse != 0, stream, true); });
+}
+KFR_API_SPEC size_t kfr_dft_uneven_describe_f32(KFR_DFT_UNEVEN_F32* plan, char* buf, size_t size)
+{
+    return try_fn(
+        [&]
+        {
+            const std::string d = as<uneven_obj>(plan, TAG_UNEVEN)->plan.describe();
+            if (buf && size)
+            {
+                const size_t k = std::min(size - 1, d.size());
+                std::memcpy(buf, d.data(), k);
+                buf[k] = 0;
+            }
+            return d.size();
+        },
+        size_t(0));
+}
+KFR_API_SPEC void kfr_dft_uneven_delete_plan_f32(KFR_DFT_UNEVEN_F32* plan)
+{
+    try_void([&] { if (plan) delete as<uneven_obj>(plan, TAG_UNEVEN); });
 }
 
 } // extern "C"

@@ -244,7 +244,7 @@ static bool is_codelet(int r)
 }
 
 // Threads per signal needed by a radix sequence at `ept` elements per thread (0 = infeasible).
-static int threads_needed(long long n, const std::vector<int>& radices, int ept)
+int threads_needed(long long n, const std::vector<int>& radices, int ept)
 {
     long long ts = 1;
     for (int r : radices)
@@ -337,13 +337,13 @@ bool block_program<T>::feasible(long long n)
 }
 
 template <typename T>
-void block_program<T>::build(int n_, int kind)
+void block_program<T>::build(int n_, int kind, const std::vector<int>* order, int ept_only)
 {
     n  = n_;
     ct = 0;
     int cts = 0;
     std::vector<int> ctr;
-    if (kind != CT_NONE && ct_lookup<T>(kind, n, cts, ctr))
+    if (!order && kind != CT_NONE && ct_lookup<T>(kind, n, cts, ctr))
     {
         radices = ctr;
         ts      = cts;
@@ -352,12 +352,19 @@ void block_program<T>::build(int n_, int kind)
     }
     else
     {
-        radices = factor_radices(n);
+        radices = order ? *order : factor_radices(n);
         if (radices.empty() || int(radices.size()) > kMaxPasses)
             throw std::invalid_argument("internal: length has no one-CTA radix plan");
+        long long prod = 1;
+        for (int r : radices)
+            prod *= r;
+        if (prod != n)
+            throw std::invalid_argument("internal: radix order does not multiply to the length");
         ept = 0;
         for (int e : { 16, 32 })
         {
+            if (ept_only && e != ept_only)
+                continue;
             const int t = threads_needed(n, radices, e);
             if (t > 0 && t <= max_threads_for(int(sizeof(T)), e))
             {
@@ -683,12 +690,8 @@ void complex_engine<T>::check_device_error() const
 }
 
 template <typename T>
-void complex_engine<T>::init_bluestein(long long n)
+void bluestein_tables(long long n, long long m, dbuf& chirp_out, dbuf& bhat_out)
 {
-    long long m = 1;
-    while (m < 2 * n - 1)
-        m <<= 1;
-    m_ = m;
     // chirp[k] = e^{-i pi k^2 / n} with the phase k^2 mod 2n kept in integers, as the reference does
     // (src/dft/dft-impl.hpp:217-226)
     std::vector<std::complex<T>> chirp(n);
@@ -705,7 +708,7 @@ void complex_engine<T>::init_bluestein(long long n)
         chirp64[k] = twiddle(ph, 2 * n);
         chirp[k]   = std::complex<T>(T(chirp64[k].real()), T(chirp64[k].imag()));
     }
-    chirp_.upload(chirp.data(), chirp.size() * sizeof(std::complex<T>));
+    chirp_out.upload(chirp.data(), chirp.size() * sizeof(std::complex<T>));
     // bhat = conj(FFT_M(b)) / M with b[k] = b[M-k] = chirp[k]: evaluated in double on the host by a plain
     // radix-2 FFT so the table is exact to double rounding before it is stored as T.
     std::vector<std::complex<double>> b(m, { 0.0, 0.0 });
@@ -720,7 +723,20 @@ void complex_engine<T>::init_bluestein(long long n)
     const double inv_m = 1.0 / double(m);
     for (long long k = 0; k < m; k++)
         bh[k] = std::complex<T>(T(b[k].real() * inv_m), T(-b[k].imag() * inv_m));
-    bhat_.upload(bh.data(), bh.size() * sizeof(std::complex<T>));
+    bhat_out.upload(bh.data(), bh.size() * sizeof(std::complex<T>));
+}
+
+template void bluestein_tables<float>(long long, long long, dbuf&, dbuf&);
+template void bluestein_tables<double>(long long, long long, dbuf&, dbuf&);
+
+template <typename T>
+void complex_engine<T>::init_bluestein(long long n)
+{
+    long long m = 1;
+    while (m < 2 * n - 1)
+        m <<= 1;
+    m_ = m;
+    bluestein_tables<T>(n, m, chirp_, bhat_);
     if (block_program<T>::feasible(m))
     {
         k_ = kind::bluestein_smem;

@@ -101,14 +101,22 @@ struct block_program
 
     // False if n cannot run in one CTA (size, registers or a large prime factor).
     static bool feasible(long long n);
-    // `kind` selects the compile-time kernel list to look in (CT_NONE: always the runtime kernel).
-    void build(int n, int kind = CT_NONE);
+    // `kind` selects the compile-time kernel list to look in (CT_NONE: always the runtime kernel).  `order`
+    // forces a runtime radix sequence (product n) and `ept_only` (16 or 32) the register array size.
+    void build(int n, int kind = CT_NONE, const std::vector<int>* order = nullptr, int ept_only = 0);
     // Launch shape for `batch` signals (`spc_cap` bounds the signals per CTA, 0 = no bound).
     block_cfg cfg(long long batch, int spc_cap = 0) const;
     // Launch shape of a four-step tile: exactly `tile` signals per CTA.
     block_cfg cfg_tile(int tile) const;
     std::string describe() const;
 };
+
+// Threads per signal a runtime radix sequence needs at `ept` complex values per thread (0 = infeasible).
+int threads_needed(long long n, const std::vector<int>& radices, int ept);
+// Bluestein tables for length n and convolution length m: chirp[k] = e^{-i pi k^2 / n} (n values) and
+// bhat = conj(DFT_m(b)) / m of the symmetric chirp sequence b (m values).
+template <typename T>
+void bluestein_tables(long long n, long long m, dbuf& chirp, dbuf& bhat);
 
 // Dynamic shared memory a block FFT kernel may use (device limit less the static pass list and a reserve).
 int smem_budget();
