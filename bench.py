@@ -208,6 +208,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
     ap.add_argument("--sizes", type=str, default=None, help="comma-separated subset of the lengths (profiling)")
     ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
     args = ap.parse_args()
@@ -314,6 +315,42 @@ def main():
                "ms_per_step": round(wall / args.steps * 1e3, 3)}
         del hin, hout
 
+    # uneven batch: 8192 signals of log-uniform lengths on [64, 65536] (7-smooth, 10% prime) in one
+    # persistent launch (graph-replayed) against one plain plan execution per signal
+    uneven = None
+    if rank == 0 and not args.no_uneven and not args.sizes:
+        from kfr_gb300.workloads import uneven_lengths
+
+        lengths = uneven_lengths(8192)
+        up = k.dft_plan_uneven(lengths, autotune=True)
+        total = int(sum(lengths))
+        g = torch.Generator(device=dev).manual_seed(4242)
+        ux = torch.complex(torch.rand(total, device=dev, generator=g) * 2 - 1,
+                           torch.rand(total, device=dev, generator=g) * 2 - 1)
+        uy = torch.empty_like(ux)
+
+        def timed(fn, reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        for _ in range(3):
+            up.execute(uy, ux, stream=stream)
+        ms_p = timed(lambda: up.execute(uy, ux, stream=stream), 10)
+        up.execute_per_signal(uy, ux, stream=stream)
+        ms_s = timed(lambda: up.execute_per_signal(uy, ux, stream=stream), 2)
+        ub = 16 * total
+        uneven = {"signals": len(lengths), "elements": total, "persistent_ms": round(ms_p, 4),
+                  "persistent_gbs": round(ub / (ms_p * 1e-3) / 1e9, 1), "per_signal_ms": round(ms_s, 3),
+                  "per_signal_gbs": round(ub / (ms_s * 1e-3) / 1e9, 1), "speedup": round(ms_s / ms_p, 2),
+                  "plan": up.describe()}
+        del ux, uy, up
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, threads, sample = cpu_baseline_run()
@@ -325,7 +362,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded N(0,1) x amplitude, c32",
             "config": config_dict(), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk, "per_size": {str(n): per[n] for n in SIZES},
+            "clocks": clk, "per_size": {str(n): per[n] for n in SIZES}, "uneven": uneven,
             "max_rel_rms": float(f"{max(errs.values()):.3e}"),
         }
         print(json.dumps(line))
