@@ -168,6 +168,111 @@ def cpu_baseline_run(steps_scale: float = 1.0, threads: int | None = None):
     return total_bytes / total_t / 1e9, threads, "1/32 of each batch (8 MiB per length), forward, all host threads"
 
 
+def measure_rows(torch, k, dev, stream, hbm, with_cpu):
+    """The other rows of the DFT path on their own configurations (device-resident inputs, CUDA events,
+    L2 flushed between repetitions where the data would fit in it), each beside the oracle's single-precision
+    port on a bounded sample on all host cores."""
+    from oracle.oracle import Oracle
+
+    orc = Oracle("orc") if with_cpu else None
+    threads = os.cpu_count() or 1
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(fn, reps=5, flush_l2=False):
+        fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(reps):
+            if flush_l2:
+                flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps
+
+    def cpu(fn, nbytes):
+        if orc is None:
+            return None
+        fn()  # warm
+        t0 = time.perf_counter()
+        fn()
+        return round(nbytes / (time.perf_counter() - t0) / 1e9, 3)
+
+    rows = {}
+    g = torch.Generator(device=dev).manual_seed(77)
+    # real DFT f32, N in {1920, 44100, 48000}, 256 MiB of reals each, CCs
+    for n in (1920, 44100, 48000):
+        b = (256 << 20) // (4 * n)
+        plan = k.dft_plan_real(n)
+        x = torch.randn(b, n, device=dev, generator=g)
+        y = torch.empty(b, n // 2 + 1, dtype=torch.complex64, device=dev)
+        ms = timed(lambda: plan.execute_batch(y, x, b, stream=stream))
+        nb = b * (4 * n + 8 * (n // 2 + 1))
+        xs = x[: max(1, b // 64)].cpu().numpy()
+        rows[f"real_dft_{n}"] = {
+            "batch": b, "ms": round(ms, 4), "gbs": round(nb / (ms * 1e-3) / 1e9, 1),
+            "frac": round(nb / (ms * 1e-3) / 1e9 / hbm, 4),
+            "cpu_port_gbs": cpu(lambda: orc.dft_real(xs, precision="f32", threads=threads),
+                                len(xs) * (4 * n + 8 * (n // 2 + 1)))}
+        del x, y, plan
+    # DCT-II of 4096 x 512 (16 MiB: L2 flushed between repetitions)
+    b, n = 4096, 512
+    plan = k.dct_plan(n)
+    x = torch.rand(b, n, device=dev, generator=g) * 2 - 1
+    y = torch.empty_like(x)
+    ms = timed(lambda: plan.execute_batch(y, x, b, stream=stream), flush_l2=True)
+    xs = x[:1024].cpu().numpy()
+    rows["dct2_4096x512"] = {"ms": round(ms, 4), "gbs": round(8 * n * b / (ms * 1e-3) / 1e9, 1),
+                             "frac": round(8 * n * b / (ms * 1e-3) / 1e9 / hbm, 4),
+                             "cpu_port_gbs": cpu(lambda: orc.dct(xs, precision="f32", threads=threads), 8 * n * 1024)}
+    del x, y, plan
+    # convolution filter: 64 signals of 2^20 f32, 1023 taps, block 1024 (each signal from a reset state)
+    chans, L, M = 64, 1 << 20, 1023
+    taps = torch.randn(M, device=dev, generator=g) / M
+    f = k.convolve_filter(taps, 1024, dtype="f32", channels=chans)
+    x = torch.randn(chans, L, device=dev, generator=g)
+    y = torch.empty_like(x)
+
+    def run_filter():
+        f.reset()
+        f.apply(y, x)
+
+    ms = timed(run_filter, reps=3)
+    nb = chans * 8 * L + 4 * M
+    xs = x[0].cpu().numpy()
+    hs = taps.cpu().numpy()
+
+    def cpu_filter():
+        flt = orc.filter(hs, 1024, precision="f32")
+        flt.process(xs)
+
+    rows["convolve_filter_64x2^20_1023taps"] = {
+        "ms": round(ms, 3), "gbs": round(nb / (ms * 1e-3) / 1e9, 1), "frac": round(nb / (ms * 1e-3) / 1e9 / hbm, 4),
+        "cpu_port_gbs": cpu(cpu_filter, 8 * L), "cpu_sample": "one 2^20 signal, one core (streaming filter)"}
+    del x, y, f
+    # large single transforms: c32 2^24 and 30,720,000, c64 2^20
+    for n, dt, name in ((1 << 24, torch.complex64, "c32_2^24"), (30720000, torch.complex64, "c32_30720000"),
+                        (1 << 20, torch.complex128, "c64_2^20")):
+        sfx = "f32" if dt == torch.complex64 else "f64"
+        plan = k.dft_plan(n, sfx)
+        x = torch.randn(n, dtype=dt, device=dev, generator=g)
+        y = torch.empty_like(x)
+        tmp = torch.empty(max(1, plan.temp_size_batch(1)), dtype=torch.uint8, device=dev)
+        ms = timed(lambda: plan.execute_batch(y, x, 1, temp=tmp, stream=stream), flush_l2=n * 16 < (256 << 20))
+        nb = (16 if sfx == "f32" else 32) * n
+        rows[name] = {"ms": round(ms, 4), "gbs": round(nb / (ms * 1e-3) / 1e9, 1),
+                      "frac": round(nb / (ms * 1e-3) / 1e9 / hbm, 4), "plan": plan.describe()}
+        if name == "c32_2^24" and orc is not None:
+            xs = x.cpu().numpy().reshape(1, n)
+            rows[name]["cpu_port_gbs"] = cpu(lambda: orc.dft(xs, precision="f32", threads=threads), nb)
+        del x, y, tmp, plan
+    del flush
+    return rows
+
+
 def run_reference(args):
     rank, world, local = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), 0
     if rank != 0:
@@ -209,6 +314,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch comparison")
+    ap.add_argument("--no-rows", action="store_true", help="skip the real / DCT / filter / large-single rows")
     ap.add_argument("--sizes", type=str, default=None, help="comma-separated subset of the lengths (profiling)")
     ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
     args = ap.parse_args()
@@ -351,6 +457,10 @@ def main():
                   "plan": up.describe()}
         del ux, uy, up
 
+    rows = None
+    if rank == 0 and not args.no_rows and not args.sizes:
+        rows = measure_rows(torch, k, dev, stream, hbm, not args.no_cpu)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, threads, sample = cpu_baseline_run()
@@ -363,6 +473,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded N(0,1) x amplitude, c32",
             "config": config_dict(), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk, "per_size": {str(n): per[n] for n in SIZES}, "uneven": uneven,
+            "rows": rows,
             "max_rel_rms": float(f"{max(errs.values()):.3e}"),
         }
         print(json.dumps(line))

@@ -267,6 +267,15 @@ KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
 
+/* Multi-channel convolution filter (no counterpart in the reference, whose filters are single-channel): the
+ * same filter applied independently to `channels` signals, each with its own state.  kfr_filter_process_*
+ * on such a plan takes channels * size samples, channel-major (channel c at c * size), and runs every block of
+ * every channel in one launch; kfr_filter_reset_* clears every channel's state. */
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_convolution_plan_channels_f32(const kfr_f32* taps, size_t size,
+                                                                           size_t block_size, size_t channels);
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_convolution_plan_channels_f64(const kfr_f64* taps, size_t size,
+                                                                           size_t block_size, size_t channels);
+
 /* Uneven batch (no counterpart in the reference, whose callers loop over one plan per length): `count` complex
  * signals of the given lengths stored back to back, transformed by one persistent work-queue launch (plus
  * regular launches for signals too long for one CTA), replayed as a CUDA graph after the first call with a

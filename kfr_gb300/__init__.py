@@ -91,6 +91,7 @@ for sfx in ("f32", "f64"):
         f"kfr_dft_real_adjoint_inverse_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _P]),
         f"kfr_dct_adjoint_batch_{sfx}": (None, [_P, _S, _P, _P, _P, _B, _P]),
         f"kfr_fir_backward_{sfx}": (None, [_P, _S, _S, _S, _P, _P, _P, _P, _P]),
+        f"kfr_filter_create_convolution_plan_channels_{sfx}": (_P, [_P, _S, _S, _S]),
     })
 for fn in ("convolve", "correlate"):
     for sfx in ("f32", "f64", "c32", "c64"):
@@ -408,19 +409,25 @@ class convolve_filter(_plan):
 
     _prefix = "kfr_filter"
 
-    def __init__(self, taps, block_size: int = 1024, dtype=None):
+    def __init__(self, taps, block_size: int = 1024, dtype=None, channels: int = 1):
         if dtype is None:
             dtype = getattr(taps, "dtype", "f32")
         sfx = _sfx(dtype)
         if isinstance(taps, np.ndarray):
             taps = np.ascontiguousarray(taps, dtype=np.float32 if sfx == "f32" else np.float64)
         self._taps = taps
+        self.channels = channels
         n = taps.numel() if hasattr(taps, "numel") else len(taps)
-        super().__init__(_call(f"kfr_filter_create_convolution_plan_{sfx}", _addr(taps), n, block_size), sfx)
+        if channels == 1:
+            h = _call(f"kfr_filter_create_convolution_plan_{sfx}", _addr(taps), n, block_size)
+        else:
+            h = _call(f"kfr_filter_create_convolution_plan_channels_{sfx}", _addr(taps), n, block_size, channels)
+        super().__init__(h, sfx)
 
     def apply(self, out, inp, size=None):
+        """size: samples per channel (default: all of inp over the plan's channels)."""
         if size is None:
-            size = inp.numel() if hasattr(inp, "numel") else len(inp)
+            size = _numel(inp) // self.channels
         _call(self._fn("process"), self.handle, _addr(out), _addr(inp), size)
 
     def reset(self):
@@ -437,6 +444,8 @@ def _conv_sfx(x):
 
 
 def _numel(x):
+    if isinstance(x, np.ndarray):
+        return x.size
     return x.numel() if hasattr(x, "numel") else len(x)
 
 

@@ -226,7 +226,10 @@ template <typename T>
 struct filter_obj : plan_base
 {
     conv_filter<T> f;
-    filter_obj(const T* taps, size_t ntaps, size_t block) : plan_base(tags<T>::flt), f(taps, ntaps, block) {}
+    filter_obj(const T* taps, size_t ntaps, size_t block, int channels = 1)
+        : plan_base(tags<T>::flt), f(taps, ntaps, block, channels)
+    {
+    }
 };
 
 template <typename Obj>
@@ -550,7 +553,7 @@ void filter_process(void* h, T* out, const T* in, size_t n)
     auto* p = as<filter_obj<T>>(h, tags<T>::flt);
     if (n == 0)
         return;
-    const size_t bytes = n * sizeof(T);
+    const size_t bytes = n * size_t(p->f.channels()) * sizeof(T);
     run(*p, out, bytes, in, bytes, nullptr, 0, nullptr, true,
         [&](void* o, const void* i, void*, cudaStream_t st)
         { p->f.process(static_cast<T*>(o), static_cast<const T*>(i), n, st); });
@@ -1314,6 +1317,32 @@ KFR_API_SPEC size_t kfr_dft_uneven_describe_f32(KFR_DFT_UNEVEN_F32* plan, char* 
 KFR_API_SPEC void kfr_dft_uneven_delete_plan_f32(KFR_DFT_UNEVEN_F32* plan)
 {
     try_void([&] { if (plan) delete as<uneven_obj>(plan, TAG_UNEVEN); });
+}
+
+/* Multi-channel convolution filter (extension) */
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_convolution_plan_channels_f32(const kfr_f32* taps, size_t size,
+                                                                           size_t block_size, size_t channels)
+{
+    return try_fn(
+        [&] {
+            if (channels < 1 || channels > (1u << 16))
+                throw std::invalid_argument("channels must be between 1 and 65536");
+            return reinterpret_cast<KFR_FILTER_F32*>(static_cast<plan_base*>(
+                new filter_obj<float>(taps, size, block_size ? block_size : 1024, int(channels))));
+        },
+        (KFR_FILTER_F32*)nullptr);
+}
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_convolution_plan_channels_f64(const kfr_f64* taps, size_t size,
+                                                                           size_t block_size, size_t channels)
+{
+    return try_fn(
+        [&] {
+            if (channels < 1 || channels > (1u << 16))
+                throw std::invalid_argument("channels must be between 1 and 65536");
+            return reinterpret_cast<KFR_FILTER_F64*>(static_cast<plan_base*>(
+                new filter_obj<double>(taps, size, block_size ? block_size : 1024, int(channels))));
+        },
+        (KFR_FILTER_F64*)nullptr);
 }
 
 } // extern "C"

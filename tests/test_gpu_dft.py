@@ -373,6 +373,31 @@ def test_convolve_filter_streaming_fixtures(sfx):
         assert rel_rms(y, g[f"fout_real_{i}_reset"]) <= 8 * tol(len(taps) + len(x), sfx), i
 
 
+def test_convolve_filter_channels_match_single_channel(orc):
+    """A 6-channel plan (one launch per call) gives each channel exactly what a one-channel plan gives it,
+    across two streaming calls, host and device buffers, and resets every channel's state."""
+    rng = np.random.default_rng(12)
+    taps = rng.standard_normal(255).astype(np.float32)
+    chans, n = 6, 5000
+    x = rng.standard_normal((chans, 2 * n)).astype(np.float32)
+    multi = k.convolve_filter(taps, 512, channels=chans)
+    y = np.empty((chans, n), np.float32)
+    outs = []
+    for part in (0, 1):
+        xp = np.ascontiguousarray(x[:, part * n:(part + 1) * n])
+        multi.apply(y, xp)
+        outs.append(y.copy())
+    got = np.concatenate(outs, axis=1)
+    for c in range(chans):
+        ref = orc.filter(taps.astype(np.float64), 512).process(x[c].astype(np.float64))
+        assert rel_rms(got[c], ref) <= 8 * c32_tolerance(2 * n), c
+    multi.reset()
+    xd = dev(np.ascontiguousarray(x[:, :n]))
+    yd = torch.empty_like(xd)
+    multi.apply(yd, xd)
+    assert np.allclose(yd.cpu().numpy(), outs[0], rtol=0, atol=1e-5)
+
+
 def test_convolve_filter_long_signal_device(orc):
     """1023-tap filter over 2^18 samples in device memory, against the streaming oracle."""
     rng = np.random.default_rng(11)
