@@ -37,9 +37,14 @@
     X(126, 9, 14, 9)                                                                                         \
     X(8190, 1024, 13, 9, 7, 10)
 
-// four-step pass lengths (columns and rows): the factors of 30720 = 160 x 192 and of the power-of-two
-// lengths 2^15 .. 2^24
+// four-step pass lengths (columns and rows): the factors of 30720 = 160 x 192, of the power-of-two lengths
+// 2^15 .. 2^24, of the real-DFT half lengths 22050 = 147 x 150 and 24000 = 150 x 160 (N = 44100, 48000) and
+// of 30,720,000 = 5120 x 6000
 #define KFR_CT_FOURSTEP_F32(X)                                                                              \
+    X(147, 21, 7, 7, 3)                                                                                      \
+    X(150, 15, 10, 15)                                                                                       \
+    X(5120, 512, 16, 16, 4, 5)                                                                               \
+    X(6000, 400, 16, 15, 5, 5)                                                                               \
     X(128, 8, 16, 8)                                                                                         \
     X(160, 16, 16, 10)                                                                                       \
     X(192, 16, 16, 12)                                                                                       \
