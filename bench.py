@@ -49,6 +49,13 @@ NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float] = {
 }
 
 
+def rel_rms(y, ref):
+    """Relative RMS error of y against a reference."""
+    y = np.asarray(y, dtype=np.complex128)
+    ref = np.asarray(ref, dtype=np.complex128)
+    return float(np.sqrt(np.sum(np.abs(y - ref) ** 2) / max(np.sum(np.abs(ref) ** 2), 1e-300)))
+
+
 def batch_for(n: int) -> int:
     return BYTES_PER_SIZE // (8 * n)
 
@@ -269,7 +276,35 @@ def measure_rows(torch, k, dev, stream, hbm, with_cpu):
             xs = x.cpu().numpy().reshape(1, n)
             rows[name]["cpu_port_gbs"] = cpu(lambda: orc.dft(xs, precision="f32", threads=threads), nb)
         del x, y, tmp, plan
-    del flush
+    # tensor-core radix-16 plans beside the FP32 CUDA-core plan: N = 4096, 1 GiB batch, the precision workload
+    # (sum of 64 random sinusoids + 1e-3 noise) for the errors against numpy's FP64 FFT
+    n = 4096
+    b = (1 << 30) // (8 * n)
+    X = torch.randn(b, n, dtype=torch.complex64, device=dev, generator=g)
+    Y = torch.empty_like(X)
+    rs = np.random.default_rng(4096)
+    t = np.arange(n)
+    xs = np.zeros((16, n), np.complex128)
+    for i in range(16):
+        f, am, ph = rs.uniform(0, n, 64), rs.uniform(0, 1, 64), rs.uniform(0, 2 * np.pi, 64)
+        xs[i] = (am[:, None] * np.exp(1j * (2 * np.pi * f[:, None] * t[None, :] / n + ph[:, None]))).sum(0)
+    xs = (xs + 1e-3 * (rs.standard_normal((16, n)) + 1j * rs.standard_normal((16, n)))).astype(np.complex64)
+    ref = np.fft.fft(xs.astype(np.complex128), axis=-1)
+    xd = torch.from_numpy(xs).to(dev)
+    yd = torch.empty_like(xd)
+    tc = {}
+    for name, plan in (("fp32_cuda_cores", k.dft_plan(n)), ("tensor_bf16x2", k.dft_plan_tensor(n, "bf16")),
+                       ("tensor_fp16x2", k.dft_plan_tensor(n, "fp16"))):
+        tmp = torch.empty(max(1, plan.temp_size_batch(b)), dtype=torch.uint8, device=dev)
+        ms = timed(lambda: plan.execute_batch(Y, X, b, temp=tmp, stream=stream))
+        plan.execute_batch(yd, xd, 16)
+        y = yd.cpu().numpy()
+        tc[name] = {"ms": round(ms, 4), "gbs": round(16 * n * b / (ms * 1e-3) / 1e9, 1),
+                    "rel_rms": float(f"{rel_rms(y, ref):.3e}"),
+                    "max_rel": float(f"{np.max(np.abs(y - ref)) / np.max(np.abs(ref)):.3e}")}
+        del tmp
+    rows["tensor_core_c32_4096_1GiB"] = tc
+    del X, Y, flush
     return rows
 
 
@@ -329,7 +364,6 @@ def main():
     import torch
 
     import kfr_gb300 as k
-    from oracle.oracle import Oracle, rel_rms
 
     rank, world, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
@@ -357,12 +391,12 @@ def main():
         step()
     torch.cuda.synchronize()
 
-    # accuracy on a sample of each batch (outside the timed region)
-    orc = Oracle("orc")
+    # accuracy on a sample of each batch (outside the timed region), against numpy's FP64 FFT (same sign and
+    # scaling convention: forward e^{-2 pi i n k / N}, unscaled)
     errs = {}
     for n in SIZES:
         s = min(8, batch_for(n))
-        ref = orc.dft(xs[n][:s].cpu().numpy().astype(np.complex128), threads=os.cpu_count() or 1)
+        ref = np.fft.fft(xs[n][:s].cpu().numpy().astype(np.complex128), axis=-1)
         errs[n] = rel_rms(ys[n][:s].cpu().numpy(), ref)
 
     clocks = ClockSampler(local)

@@ -276,6 +276,13 @@ KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_convolution_plan_channels_f32(con
 KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_convolution_plan_channels_f64(const kfr_f64* taps, size_t size,
                                                                            size_t block_size, size_t channels);
 
+/* Tensor-core plans (no counterpart in the reference): a complex plan whose radix-16 passes run on the tensor
+ * cores as DFT-matrix contractions with each operand split into a high and a low 16-bit part
+ * (split = 1: BF16, 2: FP16), products hi*hi + hi*lo + lo*hi accumulated in FP32.  Lengths 256 and 4096.  The
+ * handle is an ordinary KFR_DFT_PLAN_F32 (execute, batch, describe, delete as usual).  Accuracy is below the
+ * FP32 CUDA-core plans' (the dropped lo*lo term and 16-bit operands); the tests report it against FP64. */
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_plan_tensor_f32(size_t size, int split);
+
 /* Uneven batch (no counterpart in the reference, whose callers loop over one plan per length): `count` complex
  * signals of the given lengths stored back to back, transformed by one persistent work-queue launch (plus
  * regular launches for signals too long for one CTA), replayed as a CUDA graph after the first call with a

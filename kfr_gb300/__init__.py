@@ -113,6 +113,7 @@ _SIGS.update({
     "kfr_autocorrelate_f32": (_S, [_P, _P, _S]),
     "kfr_autocorrelate_f64": (_S, [_P, _P, _S]),
     "kfr_dft_create_uneven_plan_f32": (_P, [_P, _S, _B]),
+    "kfr_dft_create_plan_tensor_f32": (_P, [_S, ctypes.c_int]),
     "kfr_dft_uneven_get_size_f32": (_S, [_P]),
     "kfr_dft_uneven_execute_f32": (None, [_P, _P, _P, _B, _P]),
     "kfr_dft_uneven_execute_per_signal_f32": (None, [_P, _P, _P, _B, _P]),
@@ -260,6 +261,15 @@ class dft_plan(_plan):
 
     def launch_count(self, batch=1):
         return _call("kfr_dft_get_launch_count_f32", self.handle, batch) if self.sfx == "f32" else None
+
+
+class dft_plan_tensor(dft_plan):
+    """Complex c32 plan whose radix-16 passes run on the tensor cores with split hi + lo operands
+    (split: "bf16" or "fp16"); lengths 256 and 4096."""
+
+    def __init__(self, size: int, split="fp16"):
+        mode = {"bf16": 1, "fp16": 2}[split]
+        _plan.__init__(self, _call("kfr_dft_create_plan_tensor_f32", size, mode), "f32")
 
 
 class dft_plan_md(dft_plan):

@@ -141,6 +141,10 @@ struct dft_obj : plan_base
     std::unique_ptr<complex_engine<T>> eng1;
     std::unique_ptr<md_engine<T>> md;
     explicit dft_obj(size_t n_) : plan_base(tags<T>::dft), n(n_), eng1(new complex_engine<T>((long long)n_)) {}
+    dft_obj(size_t n_, int tensor_mode)
+        : plan_base(tags<T>::dft), n(n_), eng1(new complex_engine<T>((long long)n_, tensor_mode))
+    {
+    }
     explicit dft_obj(const std::vector<long long>& shape) : plan_base(tags<T>::dft), n(0)
     {
         if (shape.size() == 1)
@@ -1343,6 +1347,13 @@ KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_convolution_plan_channels_f64(con
                 new filter_obj<double>(taps, size, block_size ? block_size : 1024, int(channels))));
         },
         (KFR_FILTER_F64*)nullptr);
+}
+
+/* Tensor-core plans (extension) */
+KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_plan_tensor_f32(size_t size, int split)
+{
+    return try_fn([&] { return reinterpret_cast<KFR_DFT_PLAN_F32*>(static_cast<plan_base*>(new dft_obj<float>(size, split))); },
+                  (KFR_DFT_PLAN_F32*)nullptr);
 }
 
 } // extern "C"

@@ -1,5 +1,6 @@
 // Host-side planner and executors (see plan.hpp).
 #include "plan.hpp"
+#include "tensor.hpp"
 
 #include "ct_table.hpp"
 
@@ -495,6 +496,28 @@ static double fft_cost(long long n)
 }
 
 template <typename T>
+complex_engine<T>::complex_engine(long long n, int tensor_mode) : n_(n)
+{
+    if (sizeof(T) != 4 || (tensor_mode != TC_BF16 && tensor_mode != TC_FP16))
+        throw std::invalid_argument("tensor-core plans are single precision with a BF16 or FP16 split");
+    if (n != 256 && n != 4096)
+        throw std::invalid_argument("tensor-core plans support lengths 256 and 4096 (radix-16 passes only)");
+    const std::vector<int> order(n == 256 ? 2 : 3, 16);
+    prog_.build(int(n), CT_NONE, &order, 16);
+    std::vector<float> cs(512);
+    for (int k = 0; k < 16; k++)
+        for (int r = 0; r < 16; r++)
+        {
+            const auto w       = twiddle(k * r, 16); // e^{-2 pi i k r / 16} = cos - i sin
+            cs[k * 16 + r]       = float(w.real());
+            cs[256 + k * 16 + r] = float(-w.imag());
+        }
+    tc_cs_.upload(cs.data(), cs.size() * sizeof(float));
+    tc_mode_ = tensor_mode;
+    k_       = kind::tensor;
+}
+
+template <typename T>
 complex_engine<T>::complex_engine(long long n) : n_(n)
 {
     if (n <= 1)
@@ -881,6 +904,7 @@ int complex_engine<T>::launches(long long batch) const
     case kind::fourstep: return 2 * int((batch + 65534) / 65535);
     case kind::bluestein_multi: return 3 + 2 * inner_->launches(batch);
     case kind::rader_smem: return (rader_spc_ && (batch - 1) / rader_spc_ > 0) ? 2 : 1;
+    case kind::tensor: return 1;
     }
     return 0;
 }
@@ -894,6 +918,20 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
     const size_t esz = 2 * sizeof(T);
     switch (k_)
     {
+    case kind::tensor:
+    {
+        c2c_args a{};
+        a.in      = in;
+        a.out     = out;
+        a.batch   = batch;
+        a.istride = istride;
+        a.ostride = ostride;
+        a.inverse = inverse;
+        a.tw      = prog_.tw.get();
+        check(launch_c2c_tc_f32(a, int(n_), tc_mode_, static_cast<const float*>(tc_cs_.get()), st),
+              "launch tensor-core DFT");
+        return;
+    }
     case kind::trivial:
     {
         if (n_ == 1 && out != in)
@@ -1100,6 +1138,10 @@ std::string complex_engine<T>::describe() const
     switch (k_)
     {
     case kind::trivial: s << "trivial n=" << n_; break;
+    case kind::tensor:
+        s << "tensor-core n=" << n_ << " radix-16 passes as mma.sync contractions, "
+          << (tc_mode_ == TC_BF16 ? "BF16" : "FP16") << " hi+lo operands, FP32 accumulation";
+        break;
     case kind::smem: s << "smem " << prog_.describe(); break;
     case kind::bluestein_smem: s << "bluestein_smem n=" << n_ << " m=" << m_ << " [" << prog_.describe() << "]"; break;
     case kind::fourstep:

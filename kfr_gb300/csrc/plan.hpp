@@ -136,10 +136,14 @@ public:
         bluestein_smem,
         fourstep,
         bluestein_multi,
-        rader_smem
+        rader_smem,
+        tensor
     };
 
     explicit complex_engine(long long n);
+    // Tensor-core form (single precision, n = 256 or 4096): every radix-16 pass as a contraction on the tensor
+    // cores with operands split into two 16-bit parts (mode: TC_BF16 or TC_FP16, tensor.hpp).
+    complex_engine(long long n, int tensor_mode);
 
     // Device scratch (in complex elements) that execute() needs for `batch` signals.
     long long scratch_elems(long long batch) const;
@@ -180,6 +184,9 @@ private:
     void init_rader(long long n);
     bool plan_fourstep(long long n);
     void plan_pipe();
+    // tensor-core form
+    int tc_mode_ = 0;
+    dbuf tc_cs_;
     // Rader
     dbuf pin_, qof_, gp_;
     int rader_spc_ = 0; // signals per tile of the pipelined kernel, 0 = not used
