@@ -287,11 +287,46 @@ __device__ __forceinline__ void dft16(cpx<T>* v)
         dft4(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
 }
 
-// Register holding output r of codelet R (identity except for the transposed radix-16 codelet).
+// 3-point DFT in place: X1,2 = a - (b + c)/2 -/+ i (sqrt(3)/2)(b - c).
+template <typename T>
+__device__ __forceinline__ void dft3(cpx<T>& a, cpx<T>& b, cpx<T>& c)
+{
+    const T h      = T(0.86602540378443864676372317075294);
+    const cpx<T> t = b + c;
+    const cpx<T> d = b - c;
+    const cpx<T> m = mk(a.x - T(0.5) * t.x, a.y - T(0.5) * t.y);
+    a              = a + t;
+    b              = mk(m.x + h * d.y, m.y - h * d.x);
+    c              = mk(m.x - h * d.y, m.y + h * d.x);
+}
+
+// 9 = 3 x 3: DFT3 down each column, twiddles W9^{n1 k2}, DFT3 along each row, so X[k2 + 3 k1] ends up in
+// v[3 k2 + k1] (a transposed order; see codelet_out).  About two thirds of the arithmetic of the direct
+// symmetric form.
+template <typename T>
+__device__ __forceinline__ void dft9(cpx<T>* v)
+{
+    const T c1 = T(0.76604444311897803520239265055542), s1 = T(0.64278760968653932632264340990726); // 2pi/9
+    const T c2 = T(0.17364817766693034885171662676931), s2 = T(0.98480775301220805936674302458952); // 4pi/9
+    const T c4 = T(-0.93969262078590838405410927732473), s4 = T(0.34202014332566873304409961468226); // 8pi/9
+#pragma unroll
+    for (int n1 = 0; n1 < 3; n1++)
+        dft3(v[n1], v[n1 + 3], v[n1 + 6]);
+    // y[n1][k2] lives in v[n1 + 3 k2]
+    v[4] = v[4] * mk(c1, -s1); // n1 = 1, k2 = 1: W9^1
+    v[7] = v[7] * mk(c2, -s2); // n1 = 1, k2 = 2: W9^2
+    v[5] = v[5] * mk(c2, -s2); // n1 = 2, k2 = 1: W9^2
+    v[8] = v[8] * mk(c4, -s4); // n1 = 2, k2 = 2: W9^4
+#pragma unroll
+    for (int k2 = 0; k2 < 3; k2++)
+        dft3(v[3 * k2], v[3 * k2 + 1], v[3 * k2 + 2]);
+}
+
+// Register holding output r of codelet R (identity except for the transposed radix-16 and radix-9 codelets).
 template <int R>
 __device__ __forceinline__ constexpr int codelet_out(int r)
 {
-    return R == 16 ? (r & 3) * 4 + (r >> 2) : r;
+    return R == 16 ? (r & 3) * 4 + (r >> 2) : R == 9 ? (r % 3) * 3 + r / 3 : r;
 }
 
 template <typename T, int R>
@@ -354,6 +389,8 @@ __device__ __forceinline__ void dft_codelet(cpx<T>* v)
         dft8(v);
     else if constexpr (R == 16)
         dft16(v);
+    else if constexpr (R == 9)
+        dft9(v);
     else if constexpr (R == 6)
         dft_pfa<T, 2, 3>(v);
     else if constexpr (R == 10)
