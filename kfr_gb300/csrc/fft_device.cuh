@@ -675,207 +675,6 @@ __device__ __forceinline__ void ct_block_fft(cpx<T>* buf, const cpx<T>* __restri
     ct_passes<T, N, TS, EPT, 1, 0, Rs...>(v, buf, tw, lta);
 }
 
-// Compile-time block FFT whose first pass reads an unpadded source (a TMA-filled stage buffer) and whose
-// last pass writes straight to global memory (stride-one across threads, so the stores coalesce); the
-// passes in between work in the padded buffer `work`.  `cj` conjugates on read and on write (inverse).
-// Ends with a barrier, after which `src` and `work` may be reused.
-template <typename T, int N, int TS, int EPT, int R>
-__device__ __forceinline__ void ct_pass_first(cpx<T> (&v)[EPT], const cpx<T>* src, cpx<T>* work, const bool cj,
-                                              const int lt)
-{
-    constexpr int NBF = N / R;
-    constexpr int NB  = (NBF + TS - 1) / TS;
-#pragma unroll
-    for (int b = 0; b < NB; b++)
-    {
-        const int j = lt + b * TS;
-        if (j < NBF)
-        {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                v[b * R + r] = conj_if(src[j + r * NBF], cj);
-            dft_codelet<T, R>(&v[b * R]);
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                work[pidx_s<ct_ps<T>(N, TS)>(j * R + r)] = v[b * R + codelet_out<R>(r)];
-        }
-    }
-    __syncthreads();
-}
-
-template <typename T, int N, int TS, int EPT, int R, int NS, int TWOFF>
-__device__ __forceinline__ void ct_pass_last(cpx<T> (&v)[EPT], const cpx<T>* work, cpx<T>* gout,
-                                             const cpx<T>* __restrict__ tw, const bool cj, const int lt)
-{
-    static_assert(NS * R == N, "last pass");
-    constexpr int NBF = N / R;
-    constexpr int NB  = (NBF + TS - 1) / TS;
-#pragma unroll
-    for (int b = 0; b < NB; b++)
-    {
-        const int j = lt + b * TS;
-        if (j < NBF)
-        {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                v[b * R + r] = work[pidx_s<ct_ps<T>(N, TS)>(j + r * NBF)];
-            const cpx<T>* t = tw + TWOFF + j;
-#pragma unroll
-            for (int r = 1; r < R; r++)
-                v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * NS);
-            dft_codelet<T, R>(&v[b * R]);
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                gout[j + r * NS] = conj_if(v[b * R + codelet_out<R>(r)], cj);
-        }
-    }
-    __syncthreads();
-}
-
-template <typename T, int N, int TS, int EPT, int R>
-__device__ __forceinline__ void ct_pass_only(cpx<T> (&v)[EPT], const cpx<T>* src, cpx<T>* gout, const bool cj,
-                                             const int lt)
-{
-    constexpr int NB = (1 + TS - 1) / TS;
-    static_assert(N == R, "single pass");
-#pragma unroll
-    for (int b = 0; b < NB; b++)
-    {
-        const int j = lt + b * TS;
-        if (j < 1)
-        {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                v[b * R + r] = conj_if(src[r], cj);
-            dft_codelet<T, R>(&v[b * R]);
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                gout[r] = conj_if(v[b * R + codelet_out<R>(r)], cj);
-        }
-    }
-    __syncthreads();
-}
-
-template <typename T, int N, int TS, int EPT, int NS, int TWOFF, int R, int... Rest>
-__device__ __forceinline__ void ct_passes_io(cpx<T> (&v)[EPT], const cpx<T>* src, cpx<T>* work, cpx<T>* gout,
-                                             const cpx<T>* __restrict__ tw, const bool cj, const int lt)
-{
-    if constexpr (NS == 1 && sizeof...(Rest) == 0)
-        ct_pass_only<T, N, TS, EPT, R>(v, src, gout, cj, lt);
-    else if constexpr (NS == 1)
-    {
-        ct_pass_first<T, N, TS, EPT, R>(v, src, work, cj, lt);
-        ct_passes_io<T, N, TS, EPT, R, TWOFF, Rest...>(v, src, work, gout, tw, cj, lt);
-    }
-    else if constexpr (sizeof...(Rest) == 0)
-        ct_pass_last<T, N, TS, EPT, R, NS, TWOFF>(v, work, gout, tw, cj, lt);
-    else
-    {
-        ct_pass<T, N, TS, EPT, R, NS, TWOFF>(v, work, tw, lt);
-        ct_passes_io<T, N, TS, EPT, NS * R, TWOFF + NS * (R - 1), Rest...>(v, src, work, gout, tw, cj, lt);
-    }
-}
-
-template <typename T, int N, int TS, int... Rs>
-__device__ __forceinline__ void ct_block_fft_io(const cpx<T>* src, cpx<T>* work, cpx<T>* gout,
-                                                const cpx<T>* __restrict__ tw, const bool cj, const int lt)
-{
-    constexpr int EPT = ct_ept<N, TS, Rs...>();
-    const int lta     = lt < TS ? lt : N;
-    cpx<T> v[EPT];
-    ct_passes_io<T, N, TS, EPT, 1, 0, Rs...>(v, src, work, gout, tw, cj, lta);
-}
-
-// Compile-time block FFT with caller-supplied access to the transform's input and output: ld(p) fetches
-// input p of the first pass, st(q, x) stores output q of the last pass, and the passes in between work in
-// the padded buffer `work`.  hook() runs once, after the first pass's closing barrier (the input has been
-// consumed by then).  SEP_IN: ld reads memory that the first pass does not write; SEP_OUT: st writes
-// memory that the last pass does not read; each saves the barrier between that pass's loads and stores.
-// Ends with a barrier.
-template <typename T, int N, int TS, int EPT, int R, int NS, int TWOFF, bool SYNC_MID, class LD, class ST>
-__device__ __forceinline__ void ct_pass_fx(cpx<T> (&v)[EPT], const LD& ld, const ST& st,
-                                           const cpx<T>* __restrict__ tw, const int lt)
-{
-    constexpr int NBF = N / R;
-    constexpr int NB  = (NBF + TS - 1) / TS;
-    static_assert(NB * R <= EPT, "register array too small");
-#pragma unroll
-    for (int b = 0; b < NB; b++)
-    {
-        const int j = lt + b * TS;
-        if (j < NBF)
-        {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                v[b * R + r] = ld(j + r * NBF);
-            if constexpr (NS > 1)
-            {
-                const int k     = j % NS;
-                const cpx<T>* t = tw + TWOFF + k;
-#pragma unroll
-                for (int r = 1; r < R; r++)
-                    v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * NS);
-            }
-            dft_codelet<T, R>(&v[b * R]);
-        }
-    }
-    if constexpr (SYNC_MID)
-        __syncthreads();
-#pragma unroll
-    for (int b = 0; b < NB; b++)
-    {
-        const int j = lt + b * TS;
-        if (j < NBF)
-        {
-            const int k = NS > 1 ? j % NS : 0;
-            const int d = (j - k) * R + k;
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                st(d + r * NS, v[b * R + codelet_out<R>(r)]);
-        }
-    }
-    __syncthreads();
-}
-
-template <typename T, int N, int TS, int EPT, int NS, int TWOFF, bool SEP_IN, bool SEP_OUT, class LD, class ST,
-          class H, int R, int... Rest>
-__device__ __forceinline__ void ct_chain_fx(cpx<T> (&v)[EPT], const LD& ld, const ST& st, const H& hook,
-                                            cpx<T>* work, const cpx<T>* __restrict__ tw, const int lt)
-{
-    constexpr int TWNEXT = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
-    const auto wld       = [work](int p) { return work[pidx_s<ct_ps<T>(N, TS)>(p)]; };
-    const auto wst       = [work](int q, cpx<T> x) { work[pidx_s<ct_ps<T>(N, TS)>(q)] = x; };
-    if constexpr (NS == 1 && sizeof...(Rest) == 0)
-    {
-        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, !(SEP_IN || SEP_OUT)>(v, ld, st, tw, lt);
-        hook();
-    }
-    else if constexpr (NS == 1)
-    {
-        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, !SEP_IN>(v, ld, wst, tw, lt);
-        hook();
-        ct_chain_fx<T, N, TS, EPT, R, TWNEXT, false, SEP_OUT, decltype(wld), ST, H, Rest...>(v, wld, st, hook, work,
-                                                                                            tw, lt);
-    }
-    else if constexpr (sizeof...(Rest) == 0)
-        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, !SEP_OUT>(v, ld, st, tw, lt);
-    else
-    {
-        ct_pass_fx<T, N, TS, EPT, R, NS, TWOFF, true>(v, ld, wst, tw, lt);
-        ct_chain_fx<T, N, TS, EPT, NS * R, TWNEXT, false, SEP_OUT, LD, ST, H, Rest...>(v, ld, st, hook, work, tw, lt);
-    }
-}
-
-template <typename T, int N, int TS, bool SEP_IN, bool SEP_OUT, int... Rs, class LD, class ST, class H>
-__device__ __forceinline__ void ct_block_fft_fx(const LD& ld, const ST& st, const H& hook, cpx<T>* work,
-                                                const cpx<T>* __restrict__ tw, const int lt)
-{
-    constexpr int EPT = ct_ept<N, TS, Rs...>();
-    const int lta     = lt < TS ? lt : N;
-    cpx<T> v[EPT];
-    ct_chain_fx<T, N, TS, EPT, 1, 0, SEP_IN, SEP_OUT, LD, ST, H, Rs...>(v, ld, st, hook, work, tw, lta);
-}
-
 // Ping-pong compile-time block FFT: pass i reads buffer A (i even) or B (i odd) and writes the other, so a
 // pass needs one barrier and each butterfly's outputs are stored as soon as they are computed (no register
 // array spans the pass).  ld(p) fetches input p of the first pass, st(q, x) stores output q of the last

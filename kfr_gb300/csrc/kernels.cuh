@@ -60,23 +60,12 @@ struct ct_fft
     {
         ct_block_fft<T, N, TS, Rs...>(buf, tw, lt);
     }
-    __device__ __forceinline__ void run_io(const cpx<T>* src, cpx<T>* work, cpx<T>* gout, const cpx<T>* __restrict__ tw,
-                                           bool cj, int lt) const
-    {
-        ct_block_fft_io<T, N, TS, Rs...>(src, work, gout, tw, cj, lt);
-    }
     static constexpr int npass = sizeof...(Rs);
     template <class LD, class ST, class H, class P>
     __device__ __forceinline__ void run_pp(const LD& ld, const ST& st, const H& hook, const P& pre_last, cpx<T>* A,
                                            cpx<T>* B, const cpx<T>* __restrict__ tw, int lt) const
     {
         ct_block_fft_pp<T, N, TS, Rs...>(ld, st, hook, pre_last, A, B, tw, lt);
-    }
-    template <bool SEP_IN, bool SEP_OUT, class LD, class ST, class H>
-    __device__ __forceinline__ void run_fx(const LD& ld, const ST& st, const H& hook, cpx<T>* work,
-                                           const cpx<T>* __restrict__ tw, int lt) const
-    {
-        ct_block_fft_fx<T, N, TS, SEP_IN, SEP_OUT, Rs...>(ld, st, hook, work, tw, lt);
     }
 };
 
