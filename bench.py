@@ -276,6 +276,21 @@ def measure_rows(torch, k, dev, stream, hbm, with_cpu):
             xs = x.cpu().numpy().reshape(1, n)
             rows[name]["cpu_port_gbs"] = cpu(lambda: orc.dft(xs, precision="f32", threads=threads), nb)
         del x, y, tmp, plan
+    # power-of-two lengths 2^10 .. 2^24, 1 GiB batches (the north-star's range for the 70% target)
+    pw = {}
+    for e in (10, 12, 14, 16, 18, 20, 22, 24):
+        n = 1 << e
+        b = (1 << 30) // (8 * n)
+        plan = k.dft_plan(n)
+        x = torch.randn(b, n, dtype=torch.complex64, device=dev, generator=g)
+        y = torch.empty_like(x)
+        tmp = torch.empty(max(1, plan.temp_size_batch(b)), dtype=torch.uint8, device=dev)
+        ms = timed(lambda: plan.execute_batch(y, x, b, temp=tmp, stream=stream), reps=3)
+        gbs = 16 * n * b / (ms * 1e-3) / 1e9
+        pw[f"2^{e}"] = {"batch": b, "ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / hbm, 4),
+                        "plan": plan.describe()[:60]}
+        del x, y, tmp, plan
+    rows["pow2_c32_1GiB"] = pw
     # tensor-core radix-16 plans beside the FP32 CUDA-core plan: N = 4096, 1 GiB batch, the precision workload
     # (sum of 64 random sinusoids + 1e-3 noise) for the errors against numpy's FP64 FFT
     n = 4096
