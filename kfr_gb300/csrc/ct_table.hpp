@@ -73,6 +73,16 @@
     X(2048, 128, 16, 16, 8)                                                                                  \
     X(4096, 256, 16, 16, 16)
 
+// four-step splits whose two passes run as fully compile-time kernels (both lengths, the tiles and the
+// twiddle table split fold to constants): X(n1, n2), each a KFR_CT_FOURSTEP length
+#define KFR_CT_FSPAIR_F32(X)                                                                                \
+    X(160, 192)                                                                                              \
+    X(256, 256)                                                                                              \
+    X(512, 512)                                                                                              \
+    X(1024, 1024)                                                                                            \
+    X(147, 150)                                                                                              \
+    X(150, 160)
+
 // Shared-memory layout of a compile-time length (single precision): X(N, TS, pad shift, extra group stride).
 // Element i of a signal sits at i + (i >> shift) (shift 0: unpadded), signals of a CTA lie `stride` elements
 // apart, stride = N + (N >> shift) + 1 + extra.  The default (shift 4, extra 0) suits power-of-two strides;
@@ -109,4 +119,21 @@ KFR_CT_HD constexpr int ct_group_stride_f32(int n, int ts)
 #undef KFR_CT_LAYOUT_STRIDE
     return n + (n >> 4) + 1;
 }
+} // namespace kfr_gpu
+
+namespace kfr_gpu
+{
+// Tile (signals per CTA) of a compile-time four-step pass run ping-pong: the largest power of two <= 16 whose
+// threads fit 1024 and whose two buffers fit `smem` bytes; 0 if fewer than 8 fit (the strided passes then
+// take the in-place kernels).
+KFR_CT_HD constexpr int fsp_tile(int n, int ts, int smem)
+{
+    int s = 16;
+    while (s > 1 && (s * ts > 1024 || 2 * s * ct_group_stride_f32(n, ts) * 8 > smem))
+        s /= 2;
+    return s >= 8 ? s : 0;
+}
+// Shared memory the compile-time pair kernels are built for (the sm_103a per-block opt-in maximum less the
+// static reserve).
+constexpr int kFspSmem = 227 * 1024 - 2048;
 } // namespace kfr_gpu

@@ -871,6 +871,100 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_fs_rows(const fourstep_ar
 }
 
 // ---------------------------------------------------------------------------------------------------
+// Four-step passes with both lengths, the tile and the twiddle split known at compile time (KFR_CT_FSPAIR):
+// the same work as the ping-pong branches of k_fs_cols / k_fs_rows with every index folded to constants.
+// ---------------------------------------------------------------------------------------------------
+template <int N>
+__host__ __device__ constexpr int lbits_for()
+{
+    int lb = 0;
+    while ((1LL << (2 * lb)) < (long long)N)
+        lb++;
+    return lb;
+}
+
+template <typename T, class FA, int N2>
+__global__ void __launch_bounds__(1024, 1) k_fsp_cols(const fourstep_args a)
+{
+    constexpr int N1 = FA::n, GA = FA::gstride(), TS = FA::ts;
+    constexpr int S  = fsp_tile(N1, TS, kFspSmem), SH = S == 16 ? 4 : 3;
+    constexpr long long N = (long long)N1 * N2;
+    constexpr int LB      = lbits_for<N1 * N2>();
+    static_assert(S >= 8, "pair kernels need a tile of at least 8");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T>* sm      = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int c0    = blockIdx.x * S;
+    const cpx<T>* __restrict__ x = reinterpret_cast<const cpx<T>*>(a.in) + blockIdx.y * N;
+    cpx<T>* __restrict__ y       = reinterpret_cast<cpx<T>*>(a.out) + blockIdx.y * N;
+    const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
+    copy_batched<8>(
+        S * N1,
+        [&](int i)
+        {
+            const int c = i & (S - 1);
+            return (N2 % S == 0 || c0 + c < N2) ? x[(i >> SH) * N2 + c0 + c] : mk<T>(0, 0);
+        },
+        [&](int i, cpx<T> v) { sm[(i & (S - 1)) * GA + FA::pi(i >> SH)] = conj_if(v, cin); });
+    __syncthreads();
+    const int g  = int(threadIdx.x) / TS;
+    const int lt = g < S ? int(threadIdx.x) - g * TS : TS;
+    const int gg = g < S ? g : 0;
+    const int col = c0 + gg;
+    const cpx<T>* twA  = reinterpret_cast<const cpx<T>*>(a.twA);
+    const cpx<T>* twB  = reinterpret_cast<const cpx<T>*>(a.twB);
+    const auto nothing = []() {};
+    const FA fa(nullptr, a.d, TS);
+    fa.run_pp([&](int p) { return sm[gg * GA + FA::pi(p)]; },
+              [&](int k1, cpx<T> v)
+              {
+                  if (N2 % S == 0 || col < N2)
+                      y[col * N1 + k1] = conj_if(v * twiddle_2level(twA, twB, (long long)(col * k1), LB), cout);
+              },
+              nothing, nothing, sm + gg * GA, sm + (S + gg) * GA, reinterpret_cast<const cpx<T>*>(a.tw), lt);
+}
+
+template <typename T, class FB, int N1>
+__global__ void __launch_bounds__(1024, 1) k_fsp_rows(const fourstep_args a)
+{
+    constexpr int N2 = FB::n, GB = FB::gstride(), TS = FB::ts;
+    constexpr int S  = fsp_tile(N2, TS, kFspSmem), SH = S == 16 ? 4 : 3;
+    constexpr long long N = (long long)N1 * N2;
+    static_assert(S >= 8, "pair kernels need a tile of at least 8");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T>* sm      = reinterpret_cast<cpx<T>*>(smem_raw);
+    const int r0    = blockIdx.x * S;
+    const cpx<T>* __restrict__ y = reinterpret_cast<const cpx<T>*>(a.in) + blockIdx.y * N;
+    cpx<T>* __restrict__ X       = reinterpret_cast<cpx<T>*>(a.out) + blockIdx.y * N;
+    const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
+    copy_batched<8>(
+        S * N2,
+        [&](int i)
+        {
+            const int r = i & (S - 1);
+            return (N1 % S == 0 || r0 + r < N1) ? y[(i >> SH) * N1 + r0 + r] : mk<T>(0, 0);
+        },
+        [&](int i, cpx<T> v) { sm[(i & (S - 1)) * GB + FB::pi(i >> SH)] = conj_if(v, cin); });
+    __syncthreads();
+    const int g  = int(threadIdx.x) / TS;
+    const int lt = g < S ? int(threadIdx.x) - g * TS : TS;
+    const int gg = g < S ? g : 0;
+    cpx<T>* B          = sm + S * GB;
+    cpx<T>* stg        = FB::npass % 2 == 0 ? sm : B;
+    const auto nothing = []() {};
+    const FB fb(nullptr, a.d, TS);
+    fb.run_pp([&](int p) { return sm[gg * GB + FB::pi(p)]; },
+              [&](int k2, cpx<T> v) { stg[k2 * S + (gg ^ (k2 & (S - 1)))] = v; }, nothing, nothing, sm + gg * GB,
+              B + gg * GB, reinterpret_cast<const cpx<T>*>(a.tw), lt);
+#pragma unroll 4
+    for (int i = threadIdx.x; i < S * N2; i += blockDim.x)
+    {
+        const int k2 = i >> SH, r = i & (S - 1);
+        if (N1 % S == 0 || r0 + r < N1)
+            X[(r0 + r) + N1 * k2] = conj_if(stg[k2 * S + (r ^ (k2 & (S - 1)))], cout);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
 // Launchers.  A block_cfg with ct != 0 selects the compile-time kernel of that length (single precision,
 // launched by the launch_ct_* functions of kernels_ct_*.cu); otherwise cfg.ept picks the runtime kernel.
 // ---------------------------------------------------------------------------------------------------

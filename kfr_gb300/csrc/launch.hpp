@@ -194,6 +194,11 @@ cudaError_t launch_ct_c2r_f32(const real_args& a, const block_cfg& c, cudaStream
 cudaError_t launch_ct_dct2_f32(const dct_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_dct3_f32(const dct_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_fs_cols_f32(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
+// Compile-time pair kernels (KFR_CT_FSPAIR_F32): the column pass (cols = true) or the row pass of the split
+// a.n1 x a.n2 over a.batch signals (contiguous, a.batch <= 65535).  False / cudaErrorInvalidValue if the pair
+// has no kernel.
+bool has_ct_fsp_f32(int n1, int n2);
+cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st);
 cudaError_t launch_ct_fs_rows_f32(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
 
 // Largest thread count a block FFT kernel may be launched with (elem_bytes = sizeof(real type)).

@@ -840,8 +840,19 @@ bool complex_engine<T>::plan_fourstep(long long n)
     tile_r_ = tile_for(prows_);
     // compile-time passes run ping-pong (two buffers per signal) unless that would shrink a tile below 8
     // signals (short row segments coalesce poorly)
-    pp_c_ = pp_r_ = false;
-    if (pcols_.ct)
+    pp_c_ = pp_r_ = pair_ = false;
+    if (sizeof(T) == 4 && pcols_.ct && prows_.ct && has_ct_fsp_f32(int(n1_), int(n2_)) &&
+        fsp_tile(int(n1_), pcols_.ts, kFspSmem) >= 8 && fsp_tile(int(n2_), prows_.ts, kFspSmem) >= 8 &&
+        2 * fsp_tile(int(n1_), pcols_.ts, kFspSmem) * pcols_.gstride * int(2 * sizeof(T)) <= max_smem_bytes() &&
+        2 * fsp_tile(int(n2_), prows_.ts, kFspSmem) * prows_.gstride * int(2 * sizeof(T)) <= max_smem_bytes())
+    {
+        // both passes fully compile time (their tiles fixed by the kernels)
+        pair_   = true;
+        pp_c_   = pp_r_ = true;
+        tile_c_ = fsp_tile(int(n1_), pcols_.ts, kFspSmem);
+        tile_r_ = fsp_tile(int(n2_), prows_.ts, kFspSmem);
+    }
+    if (pcols_.ct && !pair_)
     {
         const int t2 = tile_for(pcols_, 2);
         if (t2 >= 8 || t2 == tile_c_)
@@ -850,7 +861,7 @@ bool complex_engine<T>::plan_fourstep(long long n)
             pp_c_   = true;
         }
     }
-    if (prows_.ct)
+    if (prows_.ct && !pair_)
     {
         const int t2 = tile_for(prows_, 2);
         if (t2 >= 8 || t2 == tile_r_)
@@ -1069,11 +1080,16 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             a.d        = pcols_.desc;
             a.div_n    = make_fast_div(uint32_t(n1_));
             a.pingpong   = pp_c_;
-            block_cfg cc = pcols_.cfg_tile(tile_c_);
-            if (pp_c_)
-                cc.smem *= 2; // ping-pong buffers
-            cc.grid      = (n2_ + tile_c_ - 1) / tile_c_;
-            check(launch_fs_cols<T>(a, cc, st), "launch four-step columns");
+            if (pair_)
+                check(launch_ct_fsp_f32(a, true, st), "launch four-step columns");
+            else
+            {
+                block_cfg cc = pcols_.cfg_tile(tile_c_);
+                if (pp_c_)
+                    cc.smem *= 2; // ping-pong buffers
+                cc.grid = (n2_ + tile_c_ - 1) / tile_c_;
+                check(launch_fs_cols<T>(a, cc, st), "launch four-step columns");
+            }
             // row pass: scratch -> out
             a.in       = scr;
             a.out      = outb;
@@ -1085,11 +1101,16 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             a.d        = prows_.desc;
             a.div_n    = make_fast_div(uint32_t(n2_));
             a.pingpong   = pp_r_;
-            block_cfg cr = prows_.cfg_tile(tile_r_);
-            if (pp_r_)
-                cr.smem *= 2;
-            cr.grid      = (n1_ + tile_r_ - 1) / tile_r_;
-            check(launch_fs_rows<T>(a, cr, st), "launch four-step rows");
+            if (pair_)
+                check(launch_ct_fsp_f32(a, false, st), "launch four-step rows");
+            else
+            {
+                block_cfg cr = prows_.cfg_tile(tile_r_);
+                if (pp_r_)
+                    cr.smem *= 2;
+                cr.grid = (n1_ + tile_r_ - 1) / tile_r_;
+                check(launch_fs_rows<T>(a, cr, st), "launch four-step rows");
+            }
         }
         return;
     }
@@ -1145,8 +1166,9 @@ std::string complex_engine<T>::describe() const
     case kind::smem: s << "smem " << prog_.describe(); break;
     case kind::bluestein_smem: s << "bluestein_smem n=" << n_ << " m=" << m_ << " [" << prog_.describe() << "]"; break;
     case kind::fourstep:
-        s << "fourstep n=" << n_ << " = " << n1_ << " x " << n2_ << " cols[" << pcols_.describe() << " tile=" << tile_c_
-          << "] rows[" << prows_.describe() << " tile=" << tile_r_ << "]";
+        s << "fourstep" << (pair_ ? " (compile-time pair)" : "") << " n=" << n_ << " = " << n1_ << " x " << n2_
+          << " cols[" << pcols_.describe() << " tile=" << tile_c_ << "] rows[" << prows_.describe()
+          << " tile=" << tile_r_ << "]";
         break;
     case kind::bluestein_multi: s << "bluestein_multi n=" << n_ << " m=" << m_ << " inner{" << inner_->describe() << "}"; break;
     case kind::rader_smem:

@@ -174,6 +174,7 @@ private:
     block_program<T> pcols_, prows_;
     int tile_c_ = 1, tile_r_ = 1;
     bool pp_c_ = false, pp_r_ = false; // ping-pong column / row passes
+    bool pair_ = false;                 // both passes as fully compile-time pair kernels
     dbuf twA_, twB_;
     int lbits_ = 0;
     // pipelined smem path (compile-time lengths): signals per tile, 0 = not used
