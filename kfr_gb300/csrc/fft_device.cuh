@@ -698,10 +698,16 @@ __device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>
             const int k = NS > 1 ? j % NS : 0;
             if constexpr (NS > 1)
             {
-                const cpx<T>* t = tw + TWOFF + k;
+                // W^{k r} from the one table value W^k by a binary powering tree, w_r = w_{r/2} w_{r - r/2}
+                // (at most ceil(log2 r) products deep): one load per butterfly instead of R - 1
+                cpx<T> w[R];
+                w[1] = ldg(tw + TWOFF + k);
+#pragma unroll
+                for (int r = 2; r < R; r++)
+                    w[r] = w[r / 2] * w[r - r / 2];
 #pragma unroll
                 for (int r = 1; r < R; r++)
-                    v[r] = v[r] * ldg(t + (r - 1) * NS);
+                    v[r] = v[r] * w[r];
             }
             dft_codelet<T, R>(v);
             const int d = (j - k) * R + k;
