@@ -699,15 +699,19 @@ __device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>
             if constexpr (NS > 1)
             {
                 // W^{k r} from the one table value W^k by a binary powering tree, w_r = w_{r/2} w_{r - r/2}
-                // (at most ceil(log2 r) products deep): one load per butterfly instead of R - 1
-                cpx<T> w[R];
+                // (at most ceil(log2 r) products deep): one load per butterfly instead of R - 1.  Both
+                // factors have index <= R/2 for every r < R, so only those powers stay live.
+                cpx<T> w[R / 2 + 1];
                 w[1] = ldg(tw + TWOFF + k);
+                v[1] = v[1] * w[1];
 #pragma unroll
                 for (int r = 2; r < R; r++)
-                    w[r] = w[r / 2] * w[r - r / 2];
-#pragma unroll
-                for (int r = 1; r < R; r++)
-                    v[r] = v[r] * w[r];
+                {
+                    const cpx<T> wr = w[r / 2] * w[r - r / 2];
+                    if (r <= R / 2)
+                        w[r] = wr;
+                    v[r] = v[r] * wr;
+                }
             }
             dft_codelet<T, R>(v);
             const int d = (j - k) * R + k;
