@@ -680,6 +680,25 @@ __device__ __forceinline__ void ct_block_fft(cpx<T>* buf, const cpx<T>* __restri
 // array spans the pass).  ld(p) fetches input p of the first pass, st(q, x) stores output q of the last
 // pass (which writes A when the number of passes is even, else B); the passes in between use the padded
 // layouts of A and B.  hook() runs once, after the first pass's closing barrier.  Ends with a barrier.
+// v[r] *= W^{k r} from the one table value w1 = W^k by a binary powering tree, w_r = w_{r/2} w_{r - r/2}
+// (at most ceil(log2 r) products deep): one load per butterfly instead of R - 1.  Both factors have index
+// <= R/2 for every r < R, so only those powers stay live.
+template <typename T, int R>
+__device__ __forceinline__ void twiddle_powers(cpx<T> (&v)[R], const cpx<T> w1)
+{
+    cpx<T> w[R / 2 + 1];
+    w[1] = w1;
+    v[1] = v[1] * w1;
+#pragma unroll
+    for (int r = 2; r < R; r++)
+    {
+        const cpx<T> wr = w[r / 2] * w[r - r / 2];
+        if (r <= R / 2)
+            w[r] = wr;
+        v[r] = v[r] * wr;
+    }
+}
+
 template <typename T, int N, int TS, int R, int NS, int TWOFF, class LD, class ST>
 __device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>* __restrict__ tw, const int lt)
 {
@@ -697,22 +716,7 @@ __device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>
                 v[r] = ld(j + r * NBF);
             const int k = NS > 1 ? j % NS : 0;
             if constexpr (NS > 1)
-            {
-                // W^{k r} from the one table value W^k by a binary powering tree, w_r = w_{r/2} w_{r - r/2}
-                // (at most ceil(log2 r) products deep): one load per butterfly instead of R - 1.  Both
-                // factors have index <= R/2 for every r < R, so only those powers stay live.
-                cpx<T> w[R / 2 + 1];
-                w[1] = ldg(tw + TWOFF + k);
-                v[1] = v[1] * w[1];
-#pragma unroll
-                for (int r = 2; r < R; r++)
-                {
-                    const cpx<T> wr = w[r / 2] * w[r - r / 2];
-                    if (r <= R / 2)
-                        w[r] = wr;
-                    v[r] = v[r] * wr;
-                }
-            }
+                twiddle_powers<T, R>(v, ldg(tw + TWOFF + k));
             dft_codelet<T, R>(v);
             const int d = (j - k) * R + k;
 #pragma unroll
@@ -756,6 +760,114 @@ __device__ __forceinline__ void ct_block_fft_pp(const LD& ld, const ST& st, cons
 {
     const int lta = lt < TS ? lt : N;
     pp_chain<T, N, TS, 1, 0, 0, LD, ST, H, P, Rs...>(ld, st, hook, pre_last, A, B, tw, lta);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Cyclic convolution core of Rader's algorithm in 2K - 1 ping-pong passes (K radices R_1..R_K):
+//   forward L-point DFT, pointwise map, forward L-point DFT.
+// With Stockham passes, butterfly j of the first transform's last pass (radix R_K, stride L / R_K) produces
+// its outputs j + r L / R_K, which are exactly the inputs of butterfly j of a first pass of radix R_K of the
+// second transform.  So the second transform runs its radices in reverse order (R_K, ..., R_1, twiddles in
+// tw2) and its first pass is done in registers, inside the first transform's last pass:
+//   v = DFT_RK(twiddled inputs);  z[r] = mid(q = j + r L / R_K, v[r]);  DFT_RK(z) -> outputs j R_K + r.
+// ld(p) fetches input p of the first pass, mid(q, x) maps output q of the first transform to input q of the
+// second, st(q, x) stores output q of the second transform.  Pass i (i = 0 .. 2K - 2) writes B (i even)
+// or A (i odd); the last pass (even) reads A.  hook() runs after the first pass.  Ends with a barrier.
+// ---------------------------------------------------------------------------------------------------
+template <int... Rs>
+struct radix_seq
+{
+    // the second transform's passes after its first (radices R_{K-1}, ..., R_1 starting at stride R_K)
+    template <typename T, int N, int TS, int NS, int I, class LD, class ST>
+    static __device__ __forceinline__ void tail(const LD& ld, const ST& st, cpx<T>* A, cpx<T>* B,
+                                                const cpx<T>* __restrict__ tw, const int lt)
+    {
+        const auto nothing = []() {};
+        pp_chain<T, N, TS, NS, 0, I, LD, ST, decltype(nothing), decltype(nothing), Rs...>(ld, st, nothing, nothing,
+                                                                                           A, B, tw, lt);
+    }
+};
+
+// radix_seq of R_{K-1}, ..., R_1 for the list R_1, ..., R_K (all but the last, reversed)
+template <class Acc, int... Rs>
+struct rev_init;
+template <int... A, int R>
+struct rev_init<radix_seq<A...>, R>
+{
+    using type = radix_seq<A...>;
+};
+template <int... A, int R, int R2, int... Rs>
+struct rev_init<radix_seq<A...>, R, R2, Rs...>
+{
+    using type = typename rev_init<radix_seq<R, A...>, R2, Rs...>::type;
+};
+
+template <typename T, int N, int TS, int R, int NS, int TWOFF, class LD, class MID, class ST>
+__device__ __forceinline__ void pp_pass_fused(const LD& ld, const MID& mid, const ST& st,
+                                              const cpx<T>* __restrict__ tw, const int lt)
+{
+    static_assert(NS * R == N && NS > 1, "the fused pass is the last pass of a chain of two or more");
+    constexpr int NBF = N / R;
+    constexpr int NB  = (NBF + TS - 1) / TS;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+            cpx<T> v[R];
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[r] = ld(j + r * NBF);
+            twiddle_powers<T, R>(v, ldg(tw + TWOFF + j));
+            dft_codelet<T, R>(v);
+            cpx<T> z[R];
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                z[r] = mid(j + r * NS, v[codelet_out<R>(r)]);
+            dft_codelet<T, R>(z);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                st(j * R + r, z[codelet_out<R>(r)]);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int N, int TS, int NS, int TWOFF, int I, class Tail, class LD, class MID, class ST, class H,
+          int R, int... Rest>
+__device__ __forceinline__ void pp_conv_chain(const LD& ld, const MID& mid, const ST& st, const H& hook, cpx<T>* A,
+                                              cpx<T>* B, const cpx<T>* __restrict__ tw,
+                                              const cpx<T>* __restrict__ tw2, const int lt)
+{
+    cpx<T>* dst     = (I % 2 == 0) ? B : A;
+    const auto d_st = [dst](int q, cpx<T> x) { dst[pidx_s<ct_ps<T>(N, TS)>(q)] = x; };
+    const auto d_ld = [dst](int p) { return dst[pidx_s<ct_ps<T>(N, TS)>(p)]; };
+    if constexpr (sizeof...(Rest) == 0)
+    {
+        pp_pass_fused<T, N, TS, R, NS, TWOFF>(ld, mid, d_st, tw, lt);
+        Tail::template tail<T, N, TS, R, I + 1>(d_ld, st, A, B, tw2, lt);
+    }
+    else
+    {
+        constexpr int TN = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
+        pp_pass<T, N, TS, R, NS, TWOFF>(ld, d_st, tw, lt);
+        if constexpr (NS == 1)
+            hook();
+        pp_conv_chain<T, N, TS, NS * R, TN, I + 1, Tail, decltype(d_ld), MID, ST, H, Rest...>(d_ld, mid, st, hook, A,
+                                                                                               B, tw, tw2, lt);
+    }
+}
+
+template <typename T, int N, int TS, int... Rs, class LD, class MID, class ST, class H>
+__device__ __forceinline__ void ct_conv_pp(const LD& ld, const MID& mid, const ST& st, const H& hook, cpx<T>* A,
+                                           cpx<T>* B, const cpx<T>* __restrict__ tw,
+                                           const cpx<T>* __restrict__ tw2, const int lt)
+{
+    static_assert(sizeof...(Rs) >= 2, "two or more passes");
+    const int lta = lt < TS ? lt : N;
+    using Tail    = typename rev_init<radix_seq<>, Rs...>::type;
+    pp_conv_chain<T, N, TS, 1, 0, 0, Tail, LD, MID, ST, H, Rs...>(ld, mid, st, hook, A, B, tw, tw2, lta);
 }
 
 // Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a

@@ -68,6 +68,7 @@ struct rader_args
     const int* gp;    // gp[p] = g^p (mod n), p = 0..L-1 (pipelined kernel)
     const void* bhat; // L values: DFT_L(b) / L
     const void* tw;
+    const void* tw2;  // tiled kernel: twiddles of the radices in reverse order
     fast_div div_n, div_l;
     fft_desc d;
 };

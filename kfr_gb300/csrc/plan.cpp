@@ -383,16 +383,25 @@ void block_program<T>::build(int n_, int kind, const std::vector<int>* order, in
     std::memset(&desc, 0, sizeof(desc));
     desc.n     = n;
     desc.npass = int(radices.size());
+    const auto table = pass_twiddles<T>(radices, desc.pass);
+    tw.upload(table.data(), table.size() * sizeof(std::complex<T>));
+}
+
+template <typename T>
+std::vector<std::complex<T>> pass_twiddles(const std::vector<int>& radices, pass_desc* passes)
+{
     std::vector<std::complex<T>> table;
     long long ns = 1;
     for (size_t i = 0; i < radices.size(); i++)
     {
-        const int R     = radices[i];
-        pass_desc& p    = desc.pass[i];
-        p.radix         = R;
-        p.ns            = int(ns);
-        p.div_ns        = make_fast_div(uint32_t(ns));
-        p.tw_off        = int(table.size());
+        const int R = radices[i];
+        if (passes)
+        {
+            passes[i].radix  = R;
+            passes[i].ns     = int(ns);
+            passes[i].div_ns = make_fast_div(uint32_t(ns));
+            passes[i].tw_off = int(table.size());
+        }
         const long long L = ns * R;
         if (ns > 1)
             for (int r = 1; r < R; r++)
@@ -401,7 +410,8 @@ void block_program<T>::build(int n_, int kind, const std::vector<int>* order, in
                     const auto w = twiddle(k * r, L);
                     table.emplace_back(T(w.real()), T(w.imag()));
                 }
-        p.wr_off = int(table.size());
+        if (passes)
+            passes[i].wr_off = int(table.size());
         if (!is_codelet(R))
             for (int m = 0; m < R; m++)
             {
@@ -412,7 +422,7 @@ void block_program<T>::build(int n_, int kind, const std::vector<int>* order, in
     }
     if (table.empty())
         table.emplace_back(T(1), T(0));
-    tw.upload(table.data(), table.size() * sizeof(std::complex<T>));
+    return table;
 }
 
 template <typename T>
@@ -631,6 +641,13 @@ void complex_engine<T>::init_rader(long long n)
     }
     bhat_.upload(bh.data(), bh.size() * sizeof(std::complex<T>));
     prog_.build(int(L), CT_RADER);
+    if (prog_.ct)
+    {
+        // the tiled kernel's second DFT runs the radices in reverse order
+        const std::vector<int> rev(prog_.radices.rbegin(), prog_.radices.rend());
+        const auto t2 = pass_twiddles<T>(rev, nullptr);
+        rtw2_.upload(t2.data(), t2.size() * sizeof(std::complex<T>));
+    }
     k_ = kind::rader_smem;
     // Signals per tile of the pipelined kernel: one signal when it takes half a CTA's threads or more,
     // otherwise as many as leave room for two CTAs per SM (each holding two stage tiles and a work tile).
@@ -652,10 +669,10 @@ void complex_engine<T>::init_rader(long long n)
 template <typename T>
 int complex_engine<T>::rader_tile_smem(int spc) const
 {
-    // two stage tiles, the padded work tile, x[0] and A[0] per signal, two mbarriers
+    // three rotating tile buffers, x[0] and A[0] per signal, three mbarriers
     const int esz   = int(2 * sizeof(T));
     const int stage = pipe_stage_len(spc, int(n_), prog_.gstride);
-    return (2 * stage + spc * prog_.gstride + 2 * spc) * esz + 16;
+    return (3 * stage + 2 * spc) * esz + 24;
 }
 
 template <typename T>
@@ -1023,6 +1040,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.gp      = static_cast<const int*>(gp_.get());
         a.bhat    = bhat_.get();
         a.tw      = prog_.tw.get();
+        a.tw2     = rtw2_.get();
         a.div_n   = make_fast_div(uint32_t(n_));
         a.div_l   = make_fast_div(uint32_t(n_ - 1));
         a.d       = prog_.desc;

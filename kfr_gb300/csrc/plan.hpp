@@ -113,6 +113,10 @@ struct block_program
 
 // Threads per signal a runtime radix sequence needs at `ept` complex values per thread (0 = infeasible).
 int threads_needed(long long n, const std::vector<int>& radices, int ept);
+// twiddle table of a radix order (ns * (R - 1) values W_{ns R}^{k r} per pass with ns > 1, then R roots for a
+// radix without a codelet); fills the passes' offsets when passes is not null
+template <typename T>
+std::vector<std::complex<T>> pass_twiddles(const std::vector<int>& radices, pass_desc* passes);
 // Bluestein tables for length n and convolution length m: chirp[k] = e^{-i pi k^2 / n} (n values) and
 // bhat = conj(DFT_m(b)) / m of the symmetric chirp sequence b (m values).
 template <typename T>
@@ -189,7 +193,7 @@ private:
     int tc_mode_ = 0;
     dbuf tc_cs_;
     // Rader
-    dbuf pin_, qof_, gp_;
+    dbuf pin_, qof_, gp_, rtw2_;
     int rader_spc_ = 0; // signals per tile of the pipelined kernel, 0 = not used
     int rader_tile_smem(int spc) const;
 };
