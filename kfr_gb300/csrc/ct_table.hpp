@@ -35,7 +35,7 @@
 // Good-Thomas composite codelets
 #define KFR_CT_RADER_F32(X)                                                                                 \
     X(126, 9, 14, 9)                                                                                         \
-    X(8190, 1024, 13, 9, 7, 10)
+    X(8190, 1024, 13, 9, 14, 5)
 
 // four-step pass lengths (columns and rows): the factors of 30720 = 160 x 192, of the power-of-two lengths
 // 2^15 .. 2^24, of the real-DFT half lengths 22050 = 147 x 150 and 24000 = 150 x 160 (N = 44100, 48000) and
