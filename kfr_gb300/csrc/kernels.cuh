@@ -972,6 +972,170 @@ __global__ void __launch_bounds__(1024, 1) k_fsp_rows(const fourstep_args a)
 }
 
 // ---------------------------------------------------------------------------------------------------
+// Four-step pair kernels, persistent, with 2-D tensor copies (TMA).  Same transforms as k_fsp_cols /
+// k_fsp_rows for two-pass lengths of at most 256 on tiles of 16 columns (rows): a tile is one box of 16
+// contiguous 8-byte elements (128 bytes) per row, loaded with the 128-byte swizzle (conflict-free column
+// reads), double buffered: the next tile streams in while the CTA transforms the current one.  The column
+// pass stores straight from its last pass (times the four-step twiddle); the row pass stages its output in
+// the swizzled box and stores it with one tensor copy.  Waits are bounded; one that runs out sets *err and
+// the CTA returns.
+//   in map (columns): x viewed as (2 N2 floats) x (N1 * batch) rows, box (32 floats, N1)
+//   in / out maps (rows): y and X viewed as (2 N1 floats) x (N2 * batch) rows, box (32 floats, N2)
+// ---------------------------------------------------------------------------------------------------
+template <class F>
+__host__ __device__ constexpr bool fspt_ok()
+{
+    return F::npass == 2 && F::n <= 256 && fsp_tile(F::n, F::ts, kFspSmem) == 16;
+}
+
+// shared memory of a TMA pair kernel of length N: two 1024-byte-aligned boxes of 16 x N, the second
+// ping-pong buffer, two mbarriers and the alignment slack
+template <class F>
+__host__ __device__ constexpr int fspt_smem()
+{
+    return 2 * ((16 * F::n * 8 + 1023) / 1024 * 1024) + 16 * F::gstride() * 8 + 16 + 1024;
+}
+
+template <typename T, class FA, int N2>
+__global__ void __launch_bounds__(16 * FA::ts, 3)
+    k_fspt_cols(const fourstep_args a, const __grid_constant__ tensor_map tm_in, const long long ntiles, int* err)
+{
+    static_assert(fspt_ok<FA>(), "two-pass length of at most 256 on 16-column tiles");
+    constexpr int N1 = FA::n, GA = FA::gstride(), TS = FA::ts, S = 16;
+    constexpr int NTC = (N2 + S - 1) / S;
+    constexpr int SE  = (S * N1 * 8 + 1023) / 1024 * 128; // box elements, rounded to 1024 bytes
+    constexpr int LB  = lbits_for<N1 * N2>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T>* st0    = reinterpret_cast<cpx<T>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    cpx<T>* B      = st0 + 2 * SE;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(B + S * GA);
+    const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
+    const int g    = int(threadIdx.x) / TS;
+    const int lt   = int(threadIdx.x) - g * TS;
+    const cpx<T>* twA  = reinterpret_cast<const cpx<T>*>(a.twA);
+    const cpx<T>* twB  = reinterpret_cast<const cpx<T>*>(a.twB);
+    const cpx<T>* tw   = reinterpret_cast<const cpx<T>*>(a.tw);
+    const auto nothing = []() {};
+    const FA fa(nullptr, a.d, TS);
+    constexpr uint32_t bytes = S * N1 * 8;
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles)
+    {
+        mbar_arrive_expect_tx(&bars[0], bytes);
+        tensor_g2s_2d(st0, &tm_in, int(t % NTC) * 2 * S, int(t / NTC) * N1, &bars[0]);
+    }
+    for (int it = 0; t < ntiles; t += gridDim.x, it++)
+    {
+        const int s    = it & 1;
+        cpx<T>* stage  = st0 + s * SE;
+        const bool got = mbar_wait(&bars[s], (it >> 1) & 1);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+                atomicExch(err, 1); // no other copy is in flight: the next one is issued after this wait
+            return;
+        }
+        const long long tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < ntiles)
+        {
+            // the other stage was last read by the previous tile's first pass, which ended in a barrier
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bars[s ^ 1], bytes);
+            tensor_g2s_2d(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTC) * 2 * S, int(tn / NTC) * N1, &bars[s ^ 1]);
+        }
+        const long long b = t / NTC;
+        const int col     = int(t % NTC) * S + g;
+        cpx<T>* y         = reinterpret_cast<cpx<T>*>(a.out) + b * (long long)N1 * N2;
+        fa.run_pp([&](int p) { return conj_if(stage[swz128_8b(p, g)], cin); },
+                  [&](int k1, cpx<T> v)
+                  {
+                      if (N2 % S == 0 || col < N2)
+                          y[col * N1 + k1] = conj_if(v * twiddle_2level(twA, twB, (long long)(col * k1), LB), cout);
+                  },
+                  nothing, nothing, stage, B + g * GA, tw, lt);
+    }
+}
+
+template <typename T, class FB, int N1>
+__global__ void __launch_bounds__(16 * FB::ts, 3)
+    k_fspt_rows(const fourstep_args a, const __grid_constant__ tensor_map tm_in,
+                const __grid_constant__ tensor_map tm_out, const long long ntiles, int* err)
+{
+    static_assert(fspt_ok<FB>(), "two-pass length of at most 256 on 16-row tiles");
+    constexpr int N2 = FB::n, GB = FB::gstride(), TS = FB::ts, S = 16;
+    constexpr int NTR = (N1 + S - 1) / S;
+    constexpr int SE  = (S * N2 * 8 + 1023) / 1024 * 128;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T>* st0    = reinterpret_cast<cpx<T>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    cpx<T>* B      = st0 + 2 * SE;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(B + S * GB);
+    const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
+    const int g    = int(threadIdx.x) / TS;
+    const int lt   = int(threadIdx.x) - g * TS;
+    const cpx<T>* tw   = reinterpret_cast<const cpx<T>*>(a.tw);
+    const auto nothing = []() {};
+    const FB fb(nullptr, a.d, TS);
+    constexpr uint32_t bytes = S * N2 * 8;
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles)
+    {
+        mbar_arrive_expect_tx(&bars[0], bytes);
+        tensor_g2s_2d(st0, &tm_in, int(t % NTR) * 2 * S, int(t / NTR) * N2, &bars[0]);
+    }
+    for (int it = 0; t < ntiles; t += gridDim.x, it++)
+    {
+        const int s    = it & 1;
+        cpx<T>* stage  = st0 + s * SE;
+        const bool got = mbar_wait(&bars[s], (it >> 1) & 1);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicExch(err, 1);
+                bulk_wait_all();
+            }
+            return;
+        }
+        const long long tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < ntiles)
+        {
+            // the other stage holds the previous tile's output: wait until its store has read it
+            bulk_wait_read();
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bars[s ^ 1], bytes);
+            tensor_g2s_2d(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTR) * 2 * S, int(tn / NTR) * N2, &bars[s ^ 1]);
+        }
+        // pass 1 reads the box, pass 2 writes the transformed rows back into it (same swizzled layout)
+        fb.run_pp([&](int p) { return conj_if(stage[swz128_8b(p, g)], cin); },
+                  [&](int k2, cpx<T> v) { stage[swz128_8b(k2, g)] = conj_if(v, cout); }, nothing, nothing, stage,
+                  B + g * GB, tw, lt);
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            tensor_s2g_2d(&tm_out, int(t % NTR) * 2 * S, int(t / NTR) * N2, stage);
+            bulk_commit();
+        }
+    }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------------------------------
 // Launchers.  A block_cfg with ct != 0 selects the compile-time kernel of that length (single precision,
 // launched by the launch_ct_* functions of kernels_ct_*.cu); otherwise cfg.ept picks the runtime kernel.
 // ---------------------------------------------------------------------------------------------------

@@ -1,4 +1,9 @@
 // Compile-time specialised single-precision kernels: four-step column and row passes (ct_table.hpp).
+#include <algorithm>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "kernels.cuh"
 
 namespace kfr_gpu
@@ -65,6 +70,96 @@ static cudaError_t go_fsp(K kernel, dim3 grid, int threads, int smem, cudaStream
     return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled, looked up once from the driver through the runtime (no link-time dependency)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+static_assert(sizeof(tensor_map) == sizeof(CUtensorMap) && alignof(tensor_map) == alignof(CUtensorMap),
+              "tensor_map mirrors CUtensorMap");
+
+// 2-D map over `rows` rows of `row_elems` complex single-precision values (as 2 row_elems floats), box of
+// 16 values x box_rows rows, 128-byte swizzle, zero fill out of range.  False when the base address or the
+// row pitch is not a multiple of 16 bytes, or the encoder refuses.
+static bool map_rows(tensor_map& m, const void* base, long long row_elems, long long rows, int box_rows)
+{
+    const auto fn = tensor_encoder();
+    if (!fn || reinterpret_cast<uintptr_t>(base) % 16 || (row_elems * 8) % 16 || box_rows > 256 || rows < 1)
+        return false;
+    const cuuint64_t dims[2]    = { cuuint64_t(2 * row_elems), cuuint64_t(rows) };
+    const cuuint64_t strides[1] = { cuuint64_t(row_elems * 8) };
+    const cuuint32_t box[2]     = { 32, cuuint32_t(box_rows) };
+    const cuuint32_t estr[2]    = { 1, 1 };
+    return fn(reinterpret_cast<CUtensorMap*>(&m), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims,
+              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <class K, class... Args>
+static cudaError_t go_fspt(K kernel, int threads, int smem, long long ntiles, cudaStream_t st, Args... args)
+{
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0, dev = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem)) != cudaSuccess)
+        return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    const long long grid = std::min<long long>(ntiles, (long long)per_sm * sms);
+    kernel<<<unsigned(grid), threads, smem, st>>>(args...);
+    return cudaGetLastError();
+}
+
+// The persistent tensor-copy pair kernels where the length and the buffers allow them; done = false
+// otherwise (the caller then launches k_fsp_cols / k_fsp_rows).
+template <class FA, int N2>
+static cudaError_t try_fspt_cols(const fourstep_args& a, cudaStream_t st, bool& done)
+{
+    done = false;
+    if constexpr (fspt_ok<FA>())
+    {
+        constexpr int N1 = FA::n;
+        tensor_map m;
+        if (!a.err || a.sig_stride != (long long)N1 * N2 || !map_rows(m, a.in, N2, N1 * a.batch, N1))
+            return cudaSuccess;
+        done = true;
+        return go_fspt(k_fspt_cols<float, FA, N2>, 16 * FA::ts, fspt_smem<FA>(), a.batch * ((N2 + 15) / 16), st, a,
+                       m, a.batch * ((N2 + 15) / 16), a.err);
+    }
+    return cudaSuccess;
+}
+
+template <class FB, int N1>
+static cudaError_t try_fspt_rows(const fourstep_args& a, cudaStream_t st, bool& done)
+{
+    done = false;
+    if constexpr (fspt_ok<FB>())
+    {
+        constexpr int N2 = FB::n;
+        tensor_map mi, mo;
+        if (!a.err || a.sig_stride != (long long)N1 * N2 || !map_rows(mi, a.in, N1, N2 * a.batch, N2) ||
+            !map_rows(mo, a.out, N1, N2 * a.batch, N2))
+            return cudaSuccess;
+        done = true;
+        return go_fspt(k_fspt_rows<float, FB, N1>, 16 * FB::ts, fspt_smem<FB>(), a.batch * ((N1 + 15) / 16), st, a,
+                       mi, mo, a.batch * ((N1 + 15) / 16), a.err);
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st)
 {
 #define KFR_GPU_FSP_CASE(A, B)                                                                             \
@@ -72,6 +167,10 @@ cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st
     {                                                                                                      \
         using FA = fs_len<A>::type;                                                                        \
         using FB = fs_len<B>::type;                                                                        \
+        bool done = false;                                                                                 \
+        const cudaError_t te = cols ? try_fspt_cols<FA, B>(a, st, done) : try_fspt_rows<FB, A>(a, st, done);   \
+        if (done || te != cudaSuccess)                                                                     \
+            return te;                                                                                     \
         if (cols)                                                                                          \
         {                                                                                                  \
             constexpr int S = fsp_tile(A, FA::ts, kFspSmem);                                               \

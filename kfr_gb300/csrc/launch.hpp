@@ -124,6 +124,7 @@ struct fourstep_args
     int same_layout; // cols pass: store back to x's own layout (multi-dimensional axes) and skip the twiddle
     int pingpong;    // compile-time kernels: ping-pong passes over two buffers per signal (2x shared memory)
     fast_div div_n;  // divides by the FFT length of this pass
+    int* err;        // persistent pair kernels: set when a wait for a tile copy runs out (may be null)
 };
 
 template <typename T>

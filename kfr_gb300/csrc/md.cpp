@@ -54,6 +54,7 @@ void md_axes<T>::run(void* data, long long batch, bool inverse, cudaStream_t st)
             const long long nb = std::min<long long>(65535, sigs - b0);
             char* base         = static_cast<char*>(data) + b0 * ax.n * ax.inner * 2 * sizeof(T);
             fourstep_args a;
+            a.err         = nullptr;
             a.in          = base;
             a.out         = base;
             a.batch       = nb;

@@ -868,6 +868,8 @@ bool complex_engine<T>::plan_fourstep(long long n)
         pp_c_   = pp_r_ = true;
         tile_c_ = fsp_tile(int(n1_), pcols_.ts, kFspSmem);
         tile_r_ = fsp_tile(int(n2_), prows_.ts, kFspSmem);
+        err_.alloc(sizeof(int)); // the persistent tensor-copy pair kernels report a copy that never lands
+        check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
     }
     if (pcols_.ct && !pair_)
     {
@@ -1079,6 +1081,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             char* outb          = static_cast<char*>(out) + b0 * n_ * esz;
             char* scr           = static_cast<char*>(scratch) + b0 * n_ * esz;
             fourstep_args a;
+            a.err        = pair_ ? static_cast<int*>(err_.get()) : nullptr;
             a.batch      = nb;
             a.sig_stride = n_;
             a.n1         = int(n1_);

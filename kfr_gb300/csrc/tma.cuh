@@ -60,6 +60,38 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
                  : "memory");
 }
 
+// Opaque 128-byte tensor map (the driver's CUtensorMap layout), passed to kernels as a __grid_constant__
+// parameter.
+struct alignas(128) tensor_map
+{
+    unsigned long long opaque[16];
+};
+
+// Global -> shared tiled copy of the 2-D box at element coordinates (x, y) of the tensor map, completing on
+// `bar`.  x * element size must be a multiple of 16 bytes; out-of-range elements read as zero.
+__device__ __forceinline__ void tensor_g2s_2d(void* dst_smem, const tensor_map* tm, int x, int y, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                 "[%4];" ::"r"(smem_u32(dst_smem)),
+                 "l"(tm), "r"(x), "r"(y), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Shared -> global tiled copy of a 2-D box in this thread's bulk async-group (x, y >= 0; x * element size a
+// multiple of 16 bytes).  The writes to the source must be ordered before it by fence_proxy_async_smem() and
+// a barrier.
+__device__ __forceinline__ void tensor_s2g_2d(const tensor_map* tm, int x, int y, const void* src_smem)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(tm), "r"(x),
+                 "r"(y), "r"(smem_u32(src_smem))
+                 : "memory");
+}
+
+// Element (row, col) of a box whose rows are 128 bytes of 8-byte elements (16 per row), as laid out in shared
+// memory by the 128-byte swizzle: 16-byte chunk c / 2 of row `row` lands at chunk (c / 2) ^ (row % 8).  The
+// box must start on a 1024-byte boundary.
+__device__ __forceinline__ int swz128_8b(int row, int col) { return row * 16 + (col ^ ((row & 7) << 1)); }
+
 // Shared -> global bulk copy in this thread's bulk async-group (bytes and both addresses multiples of 16).
 // The writes to the source must be ordered before it by fence_proxy_async_smem() and a barrier.
 __device__ __forceinline__ void bulk_s2g(void* dst_gmem, const void* src_smem, uint32_t bytes)

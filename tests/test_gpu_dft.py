@@ -128,6 +128,36 @@ def test_rader_tiles_many_per_cta(orc, n, batch):
     assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
 
 
+@pytest.mark.parametrize("n,batch", [(30720, 300), (24000, 200), (65536, 150)])
+def test_fourstep_pair_tiles_many_per_cta(orc, n, batch):
+    """Four-step lengths whose column and row passes run as persistent kernels fed by 2-D tensor copies
+    (160 x 192, 150 x 160, 256 x 256): several tiles per CTA, ragged row tiles (150 rows in tiles of 16),
+    forward, inverse, in place, and from an 8-byte-misaligned pointer (which takes the per-tile kernels)."""
+    rng = np.random.default_rng(n + batch)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    pick = np.r_[0:2, batch // 2, batch - 2:batch]
+    ref = orc.dft(x[pick].astype(np.complex128), threads=8)
+    refi = orc.dft(x[pick].astype(np.complex128), inverse=True, threads=8)
+    plan = k.dft_plan(n, "f32")
+    assert "compile-time pair" in plan.describe()
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    plan.execute_batch(yd, xd, batch)
+    assert rel_rms(yd.cpu().numpy()[pick], ref) <= tol(n, "f32")
+    full = yd.clone()
+    plan.execute_batch(yd, xd, batch, inverse=True)
+    assert rel_rms(yd.cpu().numpy()[pick], refi) <= tol(n, "f32")
+    zd = xd.clone()
+    plan.execute_batch(zd, zd, batch)
+    assert torch.equal(zd, full)
+    buf = torch.empty(batch * n + 1, dtype=torch.complex64, device="cuda")
+    buf[1:].copy_(xd.reshape(-1))
+    out = torch.empty_like(buf)
+    plan.execute_batch(out[1:], buf[1:], batch)
+    got = out[1:].reshape(batch, n).cpu().numpy()
+    assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
+
+
 @pytest.mark.parametrize("n,batch", [(1000, 5000), (8191, 700), (4096, 1100)])
 def test_host_buffers_pipelined_match_device(n, batch):
     """Host input and output (the reference's calling convention) split into chunks that overlap copies with
