@@ -14,6 +14,7 @@
 #include "ct_table.hpp"
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "fft_desc.hpp"
@@ -699,8 +700,19 @@ __device__ __forceinline__ void twiddle_powers(cpx<T> (&v)[R], const cpx<T> w1)
     }
 }
 
-template <typename T, int N, int TS, int R, int NS, int TWOFF, class LD, class ST>
-__device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>* __restrict__ tw, const int lt)
+// no-op post(j, o): the last pass stores its outputs as computed
+struct no_post
+{
+    template <class V>
+    __device__ __forceinline__ void operator()(int, V&) const
+    {
+    }
+};
+
+// post(j, o) sees butterfly j's outputs o[r] (output j + r NS in the last pass) before they are stored
+template <typename T, int N, int TS, int R, int NS, int TWOFF, class LD, class ST, class PO = no_post>
+__device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>* __restrict__ tw, const int lt,
+                                        const PO& post = PO())
 {
     constexpr int NBF = N / R;
     constexpr int NB  = (NBF + TS - 1) / TS;
@@ -719,23 +731,38 @@ __device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>
                 twiddle_powers<T, R>(v, ldg(tw + TWOFF + k));
             dft_codelet<T, R>(v);
             const int d = (j - k) * R + k;
+            if constexpr (std::is_same_v<PO, no_post>)
+            {
 #pragma unroll
-            for (int r = 0; r < R; r++)
-                st(d + r * NS, v[codelet_out<R>(r)]);
+                for (int r = 0; r < R; r++)
+                    st(d + r * NS, v[codelet_out<R>(r)]);
+            }
+            else
+            {
+                cpx<T> o[R];
+#pragma unroll
+                for (int r = 0; r < R; r++)
+                    o[r] = v[codelet_out<R>(r)];
+                post(j, o);
+#pragma unroll
+                for (int r = 0; r < R; r++)
+                    st(d + r * NS, o[r]);
+            }
         }
     }
     __syncthreads();
 }
 
 template <typename T, int N, int TS, int NS, int TWOFF, int I, class LD, class ST, class H, class P, int R,
-          int... Rest>
+          int... Rest, class PO = no_post>
 __device__ __forceinline__ void pp_chain(const LD& ld, const ST& st, const H& hook, const P& pre_last, cpx<T>* A,
-                                         cpx<T>* B, const cpx<T>* __restrict__ tw, const int lt)
+                                         cpx<T>* B, const cpx<T>* __restrict__ tw, const int lt,
+                                         const PO& post = PO())
 {
     if constexpr (sizeof...(Rest) == 0)
     {
         pre_last();
-        pp_pass<T, N, TS, R, NS, TWOFF>(ld, st, tw, lt);
+        pp_pass<T, N, TS, R, NS, TWOFF>(ld, st, tw, lt, post);
         if constexpr (NS == 1)
             hook();
     }
@@ -749,17 +776,19 @@ __device__ __forceinline__ void pp_chain(const LD& ld, const ST& st, const H& ho
         if constexpr (NS == 1)
             hook();
         pp_chain<T, N, TS, NS * R, TN, I + 1, decltype(d_ld), ST, H, P, Rest...>(d_ld, st, hook, pre_last, A, B, tw,
-                                                                                lt);
+                                                                                lt, post);
     }
 }
 
-// hook() runs after the first pass, pre_last() before the last pass (all threads, uniformly).
-template <typename T, int N, int TS, int... Rs, class LD, class ST, class H, class P>
+// hook() runs after the first pass, pre_last() before the last pass (all threads, uniformly); post(j, o) as
+// in pp_pass, on the last pass's outputs.
+template <typename T, int N, int TS, int... Rs, class LD, class ST, class H, class P, class PO = no_post>
 __device__ __forceinline__ void ct_block_fft_pp(const LD& ld, const ST& st, const H& hook, const P& pre_last,
-                                                cpx<T>* A, cpx<T>* B, const cpx<T>* __restrict__ tw, const int lt)
+                                                cpx<T>* A, cpx<T>* B, const cpx<T>* __restrict__ tw, const int lt,
+                                                const PO& post = PO())
 {
     const int lta = lt < TS ? lt : N;
-    pp_chain<T, N, TS, 1, 0, 0, LD, ST, H, P, Rs...>(ld, st, hook, pre_last, A, B, tw, lta);
+    pp_chain<T, N, TS, 1, 0, 0, LD, ST, H, P, Rs...>(ld, st, hook, pre_last, A, B, tw, lta, post);
 }
 
 // ---------------------------------------------------------------------------------------------------

@@ -61,11 +61,24 @@ struct ct_fft
         ct_block_fft<T, N, TS, Rs...>(buf, tw, lt);
     }
     static constexpr int npass = sizeof...(Rs);
+    // radix of the last pass (whose butterfly j produces outputs j + r n / rlast)
+    static constexpr int rlast = [] {
+        constexpr int r[] = { Rs... };
+        return r[sizeof...(Rs) - 1];
+    }();
     template <class LD, class ST, class H, class P>
     __device__ __forceinline__ void run_pp(const LD& ld, const ST& st, const H& hook, const P& pre_last, cpx<T>* A,
                                            cpx<T>* B, const cpx<T>* __restrict__ tw, int lt) const
     {
         ct_block_fft_pp<T, N, TS, Rs...>(ld, st, hook, pre_last, A, B, tw, lt);
+    }
+    // as run_pp, with post(j, o) applied to each last-pass butterfly's outputs before they are stored
+    template <class LD, class PO, class ST>
+    __device__ __forceinline__ void run_pp_post(const LD& ld, const PO& post, const ST& st, cpx<T>* A, cpx<T>* B,
+                                                const cpx<T>* __restrict__ tw, int lt) const
+    {
+        const auto nothing = []() {};
+        ct_block_fft_pp<T, N, TS, Rs...>(ld, st, nothing, nothing, A, B, tw, lt, post);
     }
     // forward DFT, mid(q, x), forward DFT with the radices reversed (twiddles tw2) in 2 npass - 1 passes
     template <class LD, class MID, class ST, class H>
@@ -1005,6 +1018,8 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
     constexpr int NTC = (N2 + S - 1) / S;
     constexpr int SE  = (S * N1 * 8 + 1023) / 1024 * 128; // box elements, rounded to 1024 bytes
     constexpr int LB  = lbits_for<N1 * N2>();
+    constexpr int NSL = N1 / FA::rlast;                   // last pass: butterfly j makes outputs j + r NSL
+    static_assert((N1 * 8) % 16 == 0, "whole columns are bulk-copied");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T>* st0    = reinterpret_cast<cpx<T>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     cpx<T>* B      = st0 + 2 * SE;
@@ -1012,10 +1027,9 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
     const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
     const int g    = int(threadIdx.x) / TS;
     const int lt   = int(threadIdx.x) - g * TS;
-    const cpx<T>* twA  = reinterpret_cast<const cpx<T>*>(a.twA);
-    const cpx<T>* twB  = reinterpret_cast<const cpx<T>*>(a.twB);
-    const cpx<T>* tw   = reinterpret_cast<const cpx<T>*>(a.tw);
-    const auto nothing = []() {};
+    const cpx<T>* twA = reinterpret_cast<const cpx<T>*>(a.twA);
+    const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
+    const cpx<T>* tw  = reinterpret_cast<const cpx<T>*>(a.tw);
     const FA fa(nullptr, a.d, TS);
     constexpr uint32_t bytes = S * N1 * 8;
     if (threadIdx.x == 0)
@@ -1039,28 +1053,50 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
-                atomicExch(err, 1); // no other copy is in flight: the next one is issued after this wait
+            {
+                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                bulk_wait_all();
+            }
             return;
         }
         const long long tn = t + gridDim.x;
         if (threadIdx.x == 0 && tn < ntiles)
         {
-            // the other stage was last read by the previous tile's first pass, which ended in a barrier
+            // the other stage holds the previous tile's output: wait until its store has read it
+            bulk_wait_read();
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(&bars[s ^ 1], bytes);
             tensor_g2s_2d(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTC) * 2 * S, int(tn / NTC) * N1, &bars[s ^ 1]);
         }
         const long long b = t / NTC;
-        const int col     = int(t % NTC) * S + g;
-        cpx<T>* y         = reinterpret_cast<cpx<T>*>(a.out) + b * (long long)N1 * N2;
-        fa.run_pp([&](int p) { return conj_if(stage[swz128_8b(p, g)], cin); },
-                  [&](int k1, cpx<T> v)
-                  {
-                      if (N2 % S == 0 || col < N2)
-                          y[col * N1 + k1] = conj_if(v * twiddle_2level(twA, twB, (long long)(col * k1), LB), cout);
-                  },
-                  nothing, nothing, stage, B + g * GA, tw, lt);
+        const int c0      = int(t % NTC) * S;
+        const int col     = c0 + g;
+        // four-step twiddle W_N^{col k1} on the last pass's outputs k1 = j + r NSL: W_N^{col j} times powers
+        // of the tile's step W_N^{col NSL}
+        const cpx<T> step = twiddle_2level(twA, twB, (long long)(col * NSL), LB);
+        const auto post   = [&](int j, auto& o)
+        {
+            twiddle_powers<T, FA::rlast>(o, step);
+            const cpx<T> w = twiddle_2level(twA, twB, (long long)(col * j), LB);
+#pragma unroll
+            for (int r = 0; r < FA::rlast; r++)
+                o[r] = o[r] * w;
+        };
+        // pass 1 reads the box; pass 2 writes the tile's 16 output columns (contiguous in y) over it
+        fa.run_pp_post([&](int p) { return conj_if(stage[swz128_8b(p, g)], cin); }, post,
+                       [&](int k1, cpx<T> v) { stage[g * N1 + k1] = conj_if(v, cout); }, stage, B + g * GA, tw, lt);
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            const int ncols = N2 % S == 0 ? S : (N2 - c0 < S ? N2 - c0 : S);
+            bulk_s2g(reinterpret_cast<cpx<T>*>(a.out) + b * (long long)N1 * N2 + (long long)c0 * N1, stage,
+                     uint32_t(ncols * N1 * 8));
+            bulk_commit();
+        }
     }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
 }
 
 template <typename T, class FB, int N1>

@@ -133,7 +133,8 @@ static cudaError_t try_fspt_cols(const fourstep_args& a, cudaStream_t st, bool& 
     {
         constexpr int N1 = FA::n;
         tensor_map m;
-        if (!a.err || a.sig_stride != (long long)N1 * N2 || !map_rows(m, a.in, N2, N1 * a.batch, N1))
+        if (!a.err || a.sig_stride != (long long)N1 * N2 || reinterpret_cast<uintptr_t>(a.out) % 16 ||
+            !map_rows(m, a.in, N2, N1 * a.batch, N1))
             return cudaSuccess;
         done = true;
         return go_fspt(k_fspt_cols<float, FA, N2>, 16 * FA::ts, fspt_smem<FA>(), a.batch * ((N2 + 15) / 16), st, a,
