@@ -101,6 +101,49 @@
 
 namespace kfr_gpu
 {
+// b^e mod m (m < 2^31)
+KFR_CT_HD constexpr long long powmod_ll(long long b, long long e, long long m)
+{
+    long long r = 1;
+    b %= m;
+    while (e > 0)
+    {
+        if (e & 1)
+            r = r * b % m;
+        b = b * b % m;
+        e >>= 1;
+    }
+    return r;
+}
+
+// smallest primitive root of the prime n (the generator of Rader's permutation, shared by the planner and
+// the compile-time kernels)
+KFR_CT_HD constexpr long long primitive_root(long long n)
+{
+    const long long L = n - 1;
+    for (long long g = 2; g < n; g++)
+    {
+        bool ok = true;
+        long long x = L;
+        for (long long p = 2; p * p <= x && ok; p++)
+            if (x % p == 0)
+            {
+                if (powmod_ll(g, L / p, n) == 1)
+                    ok = false;
+                while (x % p == 0)
+                    x /= p;
+            }
+        if (ok && x > 1 && powmod_ll(g, L / x, n) == 1)
+            ok = false;
+        if (ok)
+            return g;
+    }
+    return 1;
+}
+} // namespace kfr_gpu
+
+namespace kfr_gpu
+{
 KFR_CT_HD constexpr int ct_pad_shift_f32(int n, int ts)
 {
 #define KFR_CT_LAYOUT_SHIFT(N, TS, S, E)                                                                   \

@@ -571,46 +571,9 @@ template <typename T>
 void complex_engine<T>::init_rader(long long n)
 {
     const long long L = n - 1;
-    // smallest primitive root g of the prime n
-    std::vector<long long> fac;
-    {
-        long long x = L;
-        for (long long p = 2; p * p <= x; p++)
-            if (x % p == 0)
-            {
-                fac.push_back(p);
-                while (x % p == 0)
-                    x /= p;
-            }
-        if (x > 1)
-            fac.push_back(x);
-    }
-    auto powmod = [](long long b, long long e, long long md)
-    {
-        long long r = 1;
-        b %= md;
-        while (e)
-        {
-            if (e & 1)
-                r = r * b % md;
-            b = b * b % md;
-            e >>= 1;
-        }
-        return r;
-    };
-    long long g = 2;
-    for (;; g++)
-    {
-        bool ok = true;
-        for (long long f : fac)
-            if (powmod(g, L / f, n) == 1)
-            {
-                ok = false;
-                break;
-            }
-        if (ok)
-            break;
-    }
+    // smallest primitive root g of the prime n (the compile-time kernels derive the same one)
+    const long long g = primitive_root(n);
+    const auto powmod = powmod_ll;
     std::vector<int> pin(n, 0), qof(n, 0);
     std::vector<std::complex<double>> b(L);
     long long gp = 1; // g^p
