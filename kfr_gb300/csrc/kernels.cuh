@@ -172,11 +172,15 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2c(const c2c_args a, con
 
 // ---------------------------------------------------------------------------------------------------
 // Complex DFT, contiguous batch, persistent and pipelined (compile-time lengths).  Each CTA walks tiles of
-// `spc` whole signals (tile t = signals [t*spc, t*spc + spc)).  One thread streams the next tile into the
-// other of two stage buffers with a bulk asynchronous copy (TMA) while the CTA transforms the current
-// one: the first pass reads the stage, the middle passes run in the padded work buffer, and the last pass
-// stores straight to global memory.  Only whole tiles are handled here; the host runs the remainder with
-// k_c2c.  A wait that runs out sets *err and the CTA returns.
+// `spc` whole signals (tile t = signals [t*spc, t*spc + spc), a whole number of 16-byte units).  Three tile
+// buffers rotate: the input tile (loaded by one bulk asynchronous copy, TMA; then the passes' A buffer), the
+// scratch tile (the passes' B buffer) and the spare tile, into which the next tile streams while the CTA
+// transforms the current one.  The first pass reads the input tile, the passes ping-pong between A and B in
+// the padded layout, and the last pass writes the tile's output in natural order into whichever of the two
+// it does not read; one bulk copy stores it.  The next tile's input is this one's spare, its scratch the
+// buffer the last pass read, its spare this one's output (reloaded once its bulk store has read it).  Only
+// whole tiles are handled here; the host runs the remainder with k_c2c.  A wait that runs out sets *err and
+// the CTA returns.
 // ---------------------------------------------------------------------------------------------------
 template <typename T, class F>
 __global__ void __launch_bounds__(F::max_threads, 1)
@@ -186,12 +190,10 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     constexpr int N      = F::n;
     constexpr int STRIDE = F::gstride(N);
     const F fft(nullptr, a.d, F::ts);
-    const int tile   = spc * N;
-    const int slen   = pipe_stage_len(spc, N, STRIDE);
-    cpx<T>* stage0   = reinterpret_cast<cpx<T>*>(smem_raw);
-    cpx<T>* stage1   = stage0 + slen;
-    cpx<T>* work     = stage1 + slen;
-    uint64_t* bars   = reinterpret_cast<uint64_t*>(work + spc * STRIDE);
+    const int tile      = spc * N;
+    const int slen      = pipe_stage_len(spc, N, STRIDE);
+    cpx<T>* const tiles = reinterpret_cast<cpx<T>*>(smem_raw);
+    uint64_t* bars      = reinterpret_cast<uint64_t*>(tiles + 3 * slen);
     const uint32_t bytes = uint32_t(tile) * uint32_t(sizeof(cpx<T>));
     const cpx<T>* in = reinterpret_cast<const cpx<T>*>(a.in);
     cpx<T>* out      = reinterpret_cast<cpx<T>*>(a.out);
@@ -200,8 +202,8 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     const group_map gm(F::ts, spc);
     if (threadIdx.x == 0)
     {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int b = 0; b < 3; b++)
+            mbar_init(&bars[b], 1);
         mbar_fence_init();
     }
     __syncthreads();
@@ -209,49 +211,60 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     if (threadIdx.x == 0 && t < ntiles)
     {
         mbar_arrive_expect_tx(&bars[0], bytes);
-        bulk_g2s(stage0, in + t * tile, bytes, &bars[0]);
+        bulk_g2s(tiles, in + t * tile, bytes, &bars[0]);
     }
-    uint32_t phase   = 0;                // bit s: parity to wait for on stage s
-    uint32_t pending = t < ntiles ? 1 : 0; // bit s: a copy into stage s is in flight
-    int it           = 0;
-    for (; t < ntiles; t += gridDim.x, it++)
+    uint32_t phase = 0;              // bit b: parity to wait for on tile buffer b
+    int bi = 0, bs = 1, bn = 2;      // input, scratch and spare tile buffers
+    for (; t < ntiles; t += gridDim.x)
     {
-        const int sb   = it & 1;
-        cpx<T>* stage  = sb ? stage1 : stage0;
-        const bool got = mbar_wait(&bars[sb], (phase >> sb) & 1);
+        cpx<T>* in_t   = tiles + bi * slen;
+        cpx<T>* scr_t  = tiles + bs * slen;
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
-                atomicExch(err, 1);
-                // give the other stage's copy (if any) a bounded chance to land before the CTA exits
-                if ((pending >> (sb ^ 1)) & 1)
-                    mbar_wait(&bars[sb ^ 1], (phase >> (sb ^ 1)) & 1);
+                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                bulk_wait_all();
             }
             return;
         }
-        phase ^= 1u << sb;
-        pending &= ~(1u << sb);
+        phase ^= 1u << bi;
         const long long tn = t + gridDim.x;
-        if (tn < ntiles)
+        // after the first pass: the spare buffer holds the previous tile's output; once its bulk store has
+        // read it, stream the next tile in
+        const auto prefetch = [&]()
         {
-            pending |= 1u << (sb ^ 1);
-            if (threadIdx.x == 0)
+            if (threadIdx.x == 0 && tn < ntiles)
             {
-                // the other stage was last used by the previous tile's passes, which ended in a barrier
+                bulk_wait_read();
                 fence_proxy_async_smem();
-                mbar_arrive_expect_tx(&bars[sb ^ 1], bytes);
-                bulk_g2s(sb ? stage0 : stage1, in + tn * tile, bytes, &bars[sb ^ 1]);
+                mbar_arrive_expect_tx(&bars[bn], bytes);
+                bulk_g2s(tiles + bn * slen, in + tn * tile, bytes, &bars[bn]);
             }
-        }
-        // ping-pong between the stage (its padded layout, once the first pass has read the tile) and the
-        // work buffer; the last pass stores straight to global memory (stride one across threads)
-        const cpx<T>* src  = stage + gm.g * N;
-        cpx<T>* gout       = out + (t * spc + gm.g) * N;
+        };
+        // pass i writes B (i even) or A (i odd): the last pass reads A when the pass count is odd
+        constexpr bool odd = F::npass % 2 == 1;
+        cpx<T>* ob         = odd ? scr_t : in_t;
+        const cpx<T>* src  = in_t + gm.g * N;
+        cpx<T>* osig       = ob + gm.g * N;
         const auto nothing = []() {};
-        fft.run_pp([&](int p) { return conj_if(src[p], inv); }, [&](int q, cpx<T> x) { gout[q] = conj_if(x, inv); },
-                   nothing, nothing, stage + gm.g * STRIDE, work + gm.g * STRIDE, tw, gm.lt);
+        fft.run_pp([&](int p) { return conj_if(src[p], inv); }, [&](int q, cpx<T> x) { osig[q] = conj_if(x, inv); },
+                   prefetch, nothing, in_t + gm.g * STRIDE, scr_t + gm.g * STRIDE, tw, gm.lt);
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            bulk_s2g(out + t * tile, ob, bytes);
+            bulk_commit();
+        }
+        const int ob_i = odd ? bs : bi, free_i = odd ? bi : bs;
+        bi = bn;
+        bs = free_i;
+        bn = ob_i;
     }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
 }
 
 // ---------------------------------------------------------------------------------------------------

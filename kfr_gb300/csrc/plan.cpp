@@ -656,7 +656,7 @@ void complex_engine<T>::plan_pipe()
         const int threads = ((spc * prog_.ts + 31) / 32) * 32;
         if (threads > 1024)
             break;
-        const int smem = (2 * pipe_stage_len(spc, n, prog_.gstride) + spc * prog_.gstride) * esz + 64;
+        const int smem = 3 * pipe_stage_len(spc, n, prog_.gstride) * esz + 64;
         if (smem > smem_budget())
             break;
         const int by_smem = (max_smem_bytes() + 1024) / (smem + 1024);
@@ -957,7 +957,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             if (ntiles > 0)
             {
                 block_cfg pc = prog_.cfg_tile(pipe_spc_);
-                pc.smem = (2 * pipe_stage_len(pipe_spc_, int(n_), prog_.gstride) + pipe_spc_ * prog_.gstride) * int(esz) + 64;
+                pc.smem = 3 * pipe_stage_len(pipe_spc_, int(n_), prog_.gstride) * int(esz) + 64;
                 check(launch_ct_c2c_pipe_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st), "launch c2c (pipelined)");
                 done = ntiles * pipe_spc_;
             }
