@@ -442,13 +442,24 @@ __global__ void __launch_bounds__(F::max_threads, 1)
         mbar_fence_init();
     }
     __syncthreads();
+    // Tile t holds signals [t spc, t spc + ns), ns = spc except for a shorter last tile.  Its bytes
+    // [s0, e) are loaded as the enclosing 16-byte-aligned range; for the last tile, whose range could
+    // reach past the batch, only the aligned part [s0 & ~15, e & ~15) goes by bulk copy and a final
+    // 8-byte element beyond it by a plain load (visible to the CTA after the barrier that follows the wait).
+    const auto tile_sigs = [&](long long tt) { return int(a.batch - tt * spc < spc ? a.batch - tt * spc : spc); };
+    const auto load_tile = [&](long long tt, cpx<T>* buf, uint64_t* bar)
+    {
+        const long long s0 = tt * tile_bytes, e = s0 + (long long)tile_sigs(tt) * N * ESZ;
+        const long long a0 = s0 & ~15LL, a1 = tt == ntiles - 1 ? (e & ~15LL) : ((e + 15) & ~15LL);
+        mbar_arrive_expect_tx(bar, uint32_t(a1 - a0));
+        bulk_g2s(buf, inb + a0, uint32_t(a1 - a0), bar);
+        if (a1 < e)
+            *reinterpret_cast<cpx<T>*>(reinterpret_cast<char*>(buf) + (e - ESZ - a0)) =
+                *reinterpret_cast<const cpx<T>*>(inb + e - ESZ);
+    };
     long long t = blockIdx.x;
     if (threadIdx.x == 0 && t < ntiles)
-    {
-        const long long s0 = t * tile_bytes, a0 = s0 & ~15LL, a1 = (s0 + tile_bytes + 15) & ~15LL;
-        mbar_arrive_expect_tx(&bars[0], uint32_t(a1 - a0));
-        bulk_g2s(tiles, inb + a0, uint32_t(a1 - a0), &bars[0]);
-    }
+        load_tile(t, tiles, &bars[0]);
     uint32_t phase   = 0;                  // bit b: parity to wait for on tile buffer b
     uint32_t pending = t < ntiles ? 1 : 0; // bit b: a copy into tile buffer b is in flight
     int bi           = 0;                  // tile buffer holding the current input
@@ -493,9 +504,7 @@ __global__ void __launch_bounds__(F::max_threads, 1)
                     // the spare buffer was last read by the previous tile's bulk store
                     bulk_wait_read();
                     fence_proxy_async_smem();
-                    const long long n0 = tn * tile_bytes, b0 = n0 & ~15LL, b1 = (n0 + tile_bytes + 15) & ~15LL;
-                    mbar_arrive_expect_tx(&bars[bn], uint32_t(b1 - b0));
-                    bulk_g2s(spare, inb + b0, uint32_t(b1 - b0), &bars[bn]);
+                    load_tile(tn, spare, &bars[bn]);
                 }
             }
         };
@@ -515,7 +524,8 @@ __global__ void __launch_bounds__(F::max_threads, 1)
         __syncthreads();
         // the tile's output: its 16-byte-aligned interior by a bulk store, the (at most two) 8-byte edge
         // elements by plain stores
-        const long long e1 = s0 + tile_bytes;
+        const int ns       = tile_sigs(t);
+        const long long e1 = s0 + (long long)ns * N * ESZ;
         const long long c0 = (s0 + 15) & ~15LL, c1 = e1 & ~15LL;
         if (threadIdx.x == 0)
         {
@@ -526,7 +536,7 @@ __global__ void __launch_bounds__(F::max_threads, 1)
         if (threadIdx.x == 32 % blockDim.x && c0 != s0)
             *reinterpret_cast<cpx<T>*>(outb + s0) = scr_t[off];
         if (threadIdx.x == 64 % blockDim.x && c1 != e1)
-            *reinterpret_cast<cpx<T>*>(outb + e1 - ESZ) = scr_t[off + spc * N - 1];
+            *reinterpret_cast<cpx<T>*>(outb + e1 - ESZ) = scr_t[off + ns * N - 1];
         bi = bn;
     }
     if (threadIdx.x == 0)

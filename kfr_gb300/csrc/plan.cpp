@@ -896,7 +896,7 @@ int complex_engine<T>::launches(long long batch) const
     case kind::bluestein_smem: return 1;
     case kind::fourstep: return 2 * int((batch + 65534) / 65535);
     case kind::bluestein_multi: return 3 + 2 * inner_->launches(batch);
-    case kind::rader_smem: return (rader_spc_ && (batch - 1) / rader_spc_ > 0) ? 2 : 1;
+    case kind::rader_smem: return 1;
     case kind::tensor: return 1;
     }
     return 0;
@@ -1010,21 +1010,19 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.div_l   = make_fast_div(uint32_t(n_ - 1));
         a.d       = prog_.desc;
         long long done = 0;
-        // Persistent tiled kernel over whole tiles that end before the last signal (whose enclosing
-        // 16-byte range may end past the batch); the rest runs in the plain kernel.
+        // Persistent tiled kernel over all signals (the last tile may be shorter and ends exactly at the
+        // batch's end); the plain kernel when the layout does not allow it.
         if (rader_spc_ && err_.get() && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 &&
             (reinterpret_cast<uintptr_t>(out) % 16) == 0)
         {
-            const long long ntiles = (batch - 1) / rader_spc_;
-            if (ntiles > 0)
-            {
-                block_cfg pc = prog_.cfg_tile(rader_spc_);
-                pc.smem      = rader_tile_smem(rader_spc_);
-                check(launch_ct_rader_tile_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st),
-                      "launch rader (tiled)");
-                done = ntiles * rader_spc_;
-            }
+            const long long ntiles = (batch + rader_spc_ - 1) / rader_spc_;
+            block_cfg pc           = prog_.cfg_tile(rader_spc_);
+            pc.smem                = rader_tile_smem(rader_spc_);
+            check(launch_ct_rader_tile_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st), "launch rader (tiled)");
+            done = batch;
         }
+        if (done == batch)
+            return;
         a.in    = static_cast<const char*>(in) + done * n_ * esz;
         a.out   = static_cast<char*>(out) + done * n_ * esz;
         a.batch = batch - done;

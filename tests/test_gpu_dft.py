@@ -97,14 +97,15 @@ def test_complex_dft_batched_against_oracle(orc, n, batch, sfx):
     assert rel_rms(zd.cpu().numpy(), ref) <= tol(n, sfx), n
 
 
-@pytest.mark.parametrize("n,batch", [(127, 40000), (8191, 500)])
+@pytest.mark.parametrize("n,batch", [(127, 40000), (8191, 500), (127, 40001), (8191, 301), (8191, 1), (127, 1)])
 def test_rader_tiles_many_per_cta(orc, n, batch):
-    """Prime lengths through the persistent tiled Rader kernel with several tiles per CTA (stage buffers
-    reused, output bulk stores overlapping the next tile's load), forward, inverse, in place, and from an
-    8-byte-misaligned pointer (which takes the plain kernel)."""
+    """Prime lengths through the persistent tiled Rader kernel with several tiles per CTA (tile buffers
+    reused, output bulk stores overlapping the next tile's load), a shorter last tile, a batch whose end is
+    8 bytes past a 16-byte boundary (the last element loaded separately), forward, inverse, in place, and
+    from an 8-byte-misaligned pointer (which takes the plain kernel)."""
     rng = np.random.default_rng(n + batch)
     x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
-    pick = np.r_[0:3, batch // 2, batch - 3:batch]
+    pick = np.unique(np.r_[0:3, batch // 2, batch - 3:batch].clip(0, batch - 1))
     ref = orc.dft(x[pick].astype(np.complex128), threads=8)
     refi = orc.dft(x[pick].astype(np.complex128), inverse=True, threads=8)
     plan = k.dft_plan(n, "f32")
