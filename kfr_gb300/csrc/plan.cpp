@@ -1145,7 +1145,11 @@ std::string complex_engine<T>::describe() const
         s << "tensor-core n=" << n_ << " radix-16 passes as mma.sync contractions, "
           << (tc_mode_ == TC_BF16 ? "BF16" : "FP16") << " hi+lo operands, FP32 accumulation";
         break;
-    case kind::smem: s << "smem " << prog_.describe(); break;
+    case kind::smem:
+        s << "smem " << prog_.describe();
+        if (pipe_spc_)
+            s << " pipelined spc=" << pipe_spc_;
+        break;
     case kind::bluestein_smem: s << "bluestein_smem n=" << n_ << " m=" << m_ << " [" << prog_.describe() << "]"; break;
     case kind::fourstep:
         s << "fourstep" << (pair_ ? " (compile-time pair)" : "") << " n=" << n_ << " = " << n1_ << " x " << n2_
