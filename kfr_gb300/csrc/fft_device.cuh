@@ -899,6 +899,80 @@ __device__ __forceinline__ void ct_conv_pp(const LD& ld, const MID& mid, const S
     pp_conv_chain<T, N, TS, 1, 0, 0, Tail, LD, MID, ST, H, Rs...>(ld, mid, st, hook, A, B, tw, tw2, lta);
 }
 
+// In-place compile-time block FFT with the signal in registers between the passes (EPT values per thread)
+// and its loads and stores given as functors: the first pass reads ld(p), the passes exchange through the
+// padded buffer, the last pass writes st(q, x).  Each pass loads (and transforms) all of its butterflies,
+// then runs mid() for the last pass or a barrier otherwise, then stores; a barrier follows each store phase
+// except the last pass's.  mid() must contain a barrier (after it the buffer is no longer read).
+template <typename T, int N, int TS, int EPT, int R, int NS, int TWOFF, class LD, class MID, class ST>
+__device__ __forceinline__ void io_pass(cpx<T> (&v)[EPT], const LD& ld, const MID& mid, const ST& st,
+                                        const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int NBF = N / R;
+    constexpr int NB  = (NBF + TS - 1) / TS;
+    static_assert(NB * R <= EPT, "register array too small");
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+            cpx<T> u[R];
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                u[r] = ld(j + r * NBF);
+            if constexpr (NS > 1)
+                twiddle_powers<T, R>(u, ldg(tw + TWOFF + j % NS));
+            dft_codelet<T, R>(u);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[b * R + r] = u[codelet_out<R>(r)];
+        }
+    }
+    mid();
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+    {
+        const int j = lt + b * TS;
+        if (j < NBF)
+        {
+            const int k = NS > 1 ? j % NS : 0;
+            const int d = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                st(d + r * NS, v[b * R + r]);
+        }
+    }
+}
+
+template <typename T, int N, int TS, int EPT, int NS, int TWOFF, class LD, class MID, class ST, int R, int... Rest>
+__device__ __forceinline__ void io_chain(cpx<T> (&v)[EPT], const LD& ld, const MID& mid, const ST& st, cpx<T>* buf,
+                                         const cpx<T>* __restrict__ tw, const int lt)
+{
+    if constexpr (sizeof...(Rest) == 0)
+        io_pass<T, N, TS, EPT, R, NS, TWOFF>(v, ld, mid, st, tw, lt);
+    else
+    {
+        const auto sync = []() { __syncthreads(); };
+        const auto b_st = [buf](int q, cpx<T> x) { buf[pidx_s<ct_ps<T>(N, TS)>(q)] = x; };
+        const auto b_ld = [buf](int p) { return buf[pidx_s<ct_ps<T>(N, TS)>(p)]; };
+        io_pass<T, N, TS, EPT, R, NS, TWOFF>(v, ld, sync, b_st, tw, lt);
+        __syncthreads();
+        constexpr int TN = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
+        io_chain<T, N, TS, EPT, NS * R, TN, decltype(b_ld), MID, ST, Rest...>(v, b_ld, mid, st, buf, tw, lt);
+    }
+}
+
+template <typename T, int N, int TS, int... Rs, class LD, class MID, class ST>
+__device__ __forceinline__ void ct_block_fft_io(const LD& ld, const MID& mid, const ST& st, cpx<T>* buf,
+                                                const cpx<T>* __restrict__ tw, const int lt)
+{
+    constexpr int EPT = ct_ept<N, TS, Rs...>();
+    const int lta     = lt < TS ? lt : N;
+    cpx<T> v[EPT];
+    io_chain<T, N, TS, EPT, 1, 0, LD, MID, ST, Rs...>(v, ld, mid, st, buf, tw, lta);
+}
+
 // Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a
 // barrier.
 __device__ __forceinline__ void stage_passes(pass_desc* sp, const fft_desc& d)

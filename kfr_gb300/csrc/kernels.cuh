@@ -72,6 +72,13 @@ struct ct_fft
     {
         ct_block_fft_pp<T, N, TS, Rs...>(ld, st, hook, pre_last, A, B, tw, lt);
     }
+    // in place with the signal in registers: first pass reads ld(p), last pass stores st(q, x) after mid()
+    template <class LD, class MID, class ST>
+    __device__ __forceinline__ void run_io(const LD& ld, const MID& mid, const ST& st, cpx<T>* buf,
+                                           const cpx<T>* __restrict__ tw, int lt) const
+    {
+        ct_block_fft_io<T, N, TS, Rs...>(ld, mid, st, buf, tw, lt);
+    }
     // as run_pp, with post(j, o) applied to each last-pass butterfly's outputs before they are stored
     template <class LD, class PO, class ST>
     __device__ __forceinline__ void run_pp_post(const LD& ld, const PO& post, const ST& st, cpx<T>* A, cpx<T>* B,
@@ -265,6 +272,68 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     }
     if (threadIdx.x == 0)
         bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Complex DFT, one signal per CTA, persistent (compile-time lengths whose three-tile pipeline does not fit,
+// e.g. N = 8192, 16384).  The signal lives in registers between the passes, which exchange through one
+// padded shared buffer.  A bulk copy (TMA) brings each signal into that buffer; the last pass first loads
+// its inputs, then (after a barrier) the next signal's copy is issued into the buffer, and the last pass's
+// outputs go straight to global memory while it lands.  A wait that runs out sets *err and the CTA returns.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1)
+    k_c2c_reg(const c2c_args a, const long long nsig, int* err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int N          = F::n;
+    constexpr uint32_t bytes = uint32_t(N) * uint32_t(sizeof(cpx<T>));
+    const F fft(nullptr, a.d, F::ts);
+    static_assert(bytes % 16 == 0, "whole 16-byte units per signal");
+    cpx<T>* buf      = reinterpret_cast<cpx<T>*>(smem_raw);
+    uint64_t* bar    = reinterpret_cast<uint64_t*>(buf + F::gstride(N));
+    const cpx<T>* in = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* out      = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
+    const bool inv   = a.inverse != 0;
+    const int lt     = int(threadIdx.x);
+    if (threadIdx.x == 0)
+    {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long s = blockIdx.x;
+    if (threadIdx.x == 0 && s < nsig)
+    {
+        mbar_arrive_expect_tx(bar, bytes);
+        bulk_g2s(buf, in + s * N, bytes, bar);
+    }
+    for (uint32_t phase = 0; s < nsig; s += gridDim.x, phase ^= 1)
+    {
+        const bool got = mbar_wait(bar, phase);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+                atomicExch(err, 1);
+            return;
+        }
+        const long long sn = s + gridDim.x;
+        cpx<T>* o          = out + s * N;
+        fft.run_io([&](int p) { return conj_if(buf[p], inv); },
+                   [&]()
+                   {
+                       // every thread has read the buffer: the next signal may overwrite it
+                       __syncthreads();
+                       if (threadIdx.x == 0 && sn < nsig)
+                       {
+                           fence_proxy_async_smem();
+                           mbar_arrive_expect_tx(bar, bytes);
+                           bulk_g2s(buf, in + sn * N, bytes, bar);
+                       }
+                   },
+                   [&](int q, cpx<T> x) { o[q] = conj_if(x, inv); }, buf, tw, lt);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------

@@ -94,6 +94,28 @@ cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long l
 #undef KFR_GPU_PIPE_CASE
 }
 
+// one signal per CTA, persistent: built for the lengths whose three-tile pipeline does not fit (8192 and up)
+template <class F>
+static cudaError_t go_reg(const c2c_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st)
+{
+    if constexpr (F::n >= 8192)
+        return go_persistent(k_c2c_reg<float, F>, c, nsig, st, a, nsig, err);
+    else
+        return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st)
+{
+#define KFR_GPU_REG_CASE(N, TS, ...)                                                                       \
+    case N: return go_reg<ct_fft<float, N, TS, __VA_ARGS__>>(a, c, nsig, err, st);
+    switch (c.ct)
+    {
+        KFR_CT_C2C_F32(KFR_GPU_REG_CASE)
+    default: return cudaErrorInvalidValue;
+    }
+#undef KFR_GPU_REG_CASE
+}
+
 cudaError_t launch_ct_rader_tile_f32(const rader_args& a, const block_cfg& c, long long ntiles, int* err,
                                      cudaStream_t st)
 {

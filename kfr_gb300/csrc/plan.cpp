@@ -672,7 +672,16 @@ void complex_engine<T>::plan_pipe()
         }
     }
     if (!best)
+    {
+        // one signal per CTA with the signal in registers (lengths whose three tiles do not fit)
+        if (n >= 8192 && prog_.gstride * esz + 16 <= smem_budget())
+        {
+            reg_ = true;
+            err_.alloc(sizeof(int));
+            check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
+        }
         return;
+    }
     pipe_spc_ = best;
     err_.alloc(sizeof(int));
     check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
@@ -951,6 +960,13 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.div_n   = make_fast_div(uint32_t(n_));
         a.d       = prog_.desc;
         long long done = 0;
+        if (reg_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
+        {
+            block_cfg rc = prog_.cfg_tile(1);
+            rc.smem      = prog_.gstride * int(esz) + 16;
+            check(launch_ct_c2c_reg_f32(a, rc, batch, static_cast<int*>(err_.get()), st), "launch c2c (one per CTA)");
+            done = batch;
+        }
         if (pipe_spc_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
         {
             const long long ntiles = batch / pipe_spc_;
@@ -1149,6 +1165,8 @@ std::string complex_engine<T>::describe() const
         s << "smem " << prog_.describe();
         if (pipe_spc_)
             s << " pipelined spc=" << pipe_spc_;
+        if (reg_)
+            s << " persistent one per CTA";
         break;
     case kind::bluestein_smem: s << "bluestein_smem n=" << n_ << " m=" << m_ << " [" << prog_.describe() << "]"; break;
     case kind::fourstep:

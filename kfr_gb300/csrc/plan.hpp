@@ -183,6 +183,7 @@ private:
     int lbits_ = 0;
     // pipelined smem path (compile-time lengths): signals per tile, 0 = not used
     int pipe_spc_ = 0;
+    bool reg_     = false; // persistent one-signal-per-CTA kernel (pipeline does not fit)
     dbuf err_;
 
     void init_bluestein(long long n);

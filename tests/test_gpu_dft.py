@@ -129,6 +129,36 @@ def test_rader_tiles_many_per_cta(orc, n, batch):
     assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
 
 
+@pytest.mark.parametrize("n,batch", [(16384, 400), (8192, 500), (16384, 1)])
+def test_one_signal_per_cta_persistent(orc, n, batch):
+    """Lengths that run one signal per persistent CTA with the signal in registers (the next signal's bulk
+    copy lands while the last pass stores): several signals per CTA, forward, inverse, in place, and from an
+    8-byte-misaligned pointer (which takes the per-signal kernel)."""
+    rng = np.random.default_rng(n + batch)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    pick = np.unique(np.r_[0:2, batch // 2, batch - 2:batch].clip(0, batch - 1))
+    ref = orc.dft(x[pick].astype(np.complex128), threads=8)
+    refi = orc.dft(x[pick].astype(np.complex128), inverse=True, threads=8)
+    plan = k.dft_plan(n, "f32")
+    assert "persistent one per CTA" in plan.describe()
+    xd = dev(x)
+    yd = torch.empty_like(xd)
+    plan.execute_batch(yd, xd, batch)
+    assert rel_rms(yd.cpu().numpy()[pick], ref) <= tol(n, "f32")
+    full = yd.clone()
+    plan.execute_batch(yd, xd, batch, inverse=True)
+    assert rel_rms(yd.cpu().numpy()[pick], refi) <= tol(n, "f32")
+    zd = xd.clone()
+    plan.execute_batch(zd, zd, batch)
+    assert torch.equal(zd, full)
+    buf = torch.empty(batch * n + 1, dtype=torch.complex64, device="cuda")
+    buf[1:].copy_(xd.reshape(-1))
+    out = torch.empty_like(buf)
+    plan.execute_batch(out[1:], buf[1:], batch)
+    got = out[1:].reshape(batch, n).cpu().numpy()
+    assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
+
+
 @pytest.mark.parametrize("n,batch", [(30720, 300), (24000, 200), (65536, 150)])
 def test_fourstep_pair_tiles_many_per_cta(orc, n, batch):
     """Four-step lengths whose column and row passes run as persistent kernels fed by 2-D tensor copies
