@@ -40,12 +40,16 @@ METRIC = "batched c32 DFT GB/s (% of HBM roofline), chosen vs plain form at ≤1
 FALLBACK_HBM_GBS = 6800.0
 
 # DRAM bytes per signal measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided
-# by the signals it processed) at the full 256 MiB batch, from the --set full captures of the k_rader_pipe,
-# k_rader and k_fs_cols / k_fs_rows launches summarised under profiles/.
+# by the signals it processed; one-pass metrics captured on the full 256 MiB batches of this workload), from
+# the k_c2c_pipe, k_fspt_cols / k_fspt_rows and k_rader_tile launches summarised under profiles/.  Writes fall
+# short of the algorithmic bytes by the output still in L2 when a launch ends.
 NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float] = {
-    8191: (271_920_896 + 229_835_264) / 4095,
-    127: (268_492_800 + 222_380_800) / 264208,
-    30720: (268_423_680 + 222_224_896 + 268_483_584 + 220_418_560) / 1092,
+    1000: (268_458_752 + 220_087_808) / 33554,
+    1536: (268_478_976 + 213_590_016) / 21845,
+    2187: (268_478_464 + 216_733_952) / 15342,
+    30720: (268_411_904 + 216_763_648 + 268_468_480 + 212_934_144) / 1092,
+    127: (268_505_088 + 213_239_040) / 264208,
+    8191: (268_732_928 + 214_331_648) / 4096,
 }
 
 
