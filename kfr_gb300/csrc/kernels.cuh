@@ -1078,40 +1078,94 @@ __global__ void __launch_bounds__(1024, 1) k_fsp_rows(const fourstep_args a)
 
 // ---------------------------------------------------------------------------------------------------
 // Four-step pair kernels, persistent, with 2-D tensor copies (TMA).  Same transforms as k_fsp_cols /
-// k_fsp_rows for two-pass lengths of at most 256 on tiles of 16 columns (rows): a tile is one box of 16
-// contiguous 8-byte elements (128 bytes) per row, loaded with the 128-byte swizzle (conflict-free column
-// reads), double buffered: the next tile streams in while the CTA transforms the current one.  The column
-// pass stores straight from its last pass (times the four-step twiddle); the row pass stages its output in
-// the swizzled box and stores it with one tensor copy.  Waits are bounded; one that runs out sets *err and
-// the CTA returns.
-//   in map (columns): x viewed as (2 N2 floats) x (N1 * batch) rows, box (32 floats, N1)
-//   in / out maps (rows): y and X viewed as (2 N1 floats) x (N2 * batch) rows, box (32 floats, N2)
+// k_fsp_rows for lengths of two or three passes: a tile is S columns (rows) of the signal, S = 16 or 8
+// contiguous 8-byte elements (128 or 64 bytes) per row, loaded as one box per 256 rows with the matching
+// swizzle (conflict-free column reads) and double buffered: the next tile streams in while the CTA
+// transforms the current one.  Waits are bounded; one that runs out sets *err and the CTA returns.
+//   column pass: the four-step twiddle per butterfly of the last pass; two passes: the tile's S output
+//     columns (contiguous in the intermediate) are written over the box and stored by one bulk copy; three
+//     passes (the box is the ping-pong A buffer): stored straight from the last pass;
+//   row pass: two passes: the output is written back into the swizzled box and stored by tensor copies;
+//     three passes: threads are ordered row-fastest, so the last pass stores S consecutive outputs per
+//     column index straight to global memory.
+//   in map (columns): x viewed as (2 N2 floats) x (N1 * batch) rows, box (2 S floats, min(N1, 256))
+//   in / out maps (rows): y and X viewed as (2 N1 floats) x (N2 * batch) rows, box (2 S floats, min(N2, 256))
 // ---------------------------------------------------------------------------------------------------
+template <class F>
+__host__ __device__ constexpr int fspt_stage_elems(int S)
+{
+    // the box, or (three passes) the padded A buffer of S signals, rounded to 1024 bytes
+    const int e = F::npass == 3 && S * F::gstride() > S * F::n ? S * F::gstride() : S * F::n;
+    return (e * 8 + 1023) / 1024 * 128;
+}
+
+// shared memory of a tensor-copy pair kernel: two stage tiles, the B buffer, two mbarriers, alignment slack
+template <class F>
+__host__ __device__ constexpr int fspt_smem_s(int S)
+{
+    return 2 * fspt_stage_elems<F>(S) * 8 + S * F::gstride() * 8 + 16 + 1024;
+}
+
+// tile width: the widest of 16 and 8 whose threads and shared memory fit (0: none)
+template <class F>
+__host__ __device__ constexpr int fspt_tile()
+{
+    if (!(F::npass == 2 || F::npass == 3) || !(F::n <= 256 || F::n % 256 == 0))
+        return 0;
+    for (int S = 16; S >= 8; S /= 2)
+        if (S * F::ts <= 1024 && fspt_smem_s<F>(S) <= kFspSmem)
+            return S;
+    return 0;
+}
+
 template <class F>
 __host__ __device__ constexpr bool fspt_ok()
 {
-    return F::npass == 2 && F::n <= 256 && fsp_tile(F::n, F::ts, kFspSmem) == 16;
+    return fspt_tile<F>() != 0;
 }
 
-// shared memory of a TMA pair kernel of length N: two 1024-byte-aligned boxes of 16 x N, the second
-// ping-pong buffer, two mbarriers and the alignment slack
 template <class F>
 __host__ __device__ constexpr int fspt_smem()
 {
-    return 2 * ((16 * F::n * 8 + 1023) / 1024 * 1024) + 16 * F::gstride() * 8 + 16 + 1024;
+    return fspt_smem_s<F>(fspt_tile<F>());
+}
+
+template <class F>
+__host__ __device__ constexpr int fspt_threads()
+{
+    return fspt_tile<F>() * F::ts;
+}
+
+// CTAs per SM the launch bound asks registers for: three small CTAs, or one of up to 1024 threads
+template <class F>
+__host__ __device__ constexpr int fspt_min_ctas()
+{
+    return fspt_threads<F>() <= 256 ? 3 : 1;
+}
+
+// loads the S x N box of tile coordinates (x floats, y0 rows) as boxes of at most 256 rows
+template <int S, int N>
+__device__ __forceinline__ void fspt_load(void* dst, const tensor_map* tm, int x, int y0, uint64_t* bar)
+{
+    constexpr int BR = N < 256 ? N : 256;
+    mbar_arrive_expect_tx(bar, uint32_t(S * N * 8));
+#pragma unroll 1
+    for (int b = 0; b < N / BR; b++)
+        tensor_g2s_2d(static_cast<char*>(dst) + b * BR * S * 8, tm, x, y0 + b * BR, bar);
 }
 
 template <typename T, class FA, int N2>
-__global__ void __launch_bounds__(16 * FA::ts, 3)
+__global__ void __launch_bounds__(fspt_threads<FA>(), fspt_min_ctas<FA>())
     k_fspt_cols(const fourstep_args a, const __grid_constant__ tensor_map tm_in, const long long ntiles, int* err)
 {
-    static_assert(fspt_ok<FA>(), "two-pass length of at most 256 on 16-column tiles");
-    constexpr int N1 = FA::n, GA = FA::gstride(), TS = FA::ts, S = 16;
+    static_assert(fspt_ok<FA>(), "two or three passes on tiles of 16 or 8 columns");
+    constexpr int N1 = FA::n, GA = FA::gstride(), TS = FA::ts, S = fspt_tile<FA>();
     constexpr int NTC = (N2 + S - 1) / S;
-    constexpr int SE  = (S * N1 * 8 + 1023) / 1024 * 128; // box elements, rounded to 1024 bytes
+    constexpr int SE  = fspt_stage_elems<FA>(S);
     constexpr int LB  = lbits_for<N1 * N2>();
-    constexpr int NSL = N1 / FA::rlast;                   // last pass: butterfly j makes outputs j + r NSL
-    static_assert((N1 * 8) % 16 == 0, "whole columns are bulk-copied");
+    constexpr int NSL = N1 / FA::rlast; // last pass: butterfly j makes outputs j + r NSL
+    constexpr bool three = FA::npass == 3;
+    static_assert(three || (N1 * 8) % 16 == 0, "whole columns are bulk-copied");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T>* st0    = reinterpret_cast<cpx<T>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     cpx<T>* B      = st0 + 2 * SE;
@@ -1123,7 +1177,6 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
     const cpx<T>* twB = reinterpret_cast<const cpx<T>*>(a.twB);
     const cpx<T>* tw  = reinterpret_cast<const cpx<T>*>(a.tw);
     const FA fa(nullptr, a.d, TS);
-    constexpr uint32_t bytes = S * N1 * 8;
     if (threadIdx.x == 0)
     {
         mbar_init(&bars[0], 1);
@@ -1133,10 +1186,7 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
     __syncthreads();
     long long t = blockIdx.x;
     if (threadIdx.x == 0 && t < ntiles)
-    {
-        mbar_arrive_expect_tx(&bars[0], bytes);
-        tensor_g2s_2d(st0, &tm_in, int(t % NTC) * 2 * S, int(t / NTC) * N1, &bars[0]);
-    }
+        fspt_load<S, N1>(st0, &tm_in, int(t % NTC) * 2 * S, int(t / NTC) * N1, &bars[0]);
     for (int it = 0; t < ntiles; t += gridDim.x, it++)
     {
         const int s    = it & 1;
@@ -1154,15 +1204,16 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
         const long long tn = t + gridDim.x;
         if (threadIdx.x == 0 && tn < ntiles)
         {
-            // the other stage holds the previous tile's output: wait until its store has read it
+            // the other stage holds the previous tile's output (or its A buffer): once its bulk store, if
+            // any, has read it, stream the next tile in
             bulk_wait_read();
             fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&bars[s ^ 1], bytes);
-            tensor_g2s_2d(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTC) * 2 * S, int(tn / NTC) * N1, &bars[s ^ 1]);
+            fspt_load<S, N1>(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTC) * 2 * S, int(tn / NTC) * N1, &bars[s ^ 1]);
         }
         const long long b = t / NTC;
         const int c0      = int(t % NTC) * S;
         const int col     = c0 + g;
+        cpx<T>* y         = reinterpret_cast<cpx<T>*>(a.out) + b * (long long)N1 * N2;
         // four-step twiddle W_N^{col k1} on the last pass's outputs k1 = j + r NSL: W_N^{col j} times powers
         // of the tile's step W_N^{col NSL}
         const cpx<T> step = twiddle_2level(twA, twB, (long long)(col * NSL), LB);
@@ -1174,17 +1225,31 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
             for (int r = 0; r < FA::rlast; r++)
                 o[r] = o[r] * w;
         };
-        // pass 1 reads the box; pass 2 writes the tile's 16 output columns (contiguous in y) over it
-        fa.run_pp_post([&](int p) { return conj_if(stage[swz128_8b(p, g)], cin); }, post,
-                       [&](int k1, cpx<T> v) { stage[g * N1 + k1] = conj_if(v, cout); }, stage, B + g * GA, tw, lt);
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (threadIdx.x == 0)
+        const auto ld = [&](int p) { return conj_if(stage[swz_8b<S>(p, g)], cin); };
+        if constexpr (three)
         {
-            const int ncols = N2 % S == 0 ? S : (N2 - c0 < S ? N2 - c0 : S);
-            bulk_s2g(reinterpret_cast<cpx<T>*>(a.out) + b * (long long)N1 * N2 + (long long)c0 * N1, stage,
-                     uint32_t(ncols * N1 * 8));
-            bulk_commit();
+            // the box (consumed by pass 1) is the A buffer of pass 2; the last pass stores to global memory
+            fa.run_pp_post(ld, post,
+                           [&](int k1, cpx<T> v)
+                           {
+                               if (N2 % S == 0 || col < N2)
+                                   y[(long long)col * N1 + k1] = conj_if(v, cout);
+                           },
+                           stage + g * GA, B + g * GA, tw, lt);
+        }
+        else
+        {
+            // pass 1 reads the box; pass 2 writes the tile's S output columns (contiguous in y) over it
+            fa.run_pp_post(ld, post, [&](int k1, cpx<T> v) { stage[g * N1 + k1] = conj_if(v, cout); }, stage,
+                           B + g * GA, tw, lt);
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                const int ncols = N2 % S == 0 ? S : (N2 - c0 < S ? N2 - c0 : S);
+                bulk_s2g(y + (long long)c0 * N1, stage, uint32_t(ncols * N1 * 8));
+                bulk_commit();
+            }
         }
     }
     if (threadIdx.x == 0)
@@ -1192,25 +1257,28 @@ __global__ void __launch_bounds__(16 * FA::ts, 3)
 }
 
 template <typename T, class FB, int N1>
-__global__ void __launch_bounds__(16 * FB::ts, 3)
+__global__ void __launch_bounds__(fspt_threads<FB>(), fspt_min_ctas<FB>())
     k_fspt_rows(const fourstep_args a, const __grid_constant__ tensor_map tm_in,
                 const __grid_constant__ tensor_map tm_out, const long long ntiles, int* err)
 {
-    static_assert(fspt_ok<FB>(), "two-pass length of at most 256 on 16-row tiles");
-    constexpr int N2 = FB::n, GB = FB::gstride(), TS = FB::ts, S = 16;
+    static_assert(fspt_ok<FB>(), "two or three passes on tiles of 16 or 8 rows");
+    constexpr int N2 = FB::n, GB = FB::gstride(), TS = FB::ts, S = fspt_tile<FB>();
     constexpr int NTR = (N1 + S - 1) / S;
-    constexpr int SE  = (S * N2 * 8 + 1023) / 1024 * 128;
+    constexpr int SE  = fspt_stage_elems<FB>(S);
+    constexpr int BR  = N2 < 256 ? N2 : 256;
+    constexpr bool three = FB::npass == 3;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T>* st0    = reinterpret_cast<cpx<T>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     cpx<T>* B      = st0 + 2 * SE;
     uint64_t* bars = reinterpret_cast<uint64_t*>(B + S * GB);
     const bool cin = a.conj_in != 0, cout = a.conj_out != 0;
-    const int g    = int(threadIdx.x) / TS;
-    const int lt   = int(threadIdx.x) - g * TS;
-    const cpx<T>* tw   = reinterpret_cast<const cpx<T>*>(a.tw);
+    // two passes: the S threads' groups are contiguous (each row's TS threads together); three passes: rows
+    // fastest, so that a warp's last-pass stores cover S consecutive outputs
+    const int g  = three ? int(threadIdx.x) % S : int(threadIdx.x) / TS;
+    const int lt = three ? int(threadIdx.x) / S : int(threadIdx.x) - g * TS;
+    const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
     const auto nothing = []() {};
     const FB fb(nullptr, a.d, TS);
-    constexpr uint32_t bytes = S * N2 * 8;
     if (threadIdx.x == 0)
     {
         mbar_init(&bars[0], 1);
@@ -1220,10 +1288,7 @@ __global__ void __launch_bounds__(16 * FB::ts, 3)
     __syncthreads();
     long long t = blockIdx.x;
     if (threadIdx.x == 0 && t < ntiles)
-    {
-        mbar_arrive_expect_tx(&bars[0], bytes);
-        tensor_g2s_2d(st0, &tm_in, int(t % NTR) * 2 * S, int(t / NTR) * N2, &bars[0]);
-    }
+        fspt_load<S, N2>(st0, &tm_in, int(t % NTR) * 2 * S, int(t / NTR) * N2, &bars[0]);
     for (int it = 0; t < ntiles; t += gridDim.x, it++)
     {
         const int s    = it & 1;
@@ -1241,22 +1306,40 @@ __global__ void __launch_bounds__(16 * FB::ts, 3)
         const long long tn = t + gridDim.x;
         if (threadIdx.x == 0 && tn < ntiles)
         {
-            // the other stage holds the previous tile's output: wait until its store has read it
+            // the other stage holds the previous tile's output (or its A buffer): once its store, if any, has
+            // read it, stream the next tile in
             bulk_wait_read();
             fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&bars[s ^ 1], bytes);
-            tensor_g2s_2d(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTR) * 2 * S, int(tn / NTR) * N2, &bars[s ^ 1]);
+            fspt_load<S, N2>(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTR) * 2 * S, int(tn / NTR) * N2, &bars[s ^ 1]);
         }
-        // pass 1 reads the box, pass 2 writes the transformed rows back into it (same swizzled layout)
-        fb.run_pp([&](int p) { return conj_if(stage[swz128_8b(p, g)], cin); },
-                  [&](int k2, cpx<T> v) { stage[swz128_8b(k2, g)] = conj_if(v, cout); }, nothing, nothing, stage,
-                  B + g * GB, tw, lt);
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (threadIdx.x == 0)
+        const auto ld = [&](int p) { return conj_if(stage[swz_8b<S>(p, g)], cin); };
+        if constexpr (three)
         {
-            tensor_s2g_2d(&tm_out, int(t % NTR) * 2 * S, int(t / NTR) * N2, stage);
-            bulk_commit();
+            const long long b = t / NTR;
+            const int r       = int(t % NTR) * S + g;
+            cpx<T>* X         = reinterpret_cast<cpx<T>*>(a.out) + b * (long long)N1 * N2;
+            fb.run_pp(ld,
+                      [&](int k2, cpx<T> v)
+                      {
+                          if (N1 % S == 0 || r < N1)
+                              X[r + (long long)N1 * k2] = conj_if(v, cout);
+                      },
+                      nothing, nothing, stage + g * GB, B + g * GB, tw, lt);
+        }
+        else
+        {
+            // pass 1 reads the box, pass 2 writes the transformed rows back into it (same swizzled layout)
+            fb.run_pp(ld, [&](int k2, cpx<T> v) { stage[swz_8b<S>(k2, g)] = conj_if(v, cout); }, nothing, nothing,
+                      stage, B + g * GB, tw, lt);
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+#pragma unroll 1
+                for (int bx = 0; bx < N2 / BR; bx++)
+                    tensor_s2g_2d(&tm_out, int(t % NTR) * 2 * S, int(t / NTR) * N2 + bx * BR, stage + bx * BR * S);
+                bulk_commit();
+            }
         }
     }
     if (threadIdx.x == 0)

@@ -88,20 +88,22 @@ static_assert(sizeof(tensor_map) == sizeof(CUtensorMap) && alignof(tensor_map) =
               "tensor_map mirrors CUtensorMap");
 
 // 2-D map over `rows` rows of `row_elems` complex single-precision values (as 2 row_elems floats), box of
-// 16 values x box_rows rows, 128-byte swizzle, zero fill out of range.  False when the base address or the
-// row pitch is not a multiple of 16 bytes, or the encoder refuses.
-static bool map_rows(tensor_map& m, const void* base, long long row_elems, long long rows, int box_rows)
+// S values (S = 16 or 8: 128 or 64 bytes, with the swizzle of that width) x box_rows rows, zero fill out of
+// range.  False when the base address or the row pitch is not a multiple of 16 bytes, or the encoder refuses.
+static bool map_rows(tensor_map& m, const void* base, long long row_elems, long long rows, int box_rows, int S)
 {
     const auto fn = tensor_encoder();
-    if (!fn || reinterpret_cast<uintptr_t>(base) % 16 || (row_elems * 8) % 16 || box_rows > 256 || rows < 1)
+    if (!fn || reinterpret_cast<uintptr_t>(base) % 16 || (row_elems * 8) % 16 || box_rows > 256 || rows < 1 ||
+        (S != 16 && S != 8))
         return false;
     const cuuint64_t dims[2]    = { cuuint64_t(2 * row_elems), cuuint64_t(rows) };
     const cuuint64_t strides[1] = { cuuint64_t(row_elems * 8) };
-    const cuuint32_t box[2]     = { 32, cuuint32_t(box_rows) };
+    const cuuint32_t box[2]     = { cuuint32_t(2 * S), cuuint32_t(box_rows) };
     const cuuint32_t estr[2]    = { 1, 1 };
     return fn(reinterpret_cast<CUtensorMap*>(&m), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims,
-              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              S == 16 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <class K, class... Args>
@@ -131,14 +133,15 @@ static cudaError_t try_fspt_cols(const fourstep_args& a, cudaStream_t st, bool& 
     done = false;
     if constexpr (fspt_ok<FA>())
     {
-        constexpr int N1 = FA::n;
+        constexpr int N1 = FA::n, S = fspt_tile<FA>();
         tensor_map m;
         if (!a.err || a.sig_stride != (long long)N1 * N2 || reinterpret_cast<uintptr_t>(a.out) % 16 ||
-            !map_rows(m, a.in, N2, N1 * a.batch, N1))
+            !map_rows(m, a.in, N2, N1 * a.batch, N1 < 256 ? N1 : 256, S))
             return cudaSuccess;
         done = true;
-        return go_fspt(k_fspt_cols<float, FA, N2>, 16 * FA::ts, fspt_smem<FA>(), a.batch * ((N2 + 15) / 16), st, a,
-                       m, a.batch * ((N2 + 15) / 16), a.err);
+        const long long ntiles = a.batch * ((N2 + S - 1) / S);
+        return go_fspt(k_fspt_cols<float, FA, N2>, fspt_threads<FA>(), fspt_smem<FA>(), ntiles, st, a, m, ntiles,
+                       a.err);
     }
     return cudaSuccess;
 }
@@ -149,14 +152,19 @@ static cudaError_t try_fspt_rows(const fourstep_args& a, cudaStream_t st, bool& 
     done = false;
     if constexpr (fspt_ok<FB>())
     {
-        constexpr int N2 = FB::n;
+        constexpr int N2 = FB::n, S = fspt_tile<FB>(), BR = N2 < 256 ? N2 : 256;
+        // the three-pass kernel stores from its last pass: no output map (the input map fills the slot)
         tensor_map mi, mo;
-        if (!a.err || a.sig_stride != (long long)N1 * N2 || !map_rows(mi, a.in, N1, N2 * a.batch, N2) ||
-            !map_rows(mo, a.out, N1, N2 * a.batch, N2))
+        if (!a.err || a.sig_stride != (long long)N1 * N2 || !map_rows(mi, a.in, N1, N2 * a.batch, BR, S))
+            return cudaSuccess;
+        if (FB::npass == 3)
+            mo = mi;
+        else if (!map_rows(mo, a.out, N1, N2 * a.batch, BR, S))
             return cudaSuccess;
         done = true;
-        return go_fspt(k_fspt_rows<float, FB, N1>, 16 * FB::ts, fspt_smem<FB>(), a.batch * ((N1 + 15) / 16), st, a,
-                       mi, mo, a.batch * ((N1 + 15) / 16), a.err);
+        const long long ntiles = a.batch * ((N1 + S - 1) / S);
+        return go_fspt(k_fspt_rows<float, FB, N1>, fspt_threads<FB>(), fspt_smem<FB>(), ntiles, st, a, mi, mo, ntiles,
+                       a.err);
     }
     return cudaSuccess;
 }

@@ -159,11 +159,14 @@ def test_one_signal_per_cta_persistent(orc, n, batch):
     assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
 
 
-@pytest.mark.parametrize("n,batch", [(30720, 300), (24000, 200), (65536, 150)])
+@pytest.mark.parametrize("n,batch", [(30720, 300), (24000, 200), (65536, 150), (1 << 18, 40), (1 << 20, 12),
+                                     (22050, 200)])
 def test_fourstep_pair_tiles_many_per_cta(orc, n, batch):
     """Four-step lengths whose column and row passes run as persistent kernels fed by 2-D tensor copies
-    (160 x 192, 150 x 160, 256 x 256): several tiles per CTA, ragged row tiles (150 rows in tiles of 16),
-    forward, inverse, in place, and from an 8-byte-misaligned pointer (which takes the per-tile kernels)."""
+    (160 x 192, 150 x 160, 256 x 256 in two passes; 512 x 512 on 16-wide and 1024 x 1024 on 8-wide tiles in
+    three passes, boxes of 256 rows; the 147-point column pass of 147 x 150): several tiles per CTA, ragged row
+    tiles (150 rows in tiles of 16), forward, inverse, in place, and from an 8-byte-misaligned pointer (which
+    takes the per-tile kernels)."""
     rng = np.random.default_rng(n + batch)
     x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
     pick = np.r_[0:2, batch // 2, batch - 2:batch]
