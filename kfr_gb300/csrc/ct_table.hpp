@@ -81,7 +81,9 @@
     X(512, 512)                                                                                              \
     X(1024, 1024)                                                                                            \
     X(147, 150)                                                                                              \
-    X(150, 160)
+    X(150, 160)                                                                                              \
+    X(2048, 2048)                                                                                            \
+    X(4096, 4096)
 
 // Shared-memory layout of a compile-time length (single precision): X(N, TS, pad shift, extra group stride).
 // Element i of a signal sits at i + (i >> shift) (shift 0: unpadded), signals of a CTA lie `stride` elements

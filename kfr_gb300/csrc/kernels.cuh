@@ -1078,9 +1078,9 @@ __global__ void __launch_bounds__(1024, 1) k_fsp_rows(const fourstep_args a)
 
 // ---------------------------------------------------------------------------------------------------
 // Four-step pair kernels, persistent, with 2-D tensor copies (TMA).  Same transforms as k_fsp_cols /
-// k_fsp_rows for lengths of two or three passes: a tile is S columns (rows) of the signal, S = 16 or 8
-// contiguous 8-byte elements (128 or 64 bytes) per row, loaded as one box per 256 rows with the matching
-// swizzle (conflict-free column reads) and double buffered: the next tile streams in while the CTA
+// k_fsp_rows for lengths of two or three passes: a tile is S columns (rows) of the signal, S = 16, 8, 4 or 2
+// contiguous 8-byte elements (128 to 16 bytes) per row, loaded as one box per 256 rows with the matching
+// swizzle (128, 64, 32 bytes; none for 16) and double buffered: the next tile streams in while the CTA
 // transforms the current one.  Waits are bounded; one that runs out sets *err and the CTA returns.
 //   column pass: the four-step twiddle per butterfly of the last pass; two passes: the tile's S output
 //     columns (contiguous in the intermediate) are written over the box and stored by one bulk copy; three
@@ -1106,13 +1106,13 @@ __host__ __device__ constexpr int fspt_smem_s(int S)
     return 2 * fspt_stage_elems<F>(S) * 8 + S * F::gstride() * 8 + 16 + 1024;
 }
 
-// tile width: the widest of 16 and 8 whose threads and shared memory fit (0: none)
+// tile width: the widest of 16, 8, 4 and 2 whose threads and shared memory fit (0: none)
 template <class F>
 __host__ __device__ constexpr int fspt_tile()
 {
     if (!(F::npass == 2 || F::npass == 3) || !(F::n <= 256 || F::n % 256 == 0))
         return 0;
-    for (int S = 16; S >= 8; S /= 2)
+    for (int S = 16; S >= 2; S /= 2)
         if (S * F::ts <= 1024 && fspt_smem_s<F>(S) <= kFspSmem)
             return S;
     return 0;
@@ -1158,7 +1158,7 @@ template <typename T, class FA, int N2>
 __global__ void __launch_bounds__(fspt_threads<FA>(), fspt_min_ctas<FA>())
     k_fspt_cols(const fourstep_args a, const __grid_constant__ tensor_map tm_in, const long long ntiles, int* err)
 {
-    static_assert(fspt_ok<FA>(), "two or three passes on tiles of 16 or 8 columns");
+    static_assert(fspt_ok<FA>(), "two or three passes on tiles of 16 to 2 columns");
     constexpr int N1 = FA::n, GA = FA::gstride(), TS = FA::ts, S = fspt_tile<FA>();
     constexpr int NTC = (N2 + S - 1) / S;
     constexpr int SE  = fspt_stage_elems<FA>(S);
@@ -1261,7 +1261,7 @@ __global__ void __launch_bounds__(fspt_threads<FB>(), fspt_min_ctas<FB>())
     k_fspt_rows(const fourstep_args a, const __grid_constant__ tensor_map tm_in,
                 const __grid_constant__ tensor_map tm_out, const long long ntiles, int* err)
 {
-    static_assert(fspt_ok<FB>(), "two or three passes on tiles of 16 or 8 rows");
+    static_assert(fspt_ok<FB>(), "two or three passes on tiles of 16 to 2 rows");
     constexpr int N2 = FB::n, GB = FB::gstride(), TS = FB::ts, S = fspt_tile<FB>();
     constexpr int NTR = (N1 + S - 1) / S;
     constexpr int SE  = fspt_stage_elems<FB>(S);

@@ -88,13 +88,14 @@ static_assert(sizeof(tensor_map) == sizeof(CUtensorMap) && alignof(tensor_map) =
               "tensor_map mirrors CUtensorMap");
 
 // 2-D map over `rows` rows of `row_elems` complex single-precision values (as 2 row_elems floats), box of
-// S values (S = 16 or 8: 128 or 64 bytes, with the swizzle of that width) x box_rows rows, zero fill out of
-// range.  False when the base address or the row pitch is not a multiple of 16 bytes, or the encoder refuses.
+// S values (S = 16, 8, 4: 128, 64, 32 bytes with the swizzle of that width; 2: 16 bytes, no swizzle) x
+// box_rows rows, zero fill out of range.  False when the base address or the row pitch is not a multiple of
+// 16 bytes, or the encoder refuses.
 static bool map_rows(tensor_map& m, const void* base, long long row_elems, long long rows, int box_rows, int S)
 {
     const auto fn = tensor_encoder();
     if (!fn || reinterpret_cast<uintptr_t>(base) % 16 || (row_elems * 8) % 16 || box_rows > 256 || rows < 1 ||
-        (S != 16 && S != 8))
+        (S != 16 && S != 8 && S != 4 && S != 2))
         return false;
     const cuuint64_t dims[2]    = { cuuint64_t(2 * row_elems), cuuint64_t(rows) };
     const cuuint64_t strides[1] = { cuuint64_t(row_elems * 8) };
@@ -102,7 +103,11 @@ static bool map_rows(tensor_map& m, const void* base, long long row_elems, long 
     const cuuint32_t estr[2]    = { 1, 1 };
     return fn(reinterpret_cast<CUtensorMap*>(&m), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims,
               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              S == 16 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              S == 16  ? CU_TENSOR_MAP_SWIZZLE_128B
+              : S == 8 ? CU_TENSOR_MAP_SWIZZLE_64B
+              : S == 4 ? CU_TENSOR_MAP_SWIZZLE_32B
+                       : CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -169,6 +174,27 @@ static cudaError_t try_fspt_rows(const fourstep_args& a, cudaStream_t st, bool& 
     return cudaSuccess;
 }
 
+// The per-tile pair kernels where their tiles (at least 8 signals) fit; cudaErrorNotSupported otherwise (the
+// caller then runs the generic four-step kernels).
+template <class FA, class FB, int A, int B>
+static cudaError_t go_fsp_pair(const fourstep_args& a, bool cols, cudaStream_t st)
+{
+    constexpr int SA = fsp_tile(A, FA::ts, kFspSmem), SB = fsp_tile(B, FB::ts, kFspSmem);
+    if (cols)
+    {
+        if constexpr (SA >= 8)
+            return go_fsp(k_fsp_cols<float, FA, B>, dim3((B + SA - 1) / SA, unsigned(a.batch)),
+                          (SA * FA::ts + 31) / 32 * 32, 2 * SA * FA::gstride() * 8, st, a);
+        else
+            return cudaErrorNotSupported;
+    }
+    if constexpr (SB >= 8)
+        return go_fsp(k_fsp_rows<float, FB, A>, dim3((A + SB - 1) / SB, unsigned(a.batch)),
+                      (SB * FB::ts + 31) / 32 * 32, 2 * SB * FB::gstride() * 8, st, a);
+    else
+        return cudaErrorNotSupported;
+}
+
 cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st)
 {
 #define KFR_GPU_FSP_CASE(A, B)                                                                             \
@@ -180,15 +206,7 @@ cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st
         const cudaError_t te = cols ? try_fspt_cols<FA, B>(a, st, done) : try_fspt_rows<FB, A>(a, st, done);   \
         if (done || te != cudaSuccess)                                                                     \
             return te;                                                                                     \
-        if (cols)                                                                                          \
-        {                                                                                                  \
-            constexpr int S = fsp_tile(A, FA::ts, kFspSmem);                                               \
-            return go_fsp(k_fsp_cols<float, FA, B>, dim3((B + S - 1) / S, unsigned(a.batch)),              \
-                          (S * FA::ts + 31) / 32 * 32, 2 * S * FA::gstride() * 8, st, a);                  \
-        }                                                                                                  \
-        constexpr int S = fsp_tile(B, FB::ts, kFspSmem);                                                   \
-        return go_fsp(k_fsp_rows<float, FB, A>, dim3((A + S - 1) / S, unsigned(a.batch)),                  \
-                      (S * FB::ts + 31) / 32 * 32, 2 * S * FB::gstride() * 8, st, a);                      \
+        return go_fsp_pair<FA, FB, A, B>(a, cols, st);                                                     \
     }
     KFR_CT_FSPAIR_F32(KFR_GPU_FSP_CASE)
 #undef KFR_GPU_FSP_CASE

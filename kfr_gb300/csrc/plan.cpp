@@ -830,20 +830,8 @@ bool complex_engine<T>::plan_fourstep(long long n)
     // compile-time passes run ping-pong (two buffers per signal) unless that would shrink a tile below 8
     // signals (short row segments coalesce poorly)
     pp_c_ = pp_r_ = pair_ = false;
-    if (sizeof(T) == 4 && pcols_.ct && prows_.ct && has_ct_fsp_f32(int(n1_), int(n2_)) &&
-        fsp_tile(int(n1_), pcols_.ts, kFspSmem) >= 8 && fsp_tile(int(n2_), prows_.ts, kFspSmem) >= 8 &&
-        2 * fsp_tile(int(n1_), pcols_.ts, kFspSmem) * pcols_.gstride * int(2 * sizeof(T)) <= max_smem_bytes() &&
-        2 * fsp_tile(int(n2_), prows_.ts, kFspSmem) * prows_.gstride * int(2 * sizeof(T)) <= max_smem_bytes())
-    {
-        // both passes fully compile time (their tiles fixed by the kernels)
-        pair_   = true;
-        pp_c_   = pp_r_ = true;
-        tile_c_ = fsp_tile(int(n1_), pcols_.ts, kFspSmem);
-        tile_r_ = fsp_tile(int(n2_), prows_.ts, kFspSmem);
-        err_.alloc(sizeof(int)); // the persistent tensor-copy pair kernels report a copy that never lands
-        check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
-    }
-    if (pcols_.ct && !pair_)
+    // tiles of the generic compile-time passes (run ping-pong unless that would shrink a tile below 8)
+    if (pcols_.ct)
     {
         const int t2 = tile_for(pcols_, 2);
         if (t2 >= 8 || t2 == tile_c_)
@@ -852,7 +840,7 @@ bool complex_engine<T>::plan_fourstep(long long n)
             pp_c_   = true;
         }
     }
-    if (prows_.ct && !pair_)
+    if (prows_.ct)
     {
         const int t2 = tile_for(prows_, 2);
         if (t2 >= 8 || t2 == tile_r_)
@@ -860,6 +848,14 @@ bool complex_engine<T>::plan_fourstep(long long n)
             tile_r_ = t2;
             pp_r_   = true;
         }
+    }
+    // both passes fully compile time (their tiles fixed by the kernels); the generic passes run where the
+    // pair kernels cannot (launch_ct_fsp_f32 then answers cudaErrorNotSupported)
+    if (sizeof(T) == 4 && pcols_.ct && prows_.ct && has_ct_fsp_f32(int(n1_), int(n2_)))
+    {
+        pair_ = true;
+        err_.alloc(sizeof(int)); // the persistent tensor-copy pair kernels report a copy that never lands
+        check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
     }
     // two-level table for W_N^m, m < N
     int lb = 0;
@@ -1051,6 +1047,15 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
     {
         if (istride != n_ || ostride != n_)
             throw std::invalid_argument("internal: four-step needs contiguous signals");
+        // a pair kernel for this pass, or false when neither of them can run (the generic pass runs instead)
+        const auto run_pair = [&](const fourstep_args& fa, bool cols)
+        {
+            const cudaError_t e = launch_ct_fsp_f32(fa, cols, st);
+            if (e == cudaErrorNotSupported)
+                return false;
+            check(e, cols ? "launch four-step columns" : "launch four-step rows");
+            return true;
+        };
         for (long long b0 = 0; b0 < batch; b0 += 65535)
         {
             const long long nb  = std::min<long long>(65535, batch - b0);
@@ -1078,9 +1083,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             a.d        = pcols_.desc;
             a.div_n    = make_fast_div(uint32_t(n1_));
             a.pingpong   = pp_c_;
-            if (pair_)
-                check(launch_ct_fsp_f32(a, true, st), "launch four-step columns");
-            else
+            if (!pair_ || !run_pair(a, true))
             {
                 block_cfg cc = pcols_.cfg_tile(tile_c_);
                 if (pp_c_)
@@ -1099,9 +1102,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             a.d        = prows_.desc;
             a.div_n    = make_fast_div(uint32_t(n2_));
             a.pingpong   = pp_r_;
-            if (pair_)
-                check(launch_ct_fsp_f32(a, false, st), "launch four-step rows");
-            else
+            if (!pair_ || !run_pair(a, false))
             {
                 block_cfg cr = prows_.cfg_tile(tile_r_);
                 if (pp_r_)

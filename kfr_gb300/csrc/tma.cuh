@@ -91,16 +91,19 @@ __device__ __forceinline__ void tensor_s2g_2d(const tensor_map* tm, int x, int y
 // laid out in shared memory by the matching swizzle of 16-byte chunks: chunk c / 2 of row `row` lands at chunk
 // (c / 2) ^ (row % 8) (128-byte swizzle), ^ ((row / 2) % 4) (64-byte) or ^ ((row / 4) % 2) (32-byte).  The box
 // must start on a 1024-byte boundary.
+// S = 2 (16-byte rows) is not swizzled.
 template <int S>
 __device__ __forceinline__ int swz_8b(int row, int col)
 {
-    static_assert(S == 16 || S == 8 || S == 4, "16, 8 or 4 elements per row");
+    static_assert(S == 16 || S == 8 || S == 4 || S == 2, "16, 8, 4 or 2 elements per row");
     if constexpr (S == 16)
         return row * 16 + (col ^ ((row & 7) << 1));
     else if constexpr (S == 8)
         return row * 8 + (col ^ (((row >> 1) & 3) << 1));
-    else
+    else if constexpr (S == 4)
         return row * 4 + (col ^ (((row >> 2) & 1) << 1));
+    else
+        return row * 2 + col;
 }
 
 // Shared -> global bulk copy in this thread's bulk async-group (bytes and both addresses multiples of 16).

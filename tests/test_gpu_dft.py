@@ -160,16 +160,17 @@ def test_one_signal_per_cta_persistent(orc, n, batch):
 
 
 @pytest.mark.parametrize("n,batch", [(30720, 300), (24000, 200), (65536, 150), (1 << 18, 40), (1 << 20, 12),
-                                     (22050, 200)])
+                                     (22050, 200), (1 << 22, 3), (1 << 24, 1)])
 def test_fourstep_pair_tiles_many_per_cta(orc, n, batch):
     """Four-step lengths whose column and row passes run as persistent kernels fed by 2-D tensor copies
-    (160 x 192, 150 x 160, 256 x 256 in two passes; 512 x 512 on 16-wide and 1024 x 1024 on 8-wide tiles in
-    three passes, boxes of 256 rows; the 147-point column pass of 147 x 150): several tiles per CTA, ragged row
+    (160 x 192, 150 x 160, 256 x 256 in two passes; 512 x 512, 1024 x 1024, 2048 x 2048 and 4096 x 4096 on
+    16-, 8-, 4- and 2-wide tiles in three passes, boxes of 256 rows; the 147-point column pass of 147 x 150):
+    several tiles per CTA, ragged row
     tiles (150 rows in tiles of 16), forward, inverse, in place, and from an 8-byte-misaligned pointer (which
     takes the per-tile kernels)."""
     rng = np.random.default_rng(n + batch)
     x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
-    pick = np.r_[0:2, batch // 2, batch - 2:batch]
+    pick = np.unique(np.r_[0:2, batch // 2, batch - 2:batch].clip(0, batch - 1))
     ref = orc.dft(x[pick].astype(np.complex128), threads=8)
     refi = orc.dft(x[pick].astype(np.complex128), inverse=True, threads=8)
     plan = k.dft_plan(n, "f32")
