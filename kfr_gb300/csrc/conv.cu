@@ -39,16 +39,25 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_conv_os(const conv_args a
     T* out           = reinterpret_cast<T*>(a.out) + (long long)ch * a.n;
     const long long base  = b * a.bo;
     const long long limit = a.m1 + a.n;
+    // pairs (x[i0], x[i0 + 1]) with i0 - m1 even come from `in` as one 8-byte load when it is 8-byte aligned
+    const bool in_pairs = ((a.m1 | base) & 1) == 0 && (reinterpret_cast<uintptr_t>(in) & (2 * sizeof(T) - 1)) == 0;
 #pragma unroll 4
     for (int m = threadIdx.x; m < c; m += blockDim.x)
     {
         const long long i0 = base + 2 * m;
-        T v0 = T(0), v1 = T(0);
-        if (i0 < limit)
-            v0 = i0 < a.m1 ? hist[i0] : in[i0 - a.m1];
-        if (i0 + 1 < limit)
-            v1 = i0 + 1 < a.m1 ? hist[i0 + 1] : in[i0 + 1 - a.m1];
-        sm[F::pi(m)] = mk(v0, v1);
+        cpx<T> v;
+        if (in_pairs && i0 >= a.m1 && i0 + 1 < limit)
+            v = *reinterpret_cast<const cpx<T>*>(in + (i0 - a.m1));
+        else
+        {
+            T v0 = T(0), v1 = T(0);
+            if (i0 < limit)
+                v0 = i0 < a.m1 ? hist[i0] : in[i0 - a.m1];
+            if (i0 + 1 < limit)
+                v1 = i0 + 1 < a.m1 ? hist[i0 + 1] : in[i0 + 1 - a.m1];
+            v = mk(v0, v1);
+        }
+        sm[F::pi(m)] = v;
     }
     __syncthreads();
     const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
@@ -81,14 +90,31 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_conv_os(const conv_args a
     }
     __syncthreads();
     fft.run(sm, tw, lt);
-    for (long long t = threadIdx.x; t < a.bo; t += blockDim.x)
+    // outputs j = m1 + t, t < bo: element j / 2 holds (y[j even], -y[j + 1]); with m1, base and bo even and
+    // `out` 8-byte aligned, each pair goes out as one 8-byte store
+    if (((a.m1 | base | a.bo) & 1) == 0 && (reinterpret_cast<uintptr_t>(out) & (2 * sizeof(T) - 1)) == 0)
     {
-        const long long no = base + t;
-        if (no < a.n)
+        for (long long u = threadIdx.x; 2 * u < a.bo; u += blockDim.x)
         {
-            const long long j = a.m1 + t;
-            const cpx<T> v    = sm[F::pi(int(j >> 1))];
-            out[no]           = (j & 1) ? -v.y : v.x;
+            const long long no = base + 2 * u;
+            const cpx<T> v     = sm[F::pi(int((a.m1 >> 1) + u))];
+            if (no + 1 < a.n)
+                *reinterpret_cast<cpx<T>*>(out + no) = mk(v.x, -v.y);
+            else if (no < a.n)
+                out[no] = v.x;
+        }
+    }
+    else
+    {
+        for (long long t = threadIdx.x; t < a.bo; t += blockDim.x)
+        {
+            const long long no = base + t;
+            if (no < a.n)
+            {
+                const long long j = a.m1 + t;
+                const cpx<T> v    = sm[F::pi(int(j >> 1))];
+                out[no]           = (j & 1) ? -v.y : v.x;
+            }
         }
     }
 }
