@@ -675,6 +675,138 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_r2c(const real_args a, co
 }
 
 // ---------------------------------------------------------------------------------------------------
+// Real forward DFT, contiguous batch, persistent and pipelined (compile-time c): tiles of `spc` signals (spc
+// even, so that each tile's input, 2c reals per signal, and output, olen complex bins per signal, are whole
+// 16-byte units).  Three tile buffers rotate: the input tile (bulk copy, then the passes' A buffer), the
+// scratch tile (B) and the spare tile for the next tile's copy, issued after the first pass.  The passes
+// leave Z, the c-point DFT of the reals viewed as complex values, in natural order in one of the two
+// buffers; the split (to_fmt, src/dft/fft-impl.hpp:1799-1841) reads it and writes the tile's spectrum into
+// the other, which one bulk copy stores.  The next tile's input is this one's spare, its scratch the Z
+// buffer, its spare the buffer being stored.  Whole tiles only (the host runs the remainder with k_r2c).  A
+// wait that runs out sets *err and the CTA returns.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__host__ __device__ constexpr int r2c_stage_elems(int spc)
+{
+    // the input tile (spc c complex), the padded work layout, the output tile (up to c + 1 bins per signal)
+    const int a = spc * (F::n + 1), b = spc * F::gstride(F::n);
+    return ((a > b ? a : b) + 15) / 16 * 16;
+}
+
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1)
+    k_r2c_pipe(const real_args a, const long long ntiles, const int spc, int* err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int C      = F::n;
+    constexpr int STRIDE = F::gstride(C);
+    const F fft(nullptr, a.d, F::ts);
+    const int slen       = r2c_stage_elems<T, F>(spc);
+    const int olen       = a.ccs ? C + 1 : C;
+    cpx<T>* const tiles  = reinterpret_cast<cpx<T>*>(smem_raw);
+    uint64_t* bars       = reinterpret_cast<uint64_t*>(tiles + 3 * slen);
+    const uint32_t ibytes = uint32_t(spc) * uint32_t(C) * uint32_t(sizeof(cpx<T>));
+    const uint32_t obytes = uint32_t(spc) * uint32_t(olen) * uint32_t(sizeof(cpx<T>));
+    const cpx<T>* in     = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* out          = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* tw     = reinterpret_cast<const cpx<T>*>(a.tw);
+    const cpx<T>* __restrict__ rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
+    const group_map gm(F::ts, spc);
+    if (threadIdx.x == 0)
+    {
+        for (int b = 0; b < 3; b++)
+            mbar_init(&bars[b], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles)
+    {
+        mbar_arrive_expect_tx(&bars[0], ibytes);
+        bulk_g2s(tiles, in + t * spc * C, ibytes, &bars[0]);
+    }
+    uint32_t phase = 0;         // bit b: parity to wait for on tile buffer b
+    int bi = 0, bs = 1, bn = 2; // input, scratch and spare tile buffers
+    for (; t < ntiles; t += gridDim.x)
+    {
+        cpx<T>* in_t   = tiles + bi * slen;
+        cpx<T>* scr_t  = tiles + bs * slen;
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                bulk_wait_all();
+            }
+            return;
+        }
+        phase ^= 1u << bi;
+        const long long tn  = t + gridDim.x;
+        const auto prefetch = [&]()
+        {
+            if (threadIdx.x == 0 && tn < ntiles)
+            {
+                // the spare buffer holds the previous tile's spectrum: wait until its bulk store has read it
+                bulk_wait_read();
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bars[bn], ibytes);
+                bulk_g2s(tiles + bn * slen, in + tn * spc * C, ibytes, &bars[bn]);
+            }
+        };
+        // pass i writes B (i even) or A (i odd): with an odd pass count the last pass reads A
+        constexpr bool odd = F::npass % 2 == 1;
+        cpx<T>* zb         = odd ? scr_t : in_t; // Z in natural order
+        cpx<T>* xb         = odd ? in_t : scr_t; // the tile's spectrum
+        const cpx<T>* src  = in_t + gm.g * C;
+        cpx<T>* zsig       = zb + gm.g * C;
+        const auto nothing = []() {};
+        fft.run_pp([&](int p) { return src[p]; }, [&](int q, cpx<T> x) { zsig[q] = x; }, prefetch, nothing,
+                   in_t + gm.g * STRIDE, scr_t + gm.g * STRIDE, tw, gm.lt);
+        // the split: bin k of signal s from Z[k] and Z[c - k]
+        for (int i = threadIdx.x; i < spc * olen; i += blockDim.x)
+        {
+            const int s     = int(div_by(uint32_t(i), a.div_out));
+            const int k     = i - s * olen;
+            const cpx<T>* z = zb + s * C;
+            cpx<T> v;
+            if (k == 0)
+            {
+                const cpx<T> z0 = z[0];
+                v = a.ccs ? mk<T>(z0.x + z0.y, 0) : mk<T>(z0.x + z0.y, z0.x - z0.y);
+            }
+            else if (k == C)
+            {
+                const cpx<T> z0 = z[0];
+                v               = mk<T>(z0.x - z0.y, 0);
+            }
+            else
+            {
+                const cpx<T> zk  = z[k];
+                const cpx<T> znk = conj(z[C - k]);
+                const cpx<T> e   = scale(zk + znk, T(0.5));
+                const cpx<T> o   = scale(mul_mi(zk - znk), T(0.5));
+                v                = e + ldg(rtw + k) * o;
+            }
+            xb[i] = v;
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            bulk_s2g(out + t * spc * olen, xb, obytes);
+            bulk_commit();
+        }
+        const int zi = odd ? bs : bi, xi = odd ? bi : bs;
+        bi = bn;
+        bs = zi;
+        bn = xi;
+    }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------------------------------
 // Real inverse DFT: the merge of from_fmt (src/dft/fft-impl.hpp:1852-1896) fused into the load, then an
 // unscaled inverse c-point complex DFT whose output is the 2c reals.  Only the real parts of the DC and
 // Nyquist bins are read, as in the reference.

@@ -184,6 +184,8 @@ cudaError_t launch_ct_c2c_f32(const c2c_args& a, const block_cfg& c, cudaStream_
 // hold two unpadded tiles, the padded work tile and two mbarriers; in must be 16-byte aligned).
 cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long long ntiles, int* err,
                                    cudaStream_t st);
+// real forward DFT, persistent and pipelined over tiles of c.spc (even) signals (compile-time c = n / 2)
+cudaError_t launch_ct_r2c_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st);
 // one signal per CTA, persistent, signal in registers between the passes (compile-time lengths >= 8192)
 cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st);
 cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c, cudaStream_t st);

@@ -1205,6 +1205,34 @@ real_engine<T>::real_engine(long long n) : n_(n), c_(n / 2), ceng_(n / 2)
     fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
     if (fused_)
         prog_.build(int(c_), CT_REAL);
+    // Forward pipelined kernel (compile-time c, single precision): an even number of signals per tile, the
+    // most resident threads per SM with at least two CTAs, then the smallest tile.
+    if (fused_ && prog_.ct && sizeof(T) == 4)
+    {
+        int best = 0, best_thr = 0;
+        for (int spc = 2; spc <= 32; spc += 2)
+        {
+            const int threads = ((spc * prog_.ts + 31) / 32) * 32;
+            if (threads > 1024)
+                break;
+            const int slen = (std::max(spc * int(c_ + 1), spc * prog_.gstride) + 15) / 16 * 16;
+            const int smem = 3 * slen * int(2 * sizeof(T)) + 64;
+            if (smem > smem_budget())
+                break;
+            const int ctas = std::min((max_smem_bytes() + 1024) / (smem + 1024), 1024 / threads);
+            if (ctas >= 2 && ctas * threads > best_thr)
+            {
+                best_thr = ctas * threads;
+                best     = spc;
+            }
+        }
+        if (best)
+        {
+            pipe_spc_ = best;
+            err_.alloc(sizeof(int));
+            check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
+        }
+    }
 }
 
 template <typename T>
@@ -1218,7 +1246,7 @@ long long real_engine<T>::scratch_elems(long long batch) const
 template <typename T>
 int real_engine<T>::launches(long long batch) const
 {
-    return fused_ ? 1 : 1 + ceng_.launches(batch);
+    return fused_ ? ((pipe_spc_ && batch % pipe_spc_) ? 2 : 1) : 1 + ceng_.launches(batch);
 }
 
 template <typename T>
@@ -1260,7 +1288,26 @@ void real_engine<T>::forward(void* out, const void* in, long long batch, bool cc
         a.div_n   = make_fast_div(uint32_t(c_));
         a.div_out = make_fast_div(uint32_t(olen));
         a.d       = p.desc;
-        check(launch_r2c<T>(a, p.cfg(batch), st), "launch r2c");
+        long long done = 0;
+        if (pipe_spc_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0)
+        {
+            const long long ntiles = batch / pipe_spc_;
+            if (ntiles > 0)
+            {
+                block_cfg pc = p.cfg_tile(pipe_spc_);
+                pc.smem = 3 * ((std::max(pipe_spc_ * int(c_ + 1), pipe_spc_ * p.gstride) + 15) / 16 * 16) *
+                              int(2 * sizeof(T)) + 64;
+                check(launch_ct_r2c_pipe_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st), "launch r2c (pipelined)");
+                done = ntiles * pipe_spc_;
+            }
+        }
+        if (done < batch)
+        {
+            a.in    = static_cast<const T*>(in) + done * n_;
+            a.out   = static_cast<std::complex<T>*>(out) + done * olen;
+            a.batch = batch - done;
+            check(launch_r2c<T>(a, p.cfg(batch - done), st), "launch r2c");
+        }
         return;
     }
     char* Z     = static_cast<char*>(scratch);
@@ -1326,8 +1373,10 @@ template <typename T>
 std::string real_engine<T>::describe() const
 {
     std::ostringstream s;
-    s << "real n=" << n_ << (fused_ ? " fused split/merge" : " separate split/merge") << " complex{" << ceng_.describe()
-      << "}";
+    s << "real n=" << n_ << (fused_ ? " fused split/merge" : " separate split/merge");
+    if (pipe_spc_)
+        s << " forward pipelined spc=" << pipe_spc_;
+    s << " complex{" << ceng_.describe() << "}";
     return s.str();
 }
 

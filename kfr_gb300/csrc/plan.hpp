@@ -218,6 +218,8 @@ private:
     block_program<T> prog_; // fused kernels: c-point program
     dbuf rtw_;
     bool fused_ = false;
+    int pipe_spc_ = 0; // forward: signals per tile of the pipelined kernel, 0 = not used
+    dbuf err_;
 };
 
 // dct_plan<T>: DCT-II forward, DCT-III (X0 halved) inverse, unscaled.

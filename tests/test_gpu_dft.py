@@ -321,7 +321,7 @@ def test_real_dft_reference_fixtures(sfx):
 
 
 @pytest.mark.parametrize("n,batch", [(1920, 40), (44100, 3), (48000, 3), (4096, 33), (2048, 17), (2, 5),
-                                     (1 << 16, 2), (2 * 8191, 3), (40000, 2)])
+                                     (1 << 16, 2), (2 * 8191, 3), (40000, 2), (1920, 5001), (8192, 1201)])
 @pytest.mark.parametrize("fmt", ["CCs", "Perm"])
 def test_real_dft_batched_against_oracle(orc, n, batch, fmt):
     rng = np.random.default_rng(n + batch)
