@@ -1,5 +1,6 @@
 // FFT convolution filter kernels and host class (see conv.hpp).
 #include "conv.hpp"
+#include "convolve.hpp"
 #include "kernels.cuh"
 
 #include <algorithm>
@@ -211,9 +212,18 @@ conv_filter<T>::conv_filter(const T* taps, size_t ntaps, size_t block_size, int 
     f                 = std::max<size_t>(f, 64);
     if (f > fmax)
         f = fmax;
+    const size_t hb = std::max<size_t>(1, m1 * size_t(channels)) * sizeof(T);
+    hist_[0].alloc(hb);
+    hist_[1].alloc(hb);
     if (m1 >= f / 2)
-        throw std::invalid_argument("convolution filter: taps longer than " + std::to_string(f / 2) +
-                                    " are not supported by this build");
+    {
+        // long mode: the taps stay on the device for whole-call convolutions
+        long_ = true;
+        f_ = c_ = bo_ = 0;
+        htaps_.upload(h.data(), ntaps * sizeof(T));
+        reset();
+        return;
+    }
     f_  = f;
     c_  = f / 2;
     bo_ = f - m1;
@@ -232,9 +242,6 @@ conv_filter<T>::conv_filter(const T* taps, size_t ntaps, size_t block_size, int 
     }
     hspec_.upload(hs.data(), hs.size() * sizeof(std::complex<T>));
     rtw_.upload(rt.data(), rt.size() * sizeof(std::complex<T>));
-    const size_t hb = std::max<size_t>(1, m1 * size_t(channels)) * sizeof(T);
-    hist_[0].alloc(hb);
-    hist_[1].alloc(hb);
     reset();
 }
 
@@ -249,6 +256,8 @@ void conv_filter<T>::reset()
 template <typename T>
 int conv_filter<T>::launches(size_t n) const
 {
+    if (long_ && n)
+        return 2 + 8 * channels_; // per channel: two pads, two forward and one inverse real FFT, the product
     return (n && m_) ? (m_ > 1 ? 2 : 1) : (n ? 1 : 0);
 }
 
@@ -263,6 +272,30 @@ void conv_filter<T>::process(T* out, const T* in, size_t n, cudaStream_t st)
         return;
     }
     const long long m1 = (long long)m_ - 1;
+    if (long_)
+    {
+        // y = ([history, input] * taps)[m1 + t], t < n, one real-FFT convolution per channel
+        const long long ulen = m1 + (long long)n;
+        lin_.ensure(size_t(ulen) * sizeof(T));
+        lout_.ensure(size_t(ulen + (long long)m_ - 1) * sizeof(T));
+        T* u = static_cast<T*>(lin_.get());
+        T* y = static_cast<T*>(lout_.get());
+        for (int ch = 0; ch < channels_; ch++)
+        {
+            check(cudaMemcpyAsync(u, static_cast<const T*>(hist_[cur_].get()) + ch * m1, size_t(m1) * sizeof(T),
+                                  cudaMemcpyDeviceToDevice, st),
+                  "copy filter history");
+            check(cudaMemcpyAsync(u + m1, in + ch * (long long)n, n * sizeof(T), cudaMemcpyDeviceToDevice, st),
+                  "copy filter input");
+            convolve_device<T>(y, u, ulen, htaps_.get(), (long long)m_, false, 0, st);
+            check(cudaMemcpyAsync(out + ch * (long long)n, y + m1, n * sizeof(T), cudaMemcpyDeviceToDevice, st),
+                  "copy filter output");
+        }
+        check(launch_hist_update<T>(hist_[cur_].get(), hist_[1 - cur_].get(), in, (long long)n, m1, channels_, st),
+              "launch history update");
+        cur_ = 1 - cur_;
+        return;
+    }
     conv_args a;
     a.in       = in;
     a.out      = out;

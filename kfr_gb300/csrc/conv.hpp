@@ -43,7 +43,9 @@ class conv_filter
 {
 public:
     // taps: host or device pointer to `ntaps` values; block_size is the reference's partition size and
-    // only bounds the FFT length from below here (outputs do not depend on it).
+    // only bounds the FFT length from below here (outputs do not depend on it).  Taps too long for one
+    // overlap-save FFT per CTA (M - 1 >= F / 2 at the largest one-CTA F) take the long mode: each call
+    // convolves [history, input] with the taps through one real-FFT convolution per channel.
     conv_filter(const T* taps, size_t ntaps, size_t block_size, int channels = 1);
     // in / out: device pointers to channels x n samples (channel-major).  out must not alias in.
     void process(T* out, const T* in, size_t n, cudaStream_t st);
@@ -51,13 +53,16 @@ public:
     size_t taps() const { return m_; }
     size_t fft_size() const { return f_; }
     int channels() const { return channels_; }
+    bool long_mode() const { return long_; }
     int launches(size_t n) const;
 
 private:
     size_t m_, f_, c_, bo_;
     int channels_;
+    bool long_ = false;
     block_program<T> prog_;
     dbuf hspec_, rtw_, hist_[2];
+    dbuf htaps_, lin_, lout_; // long mode: taps, [history, input] and the full convolution of one channel
     int cur_ = 0;
 };
 

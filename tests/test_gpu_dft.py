@@ -463,6 +463,34 @@ def test_convolve_filter_channels_match_single_channel(orc):
     assert np.allclose(yd.cpu().numpy(), outs[0], rtol=0, atol=1e-5)
 
 
+@pytest.mark.parametrize("sfx,ntaps", [("f32", 20001), ("f64", 5001)])
+def test_convolve_filter_taps_longer_than_one_fft(orc, sfx, ntaps):
+    """Taps too long for one overlap-save FFT per CTA (the reference's multi-segment case, M >> block):
+    whole-call convolutions of [history, input] with the taps, two channels, two streaming calls, reset."""
+    rng = np.random.default_rng(ntaps)
+    rdt = np.float32 if sfx == "f32" else np.float64
+    taps = (rng.standard_normal(ntaps) / np.sqrt(ntaps)).astype(rdt)
+    chans, n = 2, 30000
+    x = rng.standard_normal((chans, 2 * n)).astype(rdt)
+    f = k.convolve_filter(taps, 1024, dtype=sfx, channels=chans)
+    outs = []
+    for part in (0, 1):
+        xd = dev(np.ascontiguousarray(x[:, part * n:(part + 1) * n]))
+        yd = torch.empty_like(xd)
+        f.apply(yd, xd)
+        outs.append(yd.cpu().numpy())
+    got = np.concatenate(outs, axis=1)
+    tol_f = c32_tolerance if sfx == "f32" else c64_tolerance
+    for c in range(chans):
+        ref = orc.filter(taps.astype(np.float64), 1024).process(x[c].astype(np.float64))
+        assert rel_rms(got[c], ref) <= 8 * tol_f(2 * n + ntaps), c
+    f.reset()
+    xd = dev(np.ascontiguousarray(x[:, :n]))
+    yd = torch.empty_like(xd)
+    f.apply(yd, xd)
+    assert rel_rms(yd.cpu().numpy(), outs[0]) <= 8 * tol_f(n + ntaps)
+
+
 def test_convolve_filter_long_signal_device(orc):
     """1023-tap filter over 2^18 samples in device memory, against the streaming oracle."""
     rng = np.random.default_rng(11)
