@@ -27,6 +27,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -83,7 +84,7 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"kfr_gb300_clocks_gpu{gpu_index}_{os.getpid()}.csv")
 
     def start(self):
         try:
@@ -293,7 +294,7 @@ def measure_rows(torch, k, dev, stream, hbm, with_cpu):
             xs = x.cpu().numpy().reshape(1, n)
             rows[name]["cpu_port_gbs"] = cpu(lambda: orc.dft(xs, precision="f32", threads=threads), nb)
         del x, y, tmp, plan
-    # power-of-two lengths 2^10 .. 2^24, 1 GiB batches (the north-star's range for the 70% target)
+    # power-of-two lengths 2^10 .. 2^24, 1 GiB batches
     pw = {}
     for e in (10, 12, 14, 16, 18, 20, 22, 24):
         n = 1 << e

@@ -70,7 +70,8 @@ static cudaError_t go_fsp(K kernel, dim3 grid, int threads, int smem, cudaStream
     return cudaGetLastError();
 }
 
-// cuTensorMapEncodeTiled, looked up once from the driver through the runtime (no link-time dependency)
+// cuTensorMapEncodeTiled, looked up once through the runtime's driver entry-point query (no link-time
+// dependency on the CUDA driver library)
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {

@@ -60,7 +60,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
                  : "memory");
 }
 
-// Opaque 128-byte tensor map (the driver's CUtensorMap layout), passed to kernels as a __grid_constant__
+// Opaque 128-byte tensor map (the CUDA driver API's CUtensorMap layout), passed to kernels as a __grid_constant__
 // parameter.
 struct alignas(128) tensor_map
 {

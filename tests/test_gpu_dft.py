@@ -3,7 +3,7 @@
 Checked against:
   * the golden fixtures produced by KFR 7.0.1 itself (tests/golden/), at every length they hold;
   * the CPU oracle (oracle/, pinned to the same fixtures) at lengths and batches the fixtures do not hold.
-Tolerances are the benchmark spec's bounds on relative RMS error against a double-precision reference:
+Tolerances bound the relative RMS error against a double-precision reference:
   c32: 2 * log2(N) * 2^-24        c64: 4 * log2(N) * 2^-53   (N >= 2)
 """
 import numpy as np
