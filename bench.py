@@ -229,6 +229,11 @@ def measure_rows(torch, k, dev, stream, hbm, with_cpu):
             "frac": round(nb / (ms * 1e-3) / 1e9 / hbm, 4),
             "cpu_port_gbs": cpu(lambda: orc.dft_real(xs, precision="f32", threads=threads),
                                 len(xs) * (4 * n + 8 * (n // 2 + 1)))}
+        if n == 1920:
+            # the inverse (CCs spectrum -> reals) on the same batch
+            ms_i = timed(lambda: plan.execute_batch(x, y, b, inverse=True, stream=stream))
+            rows[f"real_dft_inverse_{n}"] = {"batch": b, "ms": round(ms_i, 4), "gbs": round(nb / (ms_i * 1e-3) / 1e9, 1),
+                                             "frac": round(nb / (ms_i * 1e-3) / 1e9 / hbm, 4)}
         del x, y, plan
     # DCT-II of 4096 x 512 (16 MiB: L2 flushed between repetitions)
     b, n = 4096, 512

@@ -865,6 +865,124 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2r(const real_args a, co
 }
 
 // ---------------------------------------------------------------------------------------------------
+// Real inverse DFT, contiguous batch, persistent and pipelined (compile-time c): tiles of `spc` signals (spc
+// even: each tile's input, ilen complex bins per signal, and output, 2c reals per signal, are whole 16-byte
+// units).  Three tile buffers rotate as in k_r2c_pipe: the input tile arrives by bulk copy; the merge
+// (from_fmt, src/dft/fft-impl.hpp:1852-1896) writes conj(Z) in natural order into the scratch tile; the
+// passes ping-pong between the scratch and input tiles, the last one writing the conjugated output (the 2c
+// reals as c complex values) into the buffer it does not read, which one bulk copy stores.  The next tile's
+// copy is issued after the first pass.  Whole tiles only (the host runs the remainder with k_c2r).  A wait
+// that runs out sets *err and the CTA returns.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__global__ void __launch_bounds__(F::max_threads, 1)
+    k_c2r_pipe(const real_args a, const long long ntiles, const int spc, int* err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int C      = F::n;
+    constexpr int STRIDE = F::gstride(C);
+    const F fft(nullptr, a.d, F::ts);
+    const int slen       = r2c_stage_elems<T, F>(spc);
+    const int ilen       = a.ccs ? C + 1 : C;
+    cpx<T>* const tiles  = reinterpret_cast<cpx<T>*>(smem_raw);
+    uint64_t* bars       = reinterpret_cast<uint64_t*>(tiles + 3 * slen);
+    const uint32_t ibytes = uint32_t(spc) * uint32_t(ilen) * uint32_t(sizeof(cpx<T>));
+    const uint32_t obytes = uint32_t(spc) * uint32_t(C) * uint32_t(sizeof(cpx<T>));
+    const cpx<T>* in     = reinterpret_cast<const cpx<T>*>(a.in);
+    cpx<T>* out          = reinterpret_cast<cpx<T>*>(a.out);
+    const cpx<T>* tw     = reinterpret_cast<const cpx<T>*>(a.tw);
+    const cpx<T>* __restrict__ rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
+    const group_map gm(F::ts, spc);
+    if (threadIdx.x == 0)
+    {
+        for (int b = 0; b < 3; b++)
+            mbar_init(&bars[b], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles)
+    {
+        mbar_arrive_expect_tx(&bars[0], ibytes);
+        bulk_g2s(tiles, in + t * spc * ilen, ibytes, &bars[0]);
+    }
+    uint32_t phase = 0;         // bit b: parity to wait for on tile buffer b
+    int bi = 0, bs = 1, bn = 2; // input, scratch and spare tile buffers
+    for (; t < ntiles; t += gridDim.x)
+    {
+        cpx<T>* in_t   = tiles + bi * slen;
+        cpx<T>* scr_t  = tiles + bs * slen;
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                bulk_wait_all();
+            }
+            return;
+        }
+        phase ^= 1u << bi;
+        // the merge: conj(Z[k]) of signal s from bins k and c - k
+        for (int i = threadIdx.x; i < spc * C; i += blockDim.x)
+        {
+            const int s     = int(div_by(uint32_t(i), a.div_n));
+            const int k     = i - s * C;
+            const cpx<T>* X = in_t + s * ilen;
+            cpx<T> z;
+            if (k == 0)
+            {
+                const T x0 = X[0].x;
+                const T xn = a.ccs ? X[C].x : X[0].y;
+                z          = mk<T>(x0 + xn, x0 - xn);
+            }
+            else
+            {
+                const cpx<T> xk  = X[k];
+                const cpx<T> xnk = conj(X[C - k]);
+                z                = (xk + xnk) + mul_pi(conj(ldg(rtw + k)) * (xk - xnk));
+            }
+            scr_t[i] = conj(z);
+        }
+        __syncthreads();
+        const long long tn  = t + gridDim.x;
+        const auto prefetch = [&]()
+        {
+            if (threadIdx.x == 0 && tn < ntiles)
+            {
+                // the spare buffer holds the previous tile's output: wait until its bulk store has read it
+                bulk_wait_read();
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bars[bn], ibytes);
+                bulk_g2s(tiles + bn * slen, in + tn * spc * ilen, ibytes, &bars[bn]);
+            }
+        };
+        // passes: A = scratch (holding conj(Z)), B = input tile; pass i writes B (i even) or A (i odd), so
+        // with an odd pass count the last pass reads A and writes the output into the input tile
+        constexpr bool odd = F::npass % 2 == 1;
+        cpx<T>* ob         = odd ? in_t : scr_t;
+        const cpx<T>* zsig = scr_t + gm.g * C;
+        cpx<T>* osig       = ob + gm.g * C;
+        const auto nothing = []() {};
+        fft.run_pp([&](int p) { return zsig[p]; }, [&](int q, cpx<T> x) { osig[q] = conj(x); }, prefetch, nothing,
+                   scr_t + gm.g * STRIDE, in_t + gm.g * STRIDE, tw, gm.lt);
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            bulk_s2g(out + t * spc * C, ob, obytes);
+            bulk_commit();
+        }
+        const int oi = odd ? bi : bs, fi = odd ? bs : bi;
+        bi = bn;
+        bs = fi;
+        bn = oi;
+    }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------------------------------
 // DCT-II (dct_plan::execute, include/kfr/dft/fft.hpp:938-950): even/odd mirror on load, n-point DFT,
 // Re*cos + Im*sin on store.
 // ---------------------------------------------------------------------------------------------------

@@ -129,6 +129,19 @@ cudaError_t launch_ct_r2c_pipe_f32(const real_args& a, const block_cfg& c, long 
 #undef KFR_GPU_R2C_PIPE_CASE
 }
 
+cudaError_t launch_ct_c2r_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
+{
+#define KFR_GPU_C2R_PIPE_CASE(N, TS, ...)                                                                  \
+    case N:                                                                                                \
+        return go_persistent(k_c2r_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);
+    switch (c.ct)
+    {
+        KFR_CT_REAL_F32(KFR_GPU_C2R_PIPE_CASE)
+    default: return cudaErrorInvalidValue;
+    }
+#undef KFR_GPU_C2R_PIPE_CASE
+}
+
 cudaError_t launch_ct_rader_tile_f32(const rader_args& a, const block_cfg& c, long long ntiles, int* err,
                                      cudaStream_t st)
 {

@@ -186,6 +186,8 @@ cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long l
                                    cudaStream_t st);
 // real forward DFT, persistent and pipelined over tiles of c.spc (even) signals (compile-time c = n / 2)
 cudaError_t launch_ct_r2c_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st);
+// real inverse DFT, persistent and pipelined over tiles of c.spc (even) signals (compile-time c = n / 2)
+cudaError_t launch_ct_c2r_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st);
 // one signal per CTA, persistent, signal in registers between the passes (compile-time lengths >= 8192)
 cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st);
 cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c, cudaStream_t st);

@@ -1205,8 +1205,8 @@ real_engine<T>::real_engine(long long n) : n_(n), c_(n / 2), ceng_(n / 2)
     fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
     if (fused_)
         prog_.build(int(c_), CT_REAL);
-    // Forward pipelined kernel (compile-time c, single precision): an even number of signals per tile, the
-    // most resident threads per SM with at least two CTAs, then the smallest tile.
+    // Pipelined forward and inverse kernels (compile-time c, single precision): an even number of signals
+    // per tile, the most resident threads per SM with at least two CTAs, then the smallest tile.
     if (fused_ && prog_.ct && sizeof(T) == 4)
     {
         int best = 0, best_thr = 0;
@@ -1349,7 +1349,26 @@ void real_engine<T>::inverse(void* out, const void* in, long long batch, bool cc
         a.div_n   = make_fast_div(uint32_t(c_));
         a.div_out = make_fast_div(uint32_t(c_));
         a.d       = p.desc;
-        check(launch_c2r<T>(a, p.cfg(batch), st), "launch c2r");
+        long long done = 0;
+        if (pipe_spc_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0)
+        {
+            const long long ntiles = batch / pipe_spc_;
+            if (ntiles > 0)
+            {
+                block_cfg pc = p.cfg_tile(pipe_spc_);
+                pc.smem = 3 * ((std::max(pipe_spc_ * int(c_ + 1), pipe_spc_ * p.gstride) + 15) / 16 * 16) *
+                              int(2 * sizeof(T)) + 64;
+                check(launch_ct_c2r_pipe_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st), "launch c2r (pipelined)");
+                done = ntiles * pipe_spc_;
+            }
+        }
+        if (done < batch)
+        {
+            a.in    = static_cast<const std::complex<T>*>(in) + done * ilen;
+            a.out   = static_cast<T*>(out) + done * n_;
+            a.batch = batch - done;
+            check(launch_c2r<T>(a, p.cfg(batch - done), st), "launch c2r");
+        }
         return;
     }
     char* Z     = static_cast<char*>(scratch);
@@ -1375,7 +1394,7 @@ std::string real_engine<T>::describe() const
     std::ostringstream s;
     s << "real n=" << n_ << (fused_ ? " fused split/merge" : " separate split/merge");
     if (pipe_spc_)
-        s << " forward pipelined spc=" << pipe_spc_;
+        s << " pipelined spc=" << pipe_spc_;
     s << " complex{" << ceng_.describe() << "}";
     return s.str();
 }

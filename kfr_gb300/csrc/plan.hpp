@@ -218,7 +218,7 @@ private:
     block_program<T> prog_; // fused kernels: c-point program
     dbuf rtw_;
     bool fused_ = false;
-    int pipe_spc_ = 0; // forward: signals per tile of the pipelined kernel, 0 = not used
+    int pipe_spc_ = 0; // signals per tile of the pipelined forward / inverse kernels, 0 = not used
     dbuf err_;
 };
 
