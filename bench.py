@@ -96,6 +96,25 @@ class ClockSampler:
         except Exception:
             self.proc = None
 
+    def count(self) -> int:
+        """Samples written so far."""
+        if self.proc is None:
+            return 0
+        try:
+            self.f.flush()
+            with open(self.path) as f:
+                return sum(1 for line in f if line.count(",") >= 8)
+        except OSError:
+            return 0
+
+    def keep_busy_until(self, samples: int, busy, limit_s: float = 3.0):
+        """Runs busy() (one untimed step, synchronised) until `samples` samples exist or limit_s passes."""
+        if self.proc is None:
+            return
+        t0 = time.perf_counter()
+        while self.count() < samples and time.perf_counter() - t0 < limit_s:
+            busy()
+
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -441,15 +460,25 @@ def main():
     ev = {n: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)] for n in SIZES}
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    def busy_step():
+        step()
+        torch.cuda.synchronize()
+
+    # The timed region (~1 ms per step) is shorter than nvidia-smi's 200 ms sampling period, so the sampler
+    # runs over a loaded window: untimed steps of the same workload until its first sample, the timed
+    # region, then untimed steps until one more sample lands after it.
+    clocks.start()
+    clocks.keep_busy_until(1, busy_step)
     barrier(world)
     torch.cuda.synchronize()
-    clocks.start()
     start.record(stream)
     for s in range(args.steps):
         step({n: ev[n][s] for n in SIZES})
     stop.record(stream)
     torch.cuda.synchronize()
+    clocks.keep_busy_until(clocks.count() + 1, busy_step)
     clk = clocks.stop()
+    clk["window"] = "untimed steps of the same workload around the timed region (sampling period 200 ms)"
     barrier(world)
     total_ms = max_over_ranks(start.elapsed_time(stop), world)
     ms_step = total_ms / args.steps

@@ -903,7 +903,8 @@ __device__ __forceinline__ void ct_conv_pp(const LD& ld, const MID& mid, const S
 // and its loads and stores given as functors: the first pass reads ld(p), the passes exchange through the
 // padded buffer, the last pass writes st(q, x).  Each pass loads (and transforms) all of its butterflies,
 // then runs mid() for the last pass or a barrier otherwise, then stores; a barrier follows each store phase
-// except the last pass's.  mid() must contain a barrier (after it the buffer is no longer read).
+// except the last pass's.  mid() must contain a barrier (after it the buffer is no longer read).  The chains
+// below take a hook() that runs after the first pass.
 template <typename T, int N, int TS, int EPT, int R, int NS, int TWOFF, class LD, class MID, class ST>
 __device__ __forceinline__ void io_pass(cpx<T> (&v)[EPT], const LD& ld, const MID& mid, const ST& st,
                                         const cpx<T>* __restrict__ tw, const int lt)
@@ -945,9 +946,11 @@ __device__ __forceinline__ void io_pass(cpx<T> (&v)[EPT], const LD& ld, const MI
     }
 }
 
-template <typename T, int N, int TS, int EPT, int NS, int TWOFF, class LD, class MID, class ST, int R, int... Rest>
-__device__ __forceinline__ void io_chain(cpx<T> (&v)[EPT], const LD& ld, const MID& mid, const ST& st, cpx<T>* buf,
-                                         const cpx<T>* __restrict__ tw, const int lt)
+// hook() runs once, after the first pass's closing barrier (the first pass's sources are no longer read).
+template <typename T, int N, int TS, int EPT, int NS, int TWOFF, class LD, class MID, class ST, class H, int R,
+          int... Rest>
+__device__ __forceinline__ void io_chain(cpx<T> (&v)[EPT], const LD& ld, const MID& mid, const ST& st, const H& hook,
+                                         cpx<T>* buf, const cpx<T>* __restrict__ tw, const int lt)
 {
     if constexpr (sizeof...(Rest) == 0)
         io_pass<T, N, TS, EPT, R, NS, TWOFF>(v, ld, mid, st, tw, lt);
@@ -958,19 +961,22 @@ __device__ __forceinline__ void io_chain(cpx<T> (&v)[EPT], const LD& ld, const M
         const auto b_ld = [buf](int p) { return buf[pidx_s<ct_ps<T>(N, TS)>(p)]; };
         io_pass<T, N, TS, EPT, R, NS, TWOFF>(v, ld, sync, b_st, tw, lt);
         __syncthreads();
+        if constexpr (NS == 1)
+            hook();
         constexpr int TN = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
-        io_chain<T, N, TS, EPT, NS * R, TN, decltype(b_ld), MID, ST, Rest...>(v, b_ld, mid, st, buf, tw, lt);
+        io_chain<T, N, TS, EPT, NS * R, TN, decltype(b_ld), MID, ST, H, Rest...>(v, b_ld, mid, st, hook, buf, tw,
+                                                                                 lt);
     }
 }
 
-template <typename T, int N, int TS, int... Rs, class LD, class MID, class ST>
-__device__ __forceinline__ void ct_block_fft_io(const LD& ld, const MID& mid, const ST& st, cpx<T>* buf,
-                                                const cpx<T>* __restrict__ tw, const int lt)
+template <typename T, int N, int TS, int... Rs, class LD, class MID, class ST, class H>
+__device__ __forceinline__ void ct_block_fft_io(const LD& ld, const MID& mid, const ST& st, const H& hook,
+                                                cpx<T>* buf, const cpx<T>* __restrict__ tw, const int lt)
 {
     constexpr int EPT = ct_ept<N, TS, Rs...>();
     const int lta     = lt < TS ? lt : N;
     cpx<T> v[EPT];
-    io_chain<T, N, TS, EPT, 1, 0, LD, MID, ST, Rs...>(v, ld, mid, st, buf, tw, lta);
+    io_chain<T, N, TS, EPT, 1, 0, LD, MID, ST, H, Rs...>(v, ld, mid, st, hook, buf, tw, lta);
 }
 
 // Copies the descriptor's passes into shared memory with compile-time parameter offsets.  Ends with a

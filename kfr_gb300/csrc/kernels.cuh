@@ -72,12 +72,13 @@ struct ct_fft
     {
         ct_block_fft_pp<T, N, TS, Rs...>(ld, st, hook, pre_last, A, B, tw, lt);
     }
-    // in place with the signal in registers: first pass reads ld(p), last pass stores st(q, x) after mid()
-    template <class LD, class MID, class ST>
-    __device__ __forceinline__ void run_io(const LD& ld, const MID& mid, const ST& st, cpx<T>* buf,
+    // in place with the signal in registers: first pass reads ld(p), hook() after it, last pass stores
+    // st(q, x) after mid()
+    template <class LD, class MID, class ST, class H>
+    __device__ __forceinline__ void run_io(const LD& ld, const MID& mid, const ST& st, const H& hook, cpx<T>* buf,
                                            const cpx<T>* __restrict__ tw, int lt) const
     {
-        ct_block_fft_io<T, N, TS, Rs...>(ld, mid, st, buf, tw, lt);
+        ct_block_fft_io<T, N, TS, Rs...>(ld, mid, st, hook, buf, tw, lt);
     }
     // as run_pp, with post(j, o) applied to each last-pass butterfly's outputs before they are stored
     template <class LD, class PO, class ST>
@@ -277,21 +278,31 @@ __global__ void __launch_bounds__(F::max_threads, 1)
 // ---------------------------------------------------------------------------------------------------
 // Complex DFT, one signal per CTA, persistent (compile-time lengths whose three-tile pipeline does not fit,
 // e.g. N = 8192, 16384).  The signal lives in registers between the passes, which exchange through one
-// padded shared buffer.  A bulk copy (TMA) brings each signal into that buffer; the last pass first loads
-// its inputs, then (after a barrier) the next signal's copy is issued into the buffer, and the last pass's
-// outputs go straight to global memory while it lands.  A wait that runs out sets *err and the CTA returns.
+// padded shared buffer.  Each signal arrives by two bulk copies (TMA): its first half into a spare half-size
+// buffer, issued as soon as the previous signal's first pass has read that buffer, and its second half into
+// the exchange buffer, issued once the previous signal's last pass has read it (its outputs then go straight
+// to global memory while the copy lands).  A wait that runs out sets *err and the CTA returns.
 // ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__host__ __device__ constexpr int reg_smem_bytes()
+{
+    // exchange buffer (rounded to an even count: 16-byte boundary), spare first half, two mbarriers
+    return ((F::gstride(F::n) + 1) / 2 * 2 + F::n / 2) * int(sizeof(cpx<T>)) + 16;
+}
+
 template <typename T, class F>
 __global__ void __launch_bounds__(F::max_threads, 1)
     k_c2c_reg(const c2c_args a, const long long nsig, int* err)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int N          = F::n;
-    constexpr uint32_t bytes = uint32_t(N) * uint32_t(sizeof(cpx<T>));
+    constexpr int H          = N / 2;
+    constexpr uint32_t hbytes = uint32_t(H) * uint32_t(sizeof(cpx<T>));
     const F fft(nullptr, a.d, F::ts);
-    static_assert(bytes % 16 == 0, "whole 16-byte units per signal");
+    static_assert(N % 2 == 0 && hbytes % 16 == 0, "two halves of whole 16-byte units per signal");
     cpx<T>* buf      = reinterpret_cast<cpx<T>*>(smem_raw);
-    uint64_t* bar    = reinterpret_cast<uint64_t*>(buf + F::gstride(N));
+    cpx<T>* spare    = buf + (F::gstride(N) + 1) / 2 * 2; // on a 16-byte boundary
+    uint64_t* bars   = reinterpret_cast<uint64_t*>(spare + H); // [0]: first half (spare), [1]: second half
     const cpx<T>* in = reinterpret_cast<const cpx<T>*>(a.in);
     cpx<T>* out      = reinterpret_cast<cpx<T>*>(a.out);
     const cpx<T>* tw = reinterpret_cast<const cpx<T>*>(a.tw);
@@ -299,40 +310,54 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     const int lt     = int(threadIdx.x);
     if (threadIdx.x == 0)
     {
-        mbar_init(bar, 1);
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
         mbar_fence_init();
     }
     __syncthreads();
     long long s = blockIdx.x;
     if (threadIdx.x == 0 && s < nsig)
     {
-        mbar_arrive_expect_tx(bar, bytes);
-        bulk_g2s(buf, in + s * N, bytes, bar);
+        mbar_arrive_expect_tx(&bars[0], hbytes);
+        bulk_g2s(spare, in + s * N, hbytes, &bars[0]);
+        mbar_arrive_expect_tx(&bars[1], hbytes);
+        bulk_g2s(buf + H, in + s * N + H, hbytes, &bars[1]);
     }
     for (uint32_t phase = 0; s < nsig; s += gridDim.x, phase ^= 1)
     {
-        const bool got = mbar_wait(bar, phase);
+        const bool got = mbar_wait(&bars[0], phase) && mbar_wait(&bars[1], phase);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
-                atomicExch(err, 1);
+                atomicExch(err, 1); // nothing else is in flight: the next copies are issued after these waits
             return;
         }
         const long long sn = s + gridDim.x;
         cpx<T>* o          = out + s * N;
-        fft.run_io([&](int p) { return conj_if(buf[p], inv); },
+        fft.run_io([&](int p) { return conj_if(p < H ? spare[p] : buf[p], inv); },
                    [&]()
                    {
-                       // every thread has read the buffer: the next signal may overwrite it
+                       // every thread has read the exchange buffer: the next signal's second half may land in it
                        __syncthreads();
                        if (threadIdx.x == 0 && sn < nsig)
                        {
                            fence_proxy_async_smem();
-                           mbar_arrive_expect_tx(bar, bytes);
-                           bulk_g2s(buf, in + sn * N, bytes, bar);
+                           mbar_arrive_expect_tx(&bars[1], hbytes);
+                           bulk_g2s(buf + H, in + sn * N + H, hbytes, &bars[1]);
                        }
                    },
-                   [&](int q, cpx<T> x) { o[q] = conj_if(x, inv); }, buf, tw, lt);
+                   [&](int q, cpx<T> x) { o[q] = conj_if(x, inv); },
+                   [&]()
+                   {
+                       // the first pass has read the spare buffer: the next signal's first half may land in it
+                       if (threadIdx.x == 0 && sn < nsig)
+                       {
+                           fence_proxy_async_smem();
+                           mbar_arrive_expect_tx(&bars[0], hbytes);
+                           bulk_g2s(spare, in + sn * N, hbytes, &bars[0]);
+                       }
+                   },
+                   buf, tw, lt);
     }
 }
 

@@ -674,7 +674,7 @@ void complex_engine<T>::plan_pipe()
     if (!best)
     {
         // one signal per CTA with the signal in registers (lengths whose three tiles do not fit)
-        if (n >= 8192 && prog_.gstride * esz + 16 <= smem_budget())
+        if (n >= 8192 && ((prog_.gstride + 1) / 2 * 2 + n / 2) * esz + 16 <= smem_budget())
         {
             reg_ = true;
             err_.alloc(sizeof(int));
@@ -959,7 +959,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         if (reg_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
         {
             block_cfg rc = prog_.cfg_tile(1);
-            rc.smem      = prog_.gstride * int(esz) + 16;
+            rc.smem      = ((prog_.gstride + 1) / 2 * 2 + int(n_ / 2)) * int(esz) + 16;
             check(launch_ct_c2c_reg_f32(a, rc, batch, static_cast<int*>(err_.get()), st), "launch c2c (one per CTA)");
             done = batch;
         }
