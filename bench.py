@@ -12,8 +12,9 @@ e2e     = the same bytes / wall time of the same step through the C ABI with pin
           (kfr_dft_execute_batch_f32 with a NULL stream: H2D copy, kernels, D2H copy, synchronise).
 roofline: the kernel with the largest share of the step (per-length CUDA-event timing), its algorithmic
           GB/s against MEASURED_PEAKS.json's HBM copy bandwidth.
-cpu_baseline: the CPU oracle's single-precision port (oracle/kfr_oracle.c, same algorithm family as
-          KFR's dft_plan<float>) on all host cores over a bounded sample of each batch.
+cpu_baseline: KFR 7.0.1's own dft_plan<float> (compiled from the reference's sources on the host into
+          oracle/_ref) on all host cores over a bounded sample of each batch, plus a one-core figure; the
+          oracle's single-precision port where KFR was not built.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -180,23 +181,57 @@ def make_inputs(torch, n, batch, seed, device):
     return x
 
 
-def cpu_baseline_run(steps_scale: float = 1.0, threads: int | None = None):
-    """Oracle f32 port on the host cores over 1/32 of each batch; returns (GB/s, sample description)."""
-    from oracle.oracle import Oracle
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
 
-    orc = Oracle("orc")
+
+def cpu_baseline_run(frac: float = 1 / 32, threads: int | None = None, reps: int = 3) -> dict:
+    """The reference's CPU path on the host cores over a bounded sample of each batch: KFR 7.0.1's own
+    dft_plan<float> (oracle/_ref, compiled from the reference's sources on this machine), one plan per length
+    built beforehand and shared by all threads, best of `reps` passes; where KFR was not built here, the
+    oracle's single-precision port instead (kind "port").  Returns the cpu_baseline object."""
+    from oracle.oracle import Oracle, available
+
+    kind = "reference" if available("ref") else "port"
+    orc = Oracle("ref" if kind == "reference" else "orc")
     threads = threads or os.cpu_count() or 1
     total_bytes, total_t = 0, 0.0
     for n in SIZES:
-        b = max(1, int(batch_for(n) // 32 * steps_scale))
+        b = max(1, int(batch_for(n) * frac))
         rng = np.random.default_rng(n)
         x = (rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))).astype(np.complex64)
-        orc.dft(x[: max(1, b // 8)], precision="f32", threads=threads)  # warm the pages and plan path
-        t0 = time.perf_counter()
-        orc.dft(x, precision="f32", threads=threads)
-        total_t += time.perf_counter() - t0
+        if kind == "reference":
+            dt = orc.dft_time(x, threads=threads, reps=reps)
+        else:
+            orc.dft(x[: max(1, b // 8)], precision="f32", threads=threads)  # warm the pages and plan path
+            dt = 1e30
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                orc.dft(x, precision="f32", threads=threads)
+                dt = min(dt, time.perf_counter() - t0)
+        total_t += dt
         total_bytes += 16 * n * b
-    return total_bytes / total_t / 1e9, threads, "1/32 of each batch (8 MiB per length), forward, all host threads"
+    what = ("KFR 7.0.1 dft_plan<float> compiled with g++ -O3 on this host" if kind == "reference" else
+            "the oracle's single-precision port (KFR was not built on this host)")
+    sample = (f"{what}; {frac:g} of each batch ({BYTES_PER_SIZE * frac / 2**20:g} MiB per length), forward, "
+              f"{threads} thread(s), plan built once, best of {reps}")
+    return {"value": round(total_bytes / total_t / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": kind,
+            "sample": sample, "cpu": cpu_model()}
+
+
+def cpu_baseline_both() -> dict:
+    """All host cores (the cpu_baseline value) plus a one-core figure on a smaller sample."""
+    allc = cpu_baseline_run(1 / 32)
+    one = cpu_baseline_run(1 / 256, threads=1)
+    allc["one_core"] = {"value": one["value"], "sample": one["sample"]}
+    return allc
 
 
 def measure_rows(torch, k, dev, stream, hbm, with_cpu):
@@ -370,21 +405,21 @@ def run_reference(args):
     if rank != 0:
         return 0
     for _ in range(args.warmup):
-        cpu_baseline_run(0.25)
+        cpu_baseline_run(1 / 128, reps=1)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, threads, sample = cpu_baseline_run()
-        vals.append(v)
+        cb = cpu_baseline_run(1 / 32, reps=1)
+        vals.append(cb["value"])
     wall = time.perf_counter() - t0
     value = float(np.mean(vals))
+    cb["value"] = round(value, 3)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config_dict(),
-        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+        "cpu_baseline": cb,
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -564,8 +599,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, threads, sample = cpu_baseline_run()
-        cpu = {"value": round(v, 3), "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample}
+        cpu = cpu_baseline_both()
 
     if rank == 0:
         line = {

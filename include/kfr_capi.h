@@ -100,6 +100,15 @@ KFR_API_SPEC const char* kfr_last_error(void);     /* capi.h:128: thread-local, 
 KFR_API_SPEC void* kfr_allocate(size_t size);                           /* capi.h:170 */
 KFR_API_SPEC void* kfr_allocate_aligned(size_t size, size_t alignment); /* capi.h:173 */
 KFR_API_SPEC void kfr_deallocate(void* ptr);                            /* capi.h:176 */
+/* The reference's managed-allocation helpers (capi.h:178-193, src/capi/capi.cpp:200-216), always exported
+ * here.  A block starts with one reference; kfr_deallocate and kfr_release drop one and free the block at
+ * zero; kfr_reallocate* copy min(old, new) bytes into a new block and release the old one (new_size 0:
+ * release and return NULL; ptr NULL: plain allocation). */
+KFR_API_SPEC void* kfr_reallocate(void* ptr, size_t new_size);                             /* capi.h:180 */
+KFR_API_SPEC void* kfr_reallocate_aligned(void* ptr, size_t new_size, size_t alignment);   /* capi.h:183 */
+KFR_API_SPEC void* kfr_add_ref(void* ptr);                                                 /* capi.h:186 */
+KFR_API_SPEC void kfr_release(void* ptr);                                                  /* capi.h:189 */
+KFR_API_SPEC size_t kfr_allocated_size(void* ptr);                                         /* capi.h:192 */
 
 /* ---- complex DFT ---------------------------------------------------------------------------------- */
 KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_plan_f32(size_t size);                              /* capi.h:207 */
@@ -263,9 +272,11 @@ KFR_API_SPEC void kfr_dft_cache_clear(void);
 /* Text description of the plan's GPU strategy (kernel kind, radices, launch shape), as kfr_dft_dump_f32 prints
  * it; copies at most size-1 bytes plus a terminating zero and returns the full length. */
 KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size);
+KFR_API_SPEC size_t kfr_dft_describe_f64(KFR_DFT_PLAN_F64* plan, char* buf, size_t size);
 
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
+KFR_API_SPEC size_t kfr_dft_get_launch_count_f64(KFR_DFT_PLAN_F64* plan, size_t batch);
 
 /* Multi-channel convolution filter (no counterpart in the reference, whose filters are single-channel): the
  * same filter applied independently to `channels` signals, each with its own state.  kfr_filter_process_*
@@ -354,8 +365,11 @@ KFR_API_SPEC void kfr_fir_backward_f64(const kfr_f64* taps, size_t ntaps, size_t
  *   - batch * the plan's per-signal scratch must fit KFR_STATIC_SCRATCH_BYTES: error otherwise
  *     (kfr_dft_get_temp_size_batch_f32 gives the requirement);
  *   - stream: NULL = synchronous on the default stream, else a cudaStream_t the work is enqueued on;
- *   - the first call on each device does the one-time set-up (looks up the array's device address, which
- *     also loads this library's device code there): make that first call before any stream capture;
+ *   - the first call on each device, whatever the plan, does the one-time set-up (looks up the array's
+ *     device address): make that first call before any stream capture;
+ *   - the CUDA driver loads each kernel's code on its first launch, and that load takes device memory: run
+ *     each plan once through this entry point, with the batch it will use, before stream capture or
+ *     real-time use;
  *   - every call shares the one array and no call needs it cleared; calls that overlap on the GPU (on
  *     different streams, or from different threads) race on it and must be serialised by the caller.
  * Errors are reported through kfr_last_error() like every other entry point. */

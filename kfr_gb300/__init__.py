@@ -105,6 +105,13 @@ _SIGS.update({
     "kfr_allocate": (_P, [_S]),
     "kfr_allocate_aligned": (_P, [_S, _S]),
     "kfr_deallocate": (None, [_P]),
+    "kfr_reallocate": (_P, [_P, _S]),
+    "kfr_reallocate_aligned": (_P, [_P, _S, _S]),
+    "kfr_add_ref": (_P, [_P]),
+    "kfr_release": (None, [_P]),
+    "kfr_allocated_size": (_S, [_P]),
+    "kfr_dft_describe_f64": (_S, [_P, ctypes.c_char_p, _S]),
+    "kfr_dft_get_launch_count_f64": (_S, [_P, _S]),
     "kfr_dft_get_launch_count_f32": (_S, [_P, _S]),
     "kfr_dft_describe_f32": (_S, [_P, ctypes.c_char_p, _S]),
     "kfr_dft_execute_static_scratch_f32": (None, [_P, _S, _P, _P, _B, _P]),

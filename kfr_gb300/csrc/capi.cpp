@@ -5,6 +5,8 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
+#include <new>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -582,28 +584,43 @@ std::string& version_string()
     return s;
 }
 
-// Host allocations carry a small header: the pointer returned by malloc and whether the block is pinned.
+// Host allocations carry a small header: the pointer returned by malloc, the requested size, a reference
+// count and whether the block is pinned.  The counting follows the reference's managed allocation
+// (include/kfr/meta/memory.hpp:58-140): a block starts with one reference and is freed when the last one is
+// released.
 struct alloc_header
 {
     void* base;
     size_t size;
+    std::atomic<unsigned> refs;
     int pinned;
     int magic;
 };
 constexpr int kAllocMagic = 0x6b667241;
 
+alloc_header* header_of(void* p)
+{
+    alloc_header* h = reinterpret_cast<alloc_header*>(p) - 1;
+    if (h->magic != kAllocMagic)
+        throw std::invalid_argument("pointer was not allocated by kfr_allocate");
+    return h;
+}
+
 void* host_alloc(size_t size, size_t alignment)
 {
-    if (alignment < alignof(alloc_header) || (alignment & (alignment - 1)))
-        throw std::invalid_argument("alignment must be a power of two");
+    // the reference returns NULL for alignments of 0 or above 32768 (include/kfr/meta/memory.hpp:64-65)
+    if (alignment == 0 || alignment > 32768 || (alignment & (alignment - 1)))
+        throw std::invalid_argument("alignment must be a power of two between 1 and 32768");
+    alignment         = std::max(alignment, alignof(alloc_header));
     const size_t total = size + alignment + sizeof(alloc_header);
     void* base         = std::malloc(total);
     if (!base)
         throw std::bad_alloc();
     uintptr_t p = (reinterpret_cast<uintptr_t>(base) + sizeof(alloc_header) + alignment - 1) & ~(uintptr_t(alignment) - 1);
-    alloc_header* h = reinterpret_cast<alloc_header*>(p) - 1;
+    alloc_header* h = new (reinterpret_cast<alloc_header*>(p) - 1) alloc_header;
     h->base         = base;
     h->size         = size;
+    h->refs.store(1);
     h->magic        = kAllocMagic;
     h->pinned       = 0;
     int ndev        = 0;
@@ -619,20 +636,40 @@ void* host_alloc(size_t size, size_t alignment)
     return reinterpret_cast<void*>(p);
 }
 
+// Drops one reference; frees the block at zero.
 void host_free(void* p)
 {
     if (!p)
         return;
-    alloc_header* h = reinterpret_cast<alloc_header*>(p) - 1;
-    if (h->magic != kAllocMagic)
-        throw std::invalid_argument("pointer was not allocated by kfr_allocate");
+    alloc_header* h = header_of(p);
+    if (--h->refs != 0)
+        return;
     if (h->pinned)
     {
         cudaHostUnregister(p);
         cudaGetLastError();
     }
     h->magic = 0;
-    std::free(h->base);
+    void* base = h->base;
+    h->~alloc_header();
+    std::free(base);
+}
+
+// include/kfr/meta/memory.hpp:120-140
+void* host_realloc(void* p, size_t new_size, size_t alignment)
+{
+    if (!p)
+        return new_size ? host_alloc(new_size, alignment) : nullptr;
+    const size_t old_size = header_of(p)->size;
+    if (!new_size)
+    {
+        host_free(p);
+        return nullptr;
+    }
+    void* q = host_alloc(new_size, alignment);
+    std::memcpy(q, p, std::min(old_size, new_size));
+    host_free(p);
+    return q;
 }
 
 // init_shape (src/capi/capi.cpp:106-114)
@@ -731,6 +768,27 @@ size_t autocorrelate_any(T* out, const T* a, size_t n)
 
 } // namespace
 
+namespace
+{
+template <typename T>
+size_t describe_into(void* plan, unsigned tag, char* buf, size_t size)
+{
+    return try_fn(
+        [&]
+        {
+            const std::string d = as<dft_obj<T>>(plan, tag)->describe();
+            if (buf && size)
+            {
+                const size_t n = std::min(size - 1, d.size());
+                std::memcpy(buf, d.data(), n);
+                buf[n] = 0;
+            }
+            return d.size();
+        },
+        size_t(0));
+}
+} // namespace
+
 extern "C"
 {
 
@@ -764,6 +822,33 @@ KFR_API_SPEC void* kfr_allocate_aligned(size_t size, size_t alignment)
 KFR_API_SPEC void kfr_deallocate(void* ptr)
 {
     try_void([&] { host_free(ptr); });
+}
+KFR_API_SPEC void* kfr_reallocate(void* ptr, size_t new_size)
+{
+    return try_fn([&] { return host_realloc(ptr, new_size, KFR_DEFAULT_ALIGNMENT); }, (void*)nullptr);
+}
+KFR_API_SPEC void* kfr_reallocate_aligned(void* ptr, size_t new_size, size_t alignment)
+{
+    return try_fn([&] { return host_realloc(ptr, new_size, alignment); }, (void*)nullptr);
+}
+KFR_API_SPEC void* kfr_add_ref(void* ptr)
+{
+    return try_fn(
+        [&]
+        {
+            if (ptr)
+                header_of(ptr)->refs++;
+            return ptr;
+        },
+        (void*)nullptr);
+}
+KFR_API_SPEC void kfr_release(void* ptr)
+{
+    try_void([&] { host_free(ptr); });
+}
+KFR_API_SPEC size_t kfr_allocated_size(void* ptr)
+{
+    return try_fn([&] { return ptr ? header_of(ptr)->size : size_t(0); }, size_t(0));
 }
 
 // ---- complex DFT ---------------------------------------------------------------------------------
@@ -894,23 +979,19 @@ KFR_API_SPEC void kfr_dft_cache_clear(void)
 
 KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size)
 {
-    return try_fn(
-        [&]
-        {
-            const std::string d = as<dft_obj<float>>(plan, TAG_DFT_F32)->describe();
-            if (buf && size)
-            {
-                const size_t n = std::min(size - 1, d.size());
-                std::memcpy(buf, d.data(), n);
-                buf[n] = 0;
-            }
-            return d.size();
-        },
-        size_t(0));
+    return describe_into<float>(plan, TAG_DFT_F32, buf, size);
+}
+KFR_API_SPEC size_t kfr_dft_describe_f64(KFR_DFT_PLAN_F64* plan, char* buf, size_t size)
+{
+    return describe_into<double>(plan, TAG_DFT_F64, buf, size);
 }
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch)
 {
     return try_fn([&] { return size_t(as<dft_obj<float>>(plan, TAG_DFT_F32)->launches(batch)); }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_get_launch_count_f64(KFR_DFT_PLAN_F64* plan, size_t batch)
+{
+    return try_fn([&] { return size_t(as<dft_obj<double>>(plan, TAG_DFT_F64)->launches(batch)); }, size_t(0));
 }
 
 } // extern "C"
@@ -935,7 +1016,10 @@ void run_static_scratch_f32(void* plan, size_t batch, void* out, const void* in,
                 throw std::invalid_argument("kfr_dft_execute_static_scratch_f32: this plan and batch need " +
                                             std::to_string(need) + " bytes of scratch, more than the " +
                                             std::to_string(scratch_limit) + "-byte static scratch");
-            void* scr       = need ? scratch_of() : nullptr;
+            // The per-device set-up runs on every call, so the first call on a device always does it,
+            // whether or not this plan needs scratch.
+            void* addr      = scratch_of();
+            void* scr       = need ? addr : nullptr;
             cudaStream_t st = static_cast<cudaStream_t>(stream);
             p->execute(out, in, (long long)batch, inverse, scr, st);
             check(cudaGetLastError(), "kernel launch");

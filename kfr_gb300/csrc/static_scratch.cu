@@ -8,10 +8,12 @@
 // exits, so its size is a modest, stated maximum (KFR_STATIC_SCRATCH_BYTES in include/kfr_capi.h).
 //
 // The array's name is only a host-side stand-in in host code: its device address comes from
-// cudaGetSymbolAddress, looked up once per device (with that device current) on the first call there.
-// That first call also makes the CUDA driver load this library's device code on the device, so it belongs
-// before any stream capture.  All calls share the array; none needs it zeroed (each pass writes every
-// scratch element it later reads), and calls that overlap on the GPU race on it.
+// cudaGetSymbolAddress, looked up once per device (with that device current) on the first call there,
+// whatever the plan.  The CUDA driver loads device code lazily, one compiled module at a time, on a kernel's
+// first launch, and loading takes device memory: so run each plan once through this entry point, with the
+// batch it will use, before stream capture or real-time use.  All calls share the array; none needs it
+// zeroed (each pass writes every scratch element it later reads), and calls that overlap on the GPU race
+// on it.
 #include <cstdint>
 #include <mutex>
 #include <stdexcept>

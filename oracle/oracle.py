@@ -24,10 +24,28 @@ _c_int = ctypes.c_int
 _ptr = ctypes.c_void_p
 
 
+REF_SRC_DEFAULT = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "kfr")
+
+
+def ref_sources() -> str | None:
+    """Where the reference's sources for oracle/_ref are: $KFR_SRC, else the git-ignored copy that
+    oracle/stage_ref.sh makes under baseline/_ref/kfr; None if neither exists."""
+    for d in (os.environ.get("KFR_SRC"), REF_SRC_DEFAULT):
+        if d and os.path.exists(os.path.join(d, "src", "dft", "dft.cpp")):
+            return d
+    return None
+
+
+def build_command(ref: bool = False) -> list[str]:
+    """make command for liboracle.so (and, if asked and the reference sources exist, the reference library)."""
+    src = ref_sources() if ref else None
+    targets = ["oracle"] + (["ref", f"KFR_SRC={src}"] if src else [])
+    return ["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}"] + targets
+
+
 def build(ref: bool = False) -> None:
     """Compile liboracle.so (and, if asked and the reference sources exist, the reference library)."""
-    targets = ["oracle"] + (["ref"] if ref else [])
-    subprocess.check_call(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}"] + targets)
+    subprocess.check_call(build_command(ref))
 
 
 def available(kind: str) -> bool:
@@ -90,6 +108,19 @@ class Oracle:
         if n:
             self._fn("dft", rdt)(_p(out), _p(x), n, batch, int(inverse), threads)
         return out
+
+    def dft_time(self, x, inverse=False, threads=1, reps=3):
+        """Best wall time (seconds) of one c32 DFT pass over the batch x (signals along the last axis) with
+        the plan built once beforehand and shared by `threads` threads (KFR's dft_plan<float>; ref only)."""
+        if self.kind != "ref":
+            raise RuntimeError("dft_time times the reference library")
+        f = self.lib.ref_dft_time_f32
+        f.restype = ctypes.c_double
+        f.argtypes = [_ptr, _ptr, _c_size, _c_size, _c_int, _c_int, _c_int]
+        x = np.ascontiguousarray(x, dtype=np.complex64)
+        n = x.shape[-1]
+        out = np.empty_like(x)
+        return float(f(_p(out), _p(x), n, x.size // n, int(inverse), threads, reps))
 
     # ---- real DFT ----------------------------------------------------------------------------------
     def dft_real(self, x, ccs=True, precision="f64", threads=1):

@@ -14,6 +14,7 @@
 #include <kfr/dft.hpp>
 #include <kfr/dft/convolution.hpp>
 
+#include <chrono>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -268,6 +269,46 @@ extern "C" __attribute__((visibility("default"))) int ref_dft_md_real_f64(double
                                                                           int real_out_is_enough)
 {
     return run_md_real<double>(out, in, dims, shape, inverse, real_out_is_enough);
+}
+
+// Timed baseline: one dft_plan<float> built once (plan creation excluded), shared const across `threads`
+// std::threads over the batch, each with its own temp (the CPU-baseline method: one shared plan, per-thread
+// temp, best of `reps` runs).  Returns the best wall time of one pass over the batch, in seconds.
+extern "C" __attribute__((visibility("default"))) double ref_dft_time_f32(float* out, const float* in, size_t n,
+                                                                          size_t batch, int inverse, int threads,
+                                                                          int reps)
+{
+    if (n == 0 || batch == 0)
+        return 0.0;
+    const dft_plan<float> plan(n);
+    if (threads < 1)
+        threads = 1;
+    if (static_cast<size_t>(threads) > batch)
+        threads = static_cast<int>(batch);
+    std::vector<univector<u8>> temps(threads, univector<u8>(plan.temp_size));
+    double best = 1e30;
+    for (int r = 0; r < (reps < 1 ? 1 : reps); r++)
+    {
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<std::thread> pool;
+        for (int t = 0; t < threads; t++)
+        {
+            const size_t b0 = batch * t / threads, b1 = batch * (t + 1) / threads;
+            pool.emplace_back(
+                [&, t, b0, b1]
+                {
+                    for (size_t b = b0; b < b1; b++)
+                        plan.execute(reinterpret_cast<complex<float>*>(out) + b * n,
+                                     reinterpret_cast<const complex<float>*>(in) + b * n, temps[t].data(),
+                                     inverse != 0);
+                });
+        }
+        for (auto& th : pool)
+            th.join();
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        best            = dt < best ? dt : best;
+    }
+    return best;
 }
 
 extern "C" __attribute__((visibility("default"))) void ref_dft_dump_f32(size_t n)

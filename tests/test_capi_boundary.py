@@ -11,11 +11,12 @@ import kfr_gb300 as k
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
-# The reference's C API entry points for the DFT path (include/kfr/capi.h:116-736), minus the
-# KFR_MANAGED_ALLOCATION-only helpers (capi.h:178-193), which the reference compiles out by default.
+# Every entry point of the reference's C API (include/kfr/capi.h:116-736): 79 names, including the
+# KFR_MANAGED_ALLOCATION helpers (capi.h:178-193).
 REFERENCE_DFT_API = [
     "kfr_version_string", "kfr_version", "kfr_enabled_archs", "kfr_current_arch", "kfr_last_error",
-    "kfr_allocate", "kfr_allocate_aligned", "kfr_deallocate",
+    "kfr_allocate", "kfr_allocate_aligned", "kfr_deallocate", "kfr_reallocate", "kfr_reallocate_aligned",
+    "kfr_add_ref", "kfr_release", "kfr_allocated_size",
 ] + [f"kfr_dft_{op}_{p}" for p in ("f32", "f64") for op in (
     "create_plan", "create_2d_plan", "create_3d_plan", "create_md_plan", "dump", "get_size", "get_temp_size",
     "execute", "execute_inverse", "delete_plan")] + [f"kfr_dft_real_{op}_{p}" for p in ("f32", "f64") for op in (
@@ -80,6 +81,42 @@ def test_host_allocation_without_gpu(L):
     p = L.kfr_allocate_aligned(100, 4096)
     assert p % 4096 == 0
     L.kfr_deallocate(p)
+    assert L.kfr_last_error() == b""
+
+
+def test_reference_api_has_79_entry_points():
+    assert len(set(REFERENCE_DFT_API)) == 79
+
+
+def test_managed_allocation(L):
+    """kfr_reallocate / kfr_reallocate_aligned / kfr_add_ref / kfr_release / kfr_allocated_size follow the
+    reference's managed allocation (include/kfr/meta/memory.hpp:58-140): contents survive a reallocation,
+    a block lives until its last reference is released, and the size query returns the requested size."""
+    p = L.kfr_allocate(100)
+    assert L.kfr_allocated_size(p) == 100
+    ctypes.memmove(p, bytes(range(100)), 100)
+    q = L.kfr_reallocate(p, 300)  # grows: the first 100 bytes are kept
+    assert q and q % 64 == 0 and L.kfr_allocated_size(q) == 300
+    assert ctypes.string_at(q, 100) == bytes(range(100))
+    r = L.kfr_reallocate_aligned(q, 40, 4096)  # shrinks: the first 40 bytes are kept
+    assert r % 4096 == 0 and L.kfr_allocated_size(r) == 40
+    assert ctypes.string_at(r, 40) == bytes(range(40))
+    assert L.kfr_add_ref(r) == r  # two references now
+    L.kfr_release(r)
+    assert L.kfr_allocated_size(r) == 40  # still alive after one release
+    L.kfr_release(r)  # last reference: freed
+    assert L.kfr_last_error() == b""
+    assert not L.kfr_reallocate(None, 0)
+    s = L.kfr_reallocate(None, 16)  # NULL pointer: plain allocation
+    assert s and L.kfr_allocated_size(s) == 16
+    assert not L.kfr_reallocate(s, 0)  # size 0: released, NULL returned
+    assert L.kfr_last_error() == b""
+    assert not L.kfr_allocate_aligned(16, 0)  # alignment 0 or above 32768: NULL, as in the reference
+    assert not L.kfr_allocate_aligned(16, 65536)
+    assert b"alignment" in L.kfr_last_error()
+    big = L.kfr_allocate(1 << 20)  # large blocks are registered (pinned) where a GPU is present
+    assert L.kfr_allocated_size(big) == 1 << 20
+    L.kfr_deallocate(big)
     assert L.kfr_last_error() == b""
 
 
