@@ -274,6 +274,26 @@ KFR_API_SPEC void kfr_dft_cache_clear(void);
 KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size);
 KFR_API_SPEC size_t kfr_dft_describe_f64(KFR_DFT_PLAN_F64* plan, char* buf, size_t size);
 
+/* fft_multiply / fft_multiply_accumulate (include/kfr/dft/fft.hpp:983-1020) on device buffers, over `batch`
+ * spectra of `size` complex elements stored back to back (the outputs of a real or complex DFT plan):
+ *   kfr_fft_multiply_*:            dest = src1 * src2
+ *   kfr_fft_multiply_accumulate_*: dest = acc + src1 * src2  (acc == dest is the reference's two-operand
+ *                                  form; a separate acc is its three-operand form)
+ * fmt = Perm multiplies element 0 part by part (DC and Nyquist, both real, share it), as the reference does.
+ * src2_shared != 0: src2 is one spectrum applied to every signal (a filter); else `batch` spectra.  Every
+ * pointer must be device memory; dest may alias any input.  stream: NULL = synchronous, else enqueued on
+ * that cudaStream_t. */
+KFR_API_SPEC void kfr_fft_multiply_f32(kfr_c32* dest, const kfr_c32* src1, const kfr_c32* src2, size_t size,
+                                       size_t batch, kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream);
+KFR_API_SPEC void kfr_fft_multiply_f64(kfr_c64* dest, const kfr_c64* src1, const kfr_c64* src2, size_t size,
+                                       size_t batch, kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream);
+KFR_API_SPEC void kfr_fft_multiply_accumulate_f32(kfr_c32* dest, const kfr_c32* acc, const kfr_c32* src1,
+                                                  const kfr_c32* src2, size_t size, size_t batch,
+                                                  kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream);
+KFR_API_SPEC void kfr_fft_multiply_accumulate_f64(kfr_c64* dest, const kfr_c64* acc, const kfr_c64* src1,
+                                                  const kfr_c64* src2, size_t size, size_t batch,
+                                                  kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream);
+
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f64(KFR_DFT_PLAN_F64* plan, size_t batch);

@@ -26,7 +26,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libkfr_capi.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "kfr_capi.h")
 
 __all__ = ["KfrError", "lib", "dft_plan", "dft_plan_md", "dft_plan_real", "dft_plan_md_real", "dct_plan",
-           "convolve_filter", "declared_symbols", "CCs", "Perm"]
+           "convolve_filter", "declared_symbols", "fft_multiply", "CCs", "Perm"]
 
 CCs = 1
 Perm = 0
@@ -111,6 +111,10 @@ _SIGS.update({
     "kfr_release": (None, [_P]),
     "kfr_allocated_size": (_S, [_P]),
     "kfr_dft_describe_f64": (_S, [_P, ctypes.c_char_p, _S]),
+    "kfr_fft_multiply_f32": (None, [_P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
+    "kfr_fft_multiply_f64": (None, [_P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
+    "kfr_fft_multiply_accumulate_f32": (None, [_P, _P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
+    "kfr_fft_multiply_accumulate_f64": (None, [_P, _P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
     "kfr_dft_get_launch_count_f64": (_S, [_P, _S]),
     "kfr_dft_get_launch_count_f32": (_S, [_P, _S]),
     "kfr_dft_describe_f32": (_S, [_P, ctypes.c_char_p, _S]),
@@ -494,6 +498,22 @@ def autocorrelate(a):
     out = _like(a, _numel(a))
     _call(f"kfr_autocorrelate_{_conv_sfx(a)}", _addr(out), _addr(a), _numel(a))
     return out
+
+
+def fft_multiply(dest, src1, src2, size, batch=1, fmt="CCs", accumulate_from=None, stream=None):
+    """fft_multiply / fft_multiply_accumulate (include/kfr/dft/fft.hpp:983-1020) on device buffers: dest =
+    [accumulate_from +] src1 * src2 over `batch` spectra of `size` elements; src2 holding `size` elements only
+    is one spectrum shared by every signal.  fmt "Perm" multiplies element 0 part by part."""
+    sfx = "f64" if "128" in str(getattr(dest, "dtype", "")) else "f32"
+    shared = _numel(src2) == size and batch > 1
+    f = 1 if fmt in ("CCs", 1) else 0
+    if accumulate_from is None:
+        _call(f"kfr_fft_multiply_{sfx}", _addr(dest), _addr(src1), _addr(src2), size, batch, shared, f,
+              _stream_addr(stream))
+    else:
+        _call(f"kfr_fft_multiply_accumulate_{sfx}", _addr(dest), _addr(accumulate_from), _addr(src1), _addr(src2),
+              size, batch, shared, f, _stream_addr(stream))
+    return dest
 
 
 def allocate(size: int, alignment: int = 64) -> int:

@@ -771,6 +771,25 @@ size_t autocorrelate_any(T* out, const T* a, size_t n)
 namespace
 {
 template <typename T>
+void fft_multiply_dev(void* dest, const void* acc, const void* src1, const void* src2, size_t size, size_t batch,
+                      bool shared, bool perm, void* stream)
+{
+    if (!size || !batch)
+        return;
+    for (const void* p : { (const void*)dest, acc, src1, src2 })
+        if (p && !is_device_ptr(p))
+            throw std::invalid_argument("fft_multiply needs device pointers");
+    if (!dest || !src1 || !src2)
+        throw std::invalid_argument("fft_multiply: NULL buffer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    check(launch_fft_multiply<T>(dest, acc, src1, src2, (long long)size, (long long)batch,
+                                 shared ? 0LL : (long long)size, perm, st),
+          "fft_multiply");
+    if (!stream)
+        check(cudaStreamSynchronize(st), "fft_multiply");
+}
+
+template <typename T>
 size_t describe_into(void* plan, unsigned tag, char* buf, size_t size)
 {
     return try_fn(
@@ -977,6 +996,40 @@ KFR_API_SPEC void kfr_dft_cache_clear(void)
     try_void([&] { plan_cache::instance().clear(); });
 }
 
+KFR_API_SPEC void kfr_fft_multiply_f32(kfr_c32* dest, const kfr_c32* src1, const kfr_c32* src2, size_t size,
+                                       size_t batch, kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream)
+{
+    try_void([&] { fft_multiply_dev<float>(dest, nullptr, src1, src2, size, batch, src2_shared, fmt == Perm, stream); });
+}
+KFR_API_SPEC void kfr_fft_multiply_f64(kfr_c64* dest, const kfr_c64* src1, const kfr_c64* src2, size_t size,
+                                       size_t batch, kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream)
+{
+    try_void([&] { fft_multiply_dev<double>(dest, nullptr, src1, src2, size, batch, src2_shared, fmt == Perm, stream); });
+}
+KFR_API_SPEC void kfr_fft_multiply_accumulate_f32(kfr_c32* dest, const kfr_c32* acc, const kfr_c32* src1,
+                                                  const kfr_c32* src2, size_t size, size_t batch,
+                                                  kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream)
+{
+    try_void(
+        [&]
+        {
+            if (!acc)
+                throw std::invalid_argument("fft_multiply_accumulate: NULL accumulator");
+            fft_multiply_dev<float>(dest, acc, src1, src2, size, batch, src2_shared, fmt == Perm, stream);
+        });
+}
+KFR_API_SPEC void kfr_fft_multiply_accumulate_f64(kfr_c64* dest, const kfr_c64* acc, const kfr_c64* src1,
+                                                  const kfr_c64* src2, size_t size, size_t batch,
+                                                  kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream)
+{
+    try_void(
+        [&]
+        {
+            if (!acc)
+                throw std::invalid_argument("fft_multiply_accumulate: NULL accumulator");
+            fft_multiply_dev<double>(dest, acc, src1, src2, size, batch, src2_shared, fmt == Perm, stream);
+        });
+}
 KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size)
 {
     return describe_into<float>(plan, TAG_DFT_F32, buf, size);

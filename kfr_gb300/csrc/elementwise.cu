@@ -129,6 +129,55 @@ cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// Spectral product of include/kfr/dft/fft.hpp:983-1020 over a batch: one thread per element, grid-stride.
+// The Perm format stores the DC and Nyquist bins, both real, as the real and imaginary parts of element 0, so
+// that element is multiplied part by part instead of as a complex number.
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(256) k_fft_multiply(cpx<T>* dest, const cpx<T>* acc, const cpx<T>* src1,
+                                                      const cpx<T>* src2, const long long size,
+                                                      const long long total, const long long src2_stride,
+                                                      const int perm)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x)
+    {
+        const long long s = i / size;
+        const long long e = i - s * size;
+        const cpx<T> a    = src1[i];
+        const cpx<T> b    = src2[s * src2_stride + e];
+        cpx<T> v          = (perm && e == 0) ? mk<T>(a.x * b.x, a.y * b.y) : a * b;
+        if constexpr (ACC)
+            v = acc[i] + v;
+        dest[i] = v;
+    }
+}
+
+template <typename T>
+cudaError_t launch_fft_multiply(void* dest, const void* acc, const void* src1, const void* src2, long long size,
+                                long long batch, long long src2_stride, bool perm, cudaStream_t st)
+{
+    const long long total = size * batch;
+    if (total <= 0)
+        return cudaSuccess;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152LL * 16)
+        blocks = 152LL * 16;
+    auto* d        = static_cast<cpx<T>*>(dest);
+    const auto* a  = static_cast<const cpx<T>*>(acc);
+    const auto* s1 = static_cast<const cpx<T>*>(src1);
+    const auto* s2 = static_cast<const cpx<T>*>(src2);
+    if (acc)
+        k_fft_multiply<T, true><<<unsigned(blocks), 256, 0, st>>>(d, a, s1, s2, size, total, src2_stride, perm);
+    else
+        k_fft_multiply<T, false><<<unsigned(blocks), 256, 0, st>>>(d, a, s1, s2, size, total, src2_stride, perm);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_fft_multiply<float>(void*, const void*, const void*, const void*, long long, long long,
+                                                long long, bool, cudaStream_t);
+template cudaError_t launch_fft_multiply<double>(void*, const void*, const void*, const void*, long long,
+                                                 long long, long long, bool, cudaStream_t);
+
 template cudaError_t launch_elementwise<float>(int, const ew_args&, cudaStream_t);
 template cudaError_t launch_elementwise<double>(int, const ew_args&, cudaStream_t);
 

@@ -178,6 +178,14 @@ enum ew_op
 template <typename T>
 cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st);
 
+// fft_multiply / fft_multiply_accumulate over `batch` spectra of `size` elements stored back to back:
+// dest = (acc ? acc : 0) + src1 * src2, with the Perm format's element 0 formed from the real and the
+// imaginary parts separately.  src2_stride: 0 (one spectrum shared by every signal) or size.  acc may alias
+// dest; src1 / src2 may alias dest.
+template <typename T>
+cudaError_t launch_fft_multiply(void* dest, const void* acc, const void* src1, const void* src2, long long size,
+                                long long batch, long long src2_stride, bool perm, cudaStream_t st);
+
 // Compile-time specialised kernels (single precision; lengths in ct_table.hpp).  kind: see ct_kind.
 cudaError_t launch_ct_c2c_f32(const c2c_args& a, const block_cfg& c, cudaStream_t st);
 // Persistent TMA-pipelined complex DFT over `ntiles` whole tiles of c.spc contiguous signals (c.smem must

@@ -321,6 +321,16 @@ static void orc_parallel(orc_job_fn fn, void* ctx, size_t count, int threads)
     {                                                                                                    \
         ORC_CAT(filt_free, SFXT)((ORC_CAT(orc_filter, SFXT)*)f);                                         \
     }                                                                                                    \
+    /* fft_multiply (acc NULL) / three-operand fft_multiply_accumulate over n complex values */          \
+    EXPORT void ORC_CAT(orc_fft_multiply, SFXT)(REALT * dst, const REALT* acc, const REALT* a,           \
+                                                const REALT* b, size_t n, int perm)                      \
+    {                                                                                                    \
+        typedef ORC_CAT(cpx, SFXT) C;                                                                    \
+        if (acc)                                                                                         \
+            ORC_CAT(fft_mac3, SFXT)((C*)dst, (const C*)acc, (const C*)a, (const C*)b, n, perm);          \
+        else                                                                                             \
+            ORC_CAT(fft_mul, SFXT)((C*)dst, (const C*)a, (const C*)b, n, perm);                          \
+    }                                                                                                    \
     /* plan description for tests: returns number of passes (0 for Bluestein), fills radices */         \
     EXPORT int ORC_CAT(orc_plan_info, SFXT)(size_t n, int* radices, int max_radices, size_t* bluestein_m) \
     {                                                                                                    \

@@ -36,16 +36,22 @@ def ref_sources() -> str | None:
     return None
 
 
-def build_command(ref: bool = False) -> list[str]:
-    """make command for liboracle.so (and, if asked and the reference sources exist, the reference library)."""
-    src = ref_sources() if ref else None
-    targets = ["oracle"] + (["ref", f"KFR_SRC={src}"] if src else [])
-    return ["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}"] + targets
+def build_command(ref: bool = False) -> list[str] | None:
+    """make command for liboracle.so (ref=False) or for the reference library (ref=True; None when the
+    reference sources are absent)."""
+    if not ref:
+        return ["make", "-s", "-C", HERE, "oracle"]
+    src = ref_sources()
+    return ["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", "ref", f"KFR_SRC={src}"] if src else None
 
 
 def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and, if asked and the reference sources exist, the reference library)."""
-    subprocess.check_call(build_command(ref))
+    """Compile liboracle.so and, if asked and the reference sources exist, try the reference library (a
+    failure there leaves only the restatement available)."""
+    subprocess.check_call(build_command(False))
+    cmd = build_command(True) if ref else None
+    if cmd and subprocess.call(cmd) != 0:
+        print("oracle/_ref: the reference library did not build; the oracle's restatement stays available")
 
 
 def available(kind: str) -> bool:
@@ -121,6 +127,24 @@ class Oracle:
         n = x.shape[-1]
         out = np.empty_like(x)
         return float(f(_p(out), _p(x), n, x.size // n, int(inverse), threads, reps))
+
+    def fft_multiply(self, a, b, acc=None, perm=False):
+        """fft_multiply(a, b) or, with acc, fft_multiply_accumulate(acc, a, b) along the last axis (element 0
+        part by part in the Perm format); precision follows a's dtype (complex64 or complex128)."""
+        a = np.ascontiguousarray(a)
+        f = getattr(self.lib, self.pre + "fft_multiply" + ("_f64" if a.dtype == np.complex128 else "_f32"))
+        f.restype = None
+        f.argtypes = [_ptr, _ptr, _ptr, _ptr, _c_size, _c_int]
+        b = np.ascontiguousarray(np.broadcast_to(b, a.shape), dtype=a.dtype)
+        acc = None if acc is None else np.ascontiguousarray(np.broadcast_to(acc, a.shape), dtype=a.dtype)
+        out = np.empty_like(a)
+        n = a.shape[-1]
+        for i in range(a.size // n if n else 0):
+            sl = np.s_[i * n:(i + 1) * n]
+            o, x, y = out.reshape(-1)[sl], a.reshape(-1)[sl], b.reshape(-1)[sl]
+            z = None if acc is None else acc.reshape(-1)[sl]
+            f(_p(o), None if z is None else _p(z), _p(x), _p(y), n, int(perm))
+        return out
 
     # ---- real DFT ----------------------------------------------------------------------------------
     def dft_real(self, x, ccs=True, precision="f64", threads=1):

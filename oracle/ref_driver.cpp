@@ -311,6 +311,37 @@ extern "C" __attribute__((visibility("default"))) double ref_dft_time_f32(float*
     return best;
 }
 
+// kfr::fft_multiply (acc NULL) and the three-operand kfr::fft_multiply_accumulate over n complex values
+// (include/kfr/dft/fft.hpp:983-1020).
+template <typename T>
+void run_fft_multiply(T* dst, const T* acc, const T* a, const T* b, size_t n, int perm)
+{
+    using C = complex<T>;
+    univector<C> d(n), s1(reinterpret_cast<const C*>(a), reinterpret_cast<const C*>(a) + n),
+        s2(reinterpret_cast<const C*>(b), reinterpret_cast<const C*>(b) + n);
+    const dft_pack_format fmt = perm ? dft_pack_format::Perm : dft_pack_format::CCs;
+    if (acc)
+    {
+        univector<C> s0(reinterpret_cast<const C*>(acc), reinterpret_cast<const C*>(acc) + n);
+        fft_multiply_accumulate(d, s0, s1, s2, fmt);
+    }
+    else
+        fft_multiply(d, s1, s2, fmt);
+    std::memcpy(dst, d.data(), n * sizeof(C));
+}
+extern "C" __attribute__((visibility("default"))) void ref_fft_multiply_f32(float* dst, const float* acc,
+                                                                           const float* a, const float* b,
+                                                                           size_t n, int perm)
+{
+    run_fft_multiply<float>(dst, acc, a, b, n, perm);
+}
+extern "C" __attribute__((visibility("default"))) void ref_fft_multiply_f64(double* dst, const double* acc,
+                                                                           const double* a, const double* b,
+                                                                           size_t n, int perm)
+{
+    run_fft_multiply<double>(dst, acc, a, b, n, perm);
+}
+
 extern "C" __attribute__((visibility("default"))) void ref_dft_dump_f32(size_t n)
 {
     dft_plan<float> plan(n);

@@ -147,8 +147,29 @@ def main() -> None:
         fm[f"rinv_{i}"] = ref.dft_md_real(S, inverse=True, shape=shp)
     fm["nr"] = np.array(len(md_real_shapes))
     np.savez_compressed(os.path.join(HERE, "dft_md.npz"), **fm)
+    fft_multiply_fixture(ref)
     print("golden fixtures written to", HERE)
 
 
+def fft_multiply_fixture(ref) -> None:
+    """fft_multiply / fft_multiply_accumulate (include/kfr/dft/fft.hpp:983-1020), CCs and Perm, f32 and f64,
+    from their own seeded stream so that the other fixtures do not change when this one is added."""
+    rng = np.random.default_rng(SEED + 5)
+    ff = {}
+    n = 1025  # a 2048-point real spectrum in CCs; Perm uses the first 1024 elements
+    for prec, dt in (("f64", np.complex128), ("f32", np.complex64)):
+        a, b, c = ((rng.uniform(-1, 1, (3, n)) + 1j * rng.uniform(-1, 1, (3, n))).astype(dt) for _ in range(3))
+        ff[f"a_{prec}"], ff[f"b_{prec}"], ff[f"c_{prec}"] = a, b, c
+        for fmt, m in (("ccs", n), ("perm", n - 1)):
+            perm = fmt == "perm"
+            ff[f"mul_{fmt}_{prec}"] = ref.fft_multiply(a[:, :m], b[:, :m], perm=perm)
+            ff[f"mac_{fmt}_{prec}"] = ref.fft_multiply(a[:, :m], b[:, :m], acc=c[:, :m], perm=perm)
+    np.savez_compressed(os.path.join(HERE, "fft_multiply.npz"), **ff)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["fft_multiply"]:
+        build(ref=True)
+        fft_multiply_fixture(Oracle("ref"))
+    else:
+        main()

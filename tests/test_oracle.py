@@ -171,3 +171,21 @@ def test_real_dft_requires_even_size(orc):
     """include/kfr/dft/fft.hpp:485: dft_plan_real requires size to be even."""
     with pytest.raises(ValueError):
         orc.dft_real(np.zeros(7))
+
+
+def test_fft_multiply_matches_reference_fixtures(orc):
+    """fft_multiply / fft_multiply_accumulate (include/kfr/dft/fft.hpp:983-1020), both packings, against
+    the reference's own outputs: products agree to the last bits (one rounding of a complex product)."""
+    f = load_golden("fft_multiply.npz")
+    for prec, eps in (("f64", 2.0**-52), ("f32", 2.0**-23)):
+        a, b, c = f[f"a_{prec}"], f[f"b_{prec}"], f[f"c_{prec}"]
+        for fmt, m in (("ccs", a.shape[1]), ("perm", a.shape[1] - 1)):
+            perm = fmt == "perm"
+            got = orc.fft_multiply(a[:, :m], b[:, :m], perm=perm)
+            assert np.max(np.abs(got - f[f"mul_{fmt}_{prec}"])) <= 4 * eps
+            got = orc.fft_multiply(a[:, :m], b[:, :m], acc=c[:, :m], perm=perm)
+            assert np.max(np.abs(got - f[f"mac_{fmt}_{prec}"])) <= 8 * eps
+            # Perm: element 0 is the part-by-part product (DC and Nyquist are both real)
+            if perm:
+                want0 = a[:, 0].real * b[:, 0].real + 1j * a[:, 0].imag * b[:, 0].imag
+                assert np.allclose(f[f"mul_{fmt}_{prec}"][:, 0], want0, rtol=4 * eps)
