@@ -368,35 +368,38 @@ def measure_rows(torch, k, dev, stream, hbm, with_cpu):
                         "plan": plan.describe()[:60]}
         del x, y, tmp, plan
     rows["pow2_c32_1GiB"] = pw
-    # tensor-core radix-16 plans beside the FP32 CUDA-core plan: N = 4096, 1 GiB batch, the precision workload
-    # (sum of 64 random sinusoids + 1e-3 noise) for the errors against numpy's FP64 FFT
-    n = 4096
-    b = (1 << 30) // (8 * n)
-    X = torch.randn(b, n, dtype=torch.complex64, device=dev, generator=g)
-    Y = torch.empty_like(X)
-    rs = np.random.default_rng(4096)
-    t = np.arange(n)
-    xs = np.zeros((16, n), np.complex128)
-    for i in range(16):
-        f, am, ph = rs.uniform(0, n, 64), rs.uniform(0, 1, 64), rs.uniform(0, 2 * np.pi, 64)
-        xs[i] = (am[:, None] * np.exp(1j * (2 * np.pi * f[:, None] * t[None, :] / n + ph[:, None]))).sum(0)
-    xs = (xs + 1e-3 * (rs.standard_normal((16, n)) + 1j * rs.standard_normal((16, n)))).astype(np.complex64)
-    ref = np.fft.fft(xs.astype(np.complex128), axis=-1)
-    xd = torch.from_numpy(xs).to(dev)
-    yd = torch.empty_like(xd)
-    tc = {}
-    for name, plan in (("fp32_cuda_cores", k.dft_plan(n)), ("tensor_bf16x2", k.dft_plan_tensor(n, "bf16")),
-                       ("tensor_fp16x2", k.dft_plan_tensor(n, "fp16"))):
-        tmp = torch.empty(max(1, plan.temp_size_batch(b)), dtype=torch.uint8, device=dev)
-        ms = timed(lambda: plan.execute_batch(Y, X, b, temp=tmp, stream=stream))
-        plan.execute_batch(yd, xd, 16)
-        y = yd.cpu().numpy()
-        tc[name] = {"ms": round(ms, 4), "gbs": round(16 * n * b / (ms * 1e-3) / 1e9, 1),
-                    "rel_rms": float(f"{rel_rms(y, ref):.3e}"),
-                    "max_rel": float(f"{np.max(np.abs(y - ref)) / np.max(np.abs(ref)):.3e}")}
-        del tmp
-    rows["tensor_core_c32_4096_1GiB"] = tc
-    del X, Y, flush
+    # the precision configuration: c32 at N = 2^12, 2^16, 2^20, 2^24 with 1 GiB batches, the FP32 CUDA-core plan
+    # beside the tensor-core radix-16 plans (FP16 hi + lo scaled per butterfly; BF16 hi + mid + lo); errors on
+    # the precision workload (sum of 64 random sinusoids + 1e-3 noise) against numpy's FP64 FFT
+    from kfr_gb300.workloads import precision_signals
+
+    prec = {}
+    for e, nerr in ((12, 8), (16, 4), (20, 2), (24, 1)):
+        n = 1 << e
+        b = (1 << 30) // (8 * n)
+        X = torch.randn(b, n, dtype=torch.complex64, device=dev, generator=g)
+        Y = torch.empty_like(X)
+        xs = precision_signals(n, nerr, 4000 + e)
+        ref = np.fft.fft(xs.astype(np.complex128), axis=-1)
+        xd = torch.from_numpy(xs).to(dev)
+        yd = torch.empty_like(xd)
+        row = {"batch": b}
+        for name, plan in (("fp32_cuda_cores", k.dft_plan(n)), ("tensor_fp16x2_scaled", k.dft_plan_tensor(n, "fp16")),
+                           ("tensor_bf16x3", k.dft_plan_tensor(n, "bf16"))):
+            tmp = torch.empty(max(1, plan.temp_size_batch(b)), dtype=torch.uint8, device=dev)
+            ms = timed(lambda: plan.execute_batch(Y, X, b, temp=tmp, stream=stream), reps=3)
+            plan.execute_batch(yd, xd, nerr, temp=tmp)
+            y = yd.cpu().numpy()
+            gbs = 16 * n * b / (ms * 1e-3) / 1e9
+            row[name] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / hbm, 4),
+                         "rel_rms": float(f"{rel_rms(y, ref):.3e}"),
+                         "max_rel": float(f"{np.max(np.abs(y - ref)) / np.max(np.abs(ref)):.3e}"),
+                         "plan": plan.describe()[:90]}
+            del tmp, plan
+        prec[f"2^{e}"] = row
+        del X, Y, xd, yd
+    rows["precision_c32_1GiB"] = prec
+    del flush
     return rows
 
 

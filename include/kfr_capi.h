@@ -191,8 +191,11 @@ KFR_API_SPEC void kfr_dct_delete_plan_f32(KFR_DCT_PLAN_F32* plan); /* capi.h:630
 KFR_API_SPEC void kfr_dct_delete_plan_f64(KFR_DCT_PLAN_F64* plan); /* capi.h:636 */
 
 /* ---- filters ------------------------------------------------------------------------------------------
- * The FFT convolution filter (convolve_filter) is the GPU path.  The FIR and IIR creators are declared for
- * link compatibility; they are not DFT work, are not built here and return NULL with an error message. */
+ * The FFT convolution filter (convolve_filter) is the GPU path.  FIR plans run through it too: the
+ * reference's fir_filter and convolve_filter compute the same y[n] = sum_k taps[k] x[n - k] with state kept
+ * across process calls (docs/docs/fir.md:94), so a FIR plan is a convolution filter with the default block;
+ * results match the direct form to floating-point rounding.  The IIR creators are declared for link
+ * compatibility; IIR filtering is not DFT work, is not built here and returns NULL with an error message. */
 KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_fir_plan_f32(const kfr_f32* taps, size_t size); /* capi.h:644 */
 KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_fir_plan_f64(const kfr_f64* taps, size_t size); /* capi.h:652 */
 KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_convolution_plan_f32(const kfr_f32* taps, size_t size,
@@ -308,10 +311,13 @@ KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_convolution_plan_channels_f64(con
                                                                            size_t block_size, size_t channels);
 
 /* Tensor-core plans (no counterpart in the reference): a complex plan whose radix-16 passes run on the tensor
- * cores as DFT-matrix contractions with each operand split into a high and a low 16-bit part
- * (split = 1: BF16, 2: FP16), products hi*hi + hi*lo + lo*hi accumulated in FP32.  Lengths 256 and 4096.  The
- * handle is an ordinary KFR_DFT_PLAN_F32 (execute, batch, describe, delete as usual).  Accuracy is below the
- * FP32 CUDA-core plans' (the dropped lo*lo term and 16-bit operands); the tests report it against FP64. */
+ * cores as DFT-matrix contractions with each FP32 operand split into 16-bit parts, products accumulated in
+ * FP32.  split = 1: three BF16 parts (hi + mid + lo), the six products down to 2^-16 of the leading one;
+ * split = 2: FP16 hi + lo after a power-of-two scaling of each butterfly's inputs, products hi*hi + hi*lo +
+ * lo*hi.  Lengths 256 and 4096 (one CTA per signal group) and 65536 = 256 x 256, 2^20 = 256 x 4096 and
+ * 2^24 = 4096 x 4096 (four-step: scratch of one signal per signal, like the CUDA-core four-step).  The handle
+ * is an ordinary KFR_DFT_PLAN_F32 (execute, batch, describe, delete as usual); the tests report its error
+ * against FP64 beside the FP32 CUDA-core plan's. */
 KFR_API_SPEC KFR_DFT_PLAN_F32* kfr_dft_create_plan_tensor_f32(size_t size, int split);
 
 /* Uneven batch (no counterpart in the reference, whose callers loop over one plan per length): `count` complex
@@ -330,6 +336,20 @@ KFR_API_SPEC void kfr_dft_uneven_execute_per_signal_f32(KFR_DFT_UNEVEN_F32* plan
                                                         kfr_bool inverse, void* stream);
 KFR_API_SPEC size_t kfr_dft_uneven_describe_f32(KFR_DFT_UNEVEN_F32* plan, char* buf, size_t size);
 KFR_API_SPEC void kfr_dft_uneven_delete_plan_f32(KFR_DFT_UNEVEN_F32* plan);
+
+/* Failure detection (no counterpart in the reference).  Every wait of a kernel -- for a bulk copy into its
+ * shared memory, or (uneven batch) for an earlier stage of its signal -- gives up after a bounded number of
+ * polling rounds.  The kernel then sets its plan's device error flag, lets its own copies in flight land
+ * (waiting at most the default limit again) and returns or carries on; the next synchronous call on that plan
+ * reports "... gave up waiting ..." through kfr_last_error() and clears the flag.  With a stream, the flag is
+ * read by the next synchronous call on the same plan.
+ *   kfr_set_wait_limit: polling rounds for launches issued from now on (KFR_DEFAULT_WAIT_SPINS, about a
+ *     second or more; 0 makes every wait give up at its first poll, for tests); returns the previous value.
+ *   kfr_dft_uneven_set_unreachable_stage_f32: test hook; nonzero makes every tile that depends on an earlier
+ *     stage wait for one more tile than that stage has, so the wait runs out after the limit. */
+#define KFR_DEFAULT_WAIT_SPINS (1u << 22)
+KFR_API_SPEC uint32_t kfr_set_wait_limit(uint32_t spins);
+KFR_API_SPEC void kfr_dft_uneven_set_unreachable_stage_f32(KFR_DFT_UNEVEN_F32* plan, kfr_bool unreachable);
 
 /* Adjoints (vector-Jacobian products) for gradient-based callers; no counterpart in the reference, which has
  * no differentiation.  Each maps the gradient of a transform's output (grad_out) to the gradient of its input

@@ -26,7 +26,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libkfr_capi.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "kfr_capi.h")
 
 __all__ = ["KfrError", "lib", "dft_plan", "dft_plan_md", "dft_plan_real", "dft_plan_md_real", "dct_plan",
-           "convolve_filter", "declared_symbols", "fft_multiply", "CCs", "Perm"]
+           "convolve_filter", "fir_filter", "declared_symbols", "fft_multiply", "CCs", "Perm"]
 
 CCs = 1
 Perm = 0
@@ -111,6 +111,8 @@ _SIGS.update({
     "kfr_release": (None, [_P]),
     "kfr_allocated_size": (_S, [_P]),
     "kfr_dft_describe_f64": (_S, [_P, ctypes.c_char_p, _S]),
+    "kfr_set_wait_limit": (ctypes.c_uint32, [ctypes.c_uint32]),
+    "kfr_dft_uneven_set_unreachable_stage_f32": (None, [_P, _B]),
     "kfr_fft_multiply_f32": (None, [_P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
     "kfr_fft_multiply_f64": (None, [_P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
     "kfr_fft_multiply_accumulate_f32": (None, [_P, _P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
@@ -275,8 +277,8 @@ class dft_plan(_plan):
 
 
 class dft_plan_tensor(dft_plan):
-    """Complex c32 plan whose radix-16 passes run on the tensor cores with split hi + lo operands
-    (split: "bf16" or "fp16"); lengths 256 and 4096."""
+    """Complex c32 plan whose radix-16 passes run on the tensor cores with split 16-bit operands (split:
+    "bf16" = hi + mid + lo, "fp16" = scaled hi + lo); lengths 256, 4096, 2^16, 2^20 and 2^24."""
 
     def __init__(self, size: int, split="fp16"):
         mode = {"bf16": 1, "fp16": 2}[split]
@@ -453,6 +455,22 @@ class convolve_filter(_plan):
 
     def reset(self):
         _call(self._fn("reset"), self.handle)
+
+
+class fir_filter(convolve_filter):
+    """Streaming FIR filter (fir_filter<T>, include/kfr/dsp/fir.hpp; kfr_filter_create_fir_plan_*): y[n] =
+    sum_k taps[k] x[n - k], state across apply() until reset(), computed through the FFT convolution path."""
+
+    def __init__(self, taps, dtype=None):
+        if dtype is None:
+            dtype = getattr(taps, "dtype", "f32")
+        sfx = _sfx(dtype)
+        if isinstance(taps, np.ndarray):
+            taps = np.ascontiguousarray(taps, dtype=np.float32 if sfx == "f32" else np.float64)
+        self._taps = taps
+        self.channels = 1
+        n = taps.numel() if hasattr(taps, "numel") else len(taps)
+        _plan.__init__(self, _call(f"kfr_filter_create_fir_plan_{sfx}", _addr(taps), n), sfx)
 
 
 def _conv_sfx(x):

@@ -169,6 +169,8 @@ struct dft_obj : plan_base
     {
         if (eng1)
             eng1->check_device_error();
+        else
+            md->check_device_error();
     }
 };
 
@@ -218,6 +220,13 @@ struct real_obj : plan_base
             md->inverse(o, i, b, s, st);
     }
     std::string describe() const { return eng1 ? eng1->describe() : md->describe(); }
+    void check_device_error() const
+    {
+        if (eng1)
+            eng1->check_device_error();
+        else
+            md->check_device_error();
+    }
 };
 
 template <typename T>
@@ -421,6 +430,8 @@ void exec_real(void* h, size_t batch, void* out, const void* in, uint8_t* temp, 
             run(*p, out, rbytes, in, cbytes, temp, scr, stream, alias,
                 [&](void* o, const void* i, void* s, cudaStream_t st) { p->inverse(o, i, (long long)batch, s, st); });
     }
+    if (!stream)
+        p->check_device_error();
 }
 
 template <typename T>
@@ -438,6 +449,8 @@ void exec_dct(void* h, size_t batch, void* out, const void* in, uint8_t* temp, b
             [&](void* o, const void* i, long long nb, void* s, cudaStream_t st) { p->eng.execute(o, i, nb, inverse, s, st); }))
         run(*p, out, bytes, in, bytes, temp, scr, stream, false,
             [&](void* o, const void* i, void* s, cudaStream_t st) { p->eng.execute(o, i, (long long)batch, inverse, s, st); });
+    if (!stream)
+        p->eng.check_device_error();
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -1295,13 +1308,20 @@ KFR_API_SPEC void kfr_dct_delete_plan_f64(KFR_DCT_PLAN_F64* plan)
 }
 
 // ---- filters -------------------------------------------------------------------------------------------
-KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_fir_plan_f32(const kfr_f32*, size_t)
+// FIR filters run through the DFT path: the reference's fir_filter (src/capi/capi.cpp:567-580) and its
+// convolve_filter compute the same y[n] = sum_k taps[k] x[n - k] with state across calls (its docs:
+// docs/docs/fir.md:94), so a FIR plan is a convolution-filter plan with the default block.
+KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_fir_plan_f32(const kfr_f32* taps, size_t size)
 {
-    return try_fn([]() -> KFR_FILTER_F32* { not_built("kfr_filter_create_fir_plan_f32"); }, (KFR_FILTER_F32*)nullptr);
+    return try_fn(
+        [&] { return reinterpret_cast<KFR_FILTER_F32*>(static_cast<plan_base*>(new filter_obj<float>(taps, size, 1024))); },
+        (KFR_FILTER_F32*)nullptr);
 }
-KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_fir_plan_f64(const kfr_f64*, size_t)
+KFR_API_SPEC KFR_FILTER_F64* kfr_filter_create_fir_plan_f64(const kfr_f64* taps, size_t size)
 {
-    return try_fn([]() -> KFR_FILTER_F64* { not_built("kfr_filter_create_fir_plan_f64"); }, (KFR_FILTER_F64*)nullptr);
+    return try_fn(
+        [&] { return reinterpret_cast<KFR_FILTER_F64*>(static_cast<plan_base*>(new filter_obj<double>(taps, size, 1024))); },
+        (KFR_FILTER_F64*)nullptr);
 }
 KFR_API_SPEC KFR_FILTER_F32* kfr_filter_create_iir_plan_f32(const kfr_f32*, size_t)
 {
@@ -1433,6 +1453,21 @@ KFR_API_SPEC void kfr_dft_uneven_execute_f32(KFR_DFT_UNEVEN_F32* plan, kfr_c32* 
                                              void* stream)
 {
     try_void([&] { exec_uneven(plan, out, in, inverse != 0, stream, false); });
+}
+KFR_API_SPEC uint32_t kfr_set_wait_limit(uint32_t spins)
+{
+    static_assert(KFR_DEFAULT_WAIT_SPINS == kfr_gpu::kDefaultWaitSpins, "one default wait limit");
+    return set_wait_limit(spins);
+}
+KFR_API_SPEC void kfr_dft_uneven_set_unreachable_stage_f32(KFR_DFT_UNEVEN_F32* plan, kfr_bool unreachable)
+{
+    try_void(
+        [&]
+        {
+            auto* p = as<uneven_obj>(plan, TAG_UNEVEN);
+            std::unique_lock<std::mutex> lock(p->mu);
+            p->plan.set_unreachable_stage(unreachable != 0);
+        });
 }
 KFR_API_SPEC void kfr_dft_uneven_execute_per_signal_f32(KFR_DFT_UNEVEN_F32* plan, kfr_c32* out, const kfr_c32* in,
                                                         kfr_bool inverse, void* stream)

@@ -227,12 +227,15 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     {
         cpx<T>* in_t   = tiles + bi * slen;
         cpx<T>* scr_t  = tiles + bs * slen;
-        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1);
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
-                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                atomicExch(err, 1);
+                // the copy waited for is the only load in flight (the next one is issued after this wait):
+                // give it a bounded chance to land in this CTA's shared memory before the CTA exits
+                mbar_wait(&bars[bi], (phase >> bi) & 1);
                 bulk_wait_all();
             }
             return;
@@ -325,11 +328,18 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     }
     for (uint32_t phase = 0; s < nsig; s += gridDim.x, phase ^= 1)
     {
-        const bool got = mbar_wait(&bars[0], phase) && mbar_wait(&bars[1], phase);
+        const bool got = mbar_wait(&bars[0], phase, a.wait_spins) && mbar_wait(&bars[1], phase, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
-                atomicExch(err, 1); // nothing else is in flight: the next copies are issued after these waits
+            {
+                atomicExch(err, 1);
+                // the two halves waited for are the only copies in flight (the next ones are issued after
+                // these waits): give them a bounded chance to land before the CTA exits
+                mbar_wait(&bars[0], phase);
+                mbar_wait(&bars[1], phase);
+                bulk_wait_all();
+            }
             return;
         }
         const long long sn = s + gridDim.x;
@@ -564,15 +574,16 @@ __global__ void __launch_bounds__(F::max_threads, 1)
         cpx<T>* in_t   = tiles + bi * stage_elems;
         cpx<T>* scr_t  = tiles + bs * stage_elems;
         cpx<T>* spare  = tiles + bn * stage_elems;
-        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1);
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
                 atomicExch(err, 1);
-                // give the other copies in flight (if any) a bounded chance to land before the CTA exits
+                // give every copy in flight (the one waited for included) a bounded chance to land before
+                // the CTA exits
                 for (int b = 0; b < 3; b++)
-                    if (b != bi && ((pending >> b) & 1))
+                    if ((pending >> b) & 1)
                         mbar_wait(&bars[b], (phase >> b) & 1);
                 bulk_wait_all();
             }
@@ -756,12 +767,15 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     {
         cpx<T>* in_t   = tiles + bi * slen;
         cpx<T>* scr_t  = tiles + bs * slen;
-        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1);
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
-                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                atomicExch(err, 1);
+                // the copy waited for is the only load in flight (the next one is issued after this wait):
+                // give it a bounded chance to land in this CTA's shared memory before the CTA exits
+                mbar_wait(&bars[bi], (phase >> bi) & 1);
                 bulk_wait_all();
             }
             return;
@@ -937,12 +951,15 @@ __global__ void __launch_bounds__(F::max_threads, 1)
     {
         cpx<T>* in_t   = tiles + bi * slen;
         cpx<T>* scr_t  = tiles + bs * slen;
-        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1);
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
-                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                atomicExch(err, 1);
+                // the copy waited for is the only load in flight (the next one is issued after this wait):
+                // give it a bounded chance to land in this CTA's shared memory before the CTA exits
+                mbar_wait(&bars[bi], (phase >> bi) & 1);
                 bulk_wait_all();
             }
             return;
@@ -1466,12 +1483,15 @@ __global__ void __launch_bounds__(fspt_threads<FA>(), fspt_min_ctas<FA>())
     {
         const int s    = it & 1;
         cpx<T>* stage  = st0 + s * SE;
-        const bool got = mbar_wait(&bars[s], (it >> 1) & 1);
+        const bool got = mbar_wait(&bars[s], (it >> 1) & 1, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
-                atomicExch(err, 1); // no other load is in flight: the next one is issued after this wait
+                atomicExch(err, 1);
+                // the copy waited for is the only load in flight (the next one is issued after this wait):
+                // give it a bounded chance to land before the CTA exits
+                mbar_wait(&bars[s], (it >> 1) & 1);
                 bulk_wait_all();
             }
             return;
@@ -1568,12 +1588,15 @@ __global__ void __launch_bounds__(fspt_threads<FB>(), fspt_min_ctas<FB>())
     {
         const int s    = it & 1;
         cpx<T>* stage  = st0 + s * SE;
-        const bool got = mbar_wait(&bars[s], (it >> 1) & 1);
+        const bool got = mbar_wait(&bars[s], (it >> 1) & 1, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
                 atomicExch(err, 1);
+                // the copy waited for is the only load in flight (the next one is issued after this wait):
+                // give it a bounded chance to land before the CTA exits
+                mbar_wait(&bars[s], (it >> 1) & 1);
                 bulk_wait_all();
             }
             return;

@@ -81,8 +81,10 @@ static cudaError_t go_persistent(K kernel, const block_cfg& c, long long ntiles,
     return cudaGetLastError();
 }
 
-cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
+cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a0, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
 {
+    c2c_args a   = a0;
+    a.wait_spins = wait_limit();
 #define KFR_GPU_PIPE_CASE(N, TS, ...)                                                                      \
     case N:                                                                                                \
         return go_persistent(k_c2c_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);
@@ -104,8 +106,10 @@ static cudaError_t go_reg(const c2c_args& a, const block_cfg& c, long long nsig,
         return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st)
+cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a0, const block_cfg& c, long long nsig, int* err, cudaStream_t st)
 {
+    c2c_args a   = a0;
+    a.wait_spins = wait_limit();
 #define KFR_GPU_REG_CASE(N, TS, ...)                                                                       \
     case N: return go_reg<ct_fft<float, N, TS, __VA_ARGS__>>(a, c, nsig, err, st);
     switch (c.ct)
@@ -116,8 +120,10 @@ cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a, const block_cfg& c, long lo
 #undef KFR_GPU_REG_CASE
 }
 
-cudaError_t launch_ct_r2c_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
+cudaError_t launch_ct_r2c_pipe_f32(const real_args& a0, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
 {
+    real_args a  = a0;
+    a.wait_spins = wait_limit();
 #define KFR_GPU_R2C_PIPE_CASE(N, TS, ...)                                                                  \
     case N:                                                                                                \
         return go_persistent(k_r2c_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);
@@ -129,8 +135,10 @@ cudaError_t launch_ct_r2c_pipe_f32(const real_args& a, const block_cfg& c, long 
 #undef KFR_GPU_R2C_PIPE_CASE
 }
 
-cudaError_t launch_ct_c2r_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
+cudaError_t launch_ct_c2r_pipe_f32(const real_args& a0, const block_cfg& c, long long ntiles, int* err, cudaStream_t st)
 {
+    real_args a  = a0;
+    a.wait_spins = wait_limit();
 #define KFR_GPU_C2R_PIPE_CASE(N, TS, ...)                                                                  \
     case N:                                                                                                \
         return go_persistent(k_c2r_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);
@@ -142,9 +150,11 @@ cudaError_t launch_ct_c2r_pipe_f32(const real_args& a, const block_cfg& c, long 
 #undef KFR_GPU_C2R_PIPE_CASE
 }
 
-cudaError_t launch_ct_rader_tile_f32(const rader_args& a, const block_cfg& c, long long ntiles, int* err,
+cudaError_t launch_ct_rader_tile_f32(const rader_args& a0, const block_cfg& c, long long ntiles, int* err,
                                      cudaStream_t st)
 {
+    rader_args a = a0;
+    a.wait_spins = wait_limit();
 #define KFR_GPU_RTILE_CASE(N, TS, ...)                                                                     \
     case N:                                                                                                \
         return go_persistent(k_rader_tile<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);

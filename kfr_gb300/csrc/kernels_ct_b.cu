@@ -196,8 +196,10 @@ static cudaError_t go_fsp_pair(const fourstep_args& a, bool cols, cudaStream_t s
         return cudaErrorNotSupported;
 }
 
-cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st)
+cudaError_t launch_ct_fsp_f32(const fourstep_args& a0, bool cols, cudaStream_t st)
 {
+    fourstep_args a = a0;
+    a.wait_spins    = wait_limit();
 #define KFR_GPU_FSP_CASE(A, B)                                                                             \
     if (a.n1 == A && a.n2 == B)                                                                            \
     {                                                                                                      \

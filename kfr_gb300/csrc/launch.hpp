@@ -10,6 +10,15 @@
 namespace kfr_gpu
 {
 
+// Polling rounds after which a kernel's wait for a bulk copy (mbarrier try_wait rounds, each suspending for
+// a bounded, hardware-defined time) or for an earlier stage of its signal (256 ns sleeps) gives up: about a
+// second or more.  On expiry the kernel sets its plan's device error flag, lets its own copies in flight
+// land (waiting at most this default again) and returns.
+constexpr unsigned kDefaultWaitSpins = 1u << 22;
+// The limit that launches issued from now on carry (kfr_set_wait_limit; 0 gives up at the first poll).
+unsigned wait_limit();
+unsigned set_wait_limit(unsigned spins);
+
 // Shape of one shared-memory FFT launch: `spc` signals per CTA, `ts` threads per signal, each thread owning
 // at most `ept` elements per pass.
 struct block_cfg
@@ -34,6 +43,7 @@ struct c2c_args
     const void* tw;
     fast_div div_n;
     fft_desc d;
+    unsigned wait_spins = kDefaultWaitSpins; // persistent pipelined kernels: see kDefaultWaitSpins
 };
 
 // Bluestein chirp-z for lengths n whose power-of-two convolution size M = d.n fits one CTA.
@@ -71,6 +81,7 @@ struct rader_args
     const void* tw2;  // tiled kernel: twiddles of the radices in reverse order
     fast_div div_n, div_l;
     fft_desc d;
+    unsigned wait_spins = kDefaultWaitSpins; // persistent pipelined kernels: see kDefaultWaitSpins
 };
 
 // Real DFT of even length 2c through a c-point complex DFT (d.n = c).
@@ -87,6 +98,7 @@ struct real_args
     const void* tw;
     fast_div div_n, div_out;
     fft_desc d;
+    unsigned wait_spins = kDefaultWaitSpins; // persistent pipelined kernels: see kDefaultWaitSpins
 };
 
 // DCT-II / DCT-III of length n = d.n through an n-point complex DFT.
@@ -125,6 +137,7 @@ struct fourstep_args
     int pingpong;    // compile-time kernels: ping-pong passes over two buffers per signal (2x shared memory)
     fast_div div_n;  // divides by the FFT length of this pass
     int* err;        // persistent pair kernels: set when a wait for a tile copy runs out (may be null)
+    unsigned wait_spins = kDefaultWaitSpins;
 };
 
 template <typename T>

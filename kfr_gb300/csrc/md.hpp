@@ -45,6 +45,11 @@ public:
     void execute(void* out, const void* in, long long batch, bool inverse, void* scratch, cudaStream_t st) const;
     std::string describe() const;
     int launches(long long batch) const;
+    void check_device_error() const
+    {
+        if (last_)
+            last_->check_device_error();
+    }
 
 private:
     std::vector<long long> shape_;
@@ -66,6 +71,11 @@ public:
     void inverse(void* out, const void* in, long long batch, void* scratch, cudaStream_t st) const;
     std::string describe() const;
     int launches(long long batch) const;
+    void check_device_error() const
+    {
+        if (last_)
+            last_->check_device_error();
+    }
 
 private:
     std::vector<long long> shape_, cshape_;

@@ -5,12 +5,21 @@
 #include "ct_table.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <sstream>
 
 namespace kfr_gpu
 {
+
+namespace
+{
+std::atomic<unsigned> g_wait_spins{ kDefaultWaitSpins };
+} // namespace
+
+unsigned wait_limit() { return g_wait_spins.load(); }
+unsigned set_wait_limit(unsigned spins) { return g_wait_spins.exchange(spins); }
 
 void check(cudaError_t e, const char* what)
 {
@@ -505,15 +514,38 @@ static double fft_cost(long long n)
     return double(n) * c;
 }
 
+// Twiddles of the radix-16 passes of an L-point tensor-core block FFT (L = 16^p): the pass with stride
+// ns > 1 holds W_{16 ns}^{r k} at (r - 1) ns + k (r = 1..15, k < ns), passes in order.
+static std::vector<std::complex<float>> tc_pass_twiddles(int L)
+{
+    std::vector<std::complex<float>> tw;
+    for (int ns = 16; ns < L; ns *= 16)
+        for (int r = 1; r < 16; r++)
+            for (int k = 0; k < ns; k++)
+            {
+                const auto w = twiddle((long long)r * k, 16LL * ns);
+                tw.emplace_back(float(w.real()), float(w.imag()));
+            }
+    return tw;
+}
+
 template <typename T>
 complex_engine<T>::complex_engine(long long n, int tensor_mode) : n_(n)
 {
     if (sizeof(T) != 4 || (tensor_mode != TC_BF16 && tensor_mode != TC_FP16))
         throw std::invalid_argument("tensor-core plans are single precision with a BF16 or FP16 split");
-    if (n != 256 && n != 4096)
-        throw std::invalid_argument("tensor-core plans support lengths 256 and 4096 (radix-16 passes only)");
-    const std::vector<int> order(n == 256 ? 2 : 3, 16);
-    prog_.build(int(n), CT_NONE, &order, 16);
+    // one CTA for 16^2 and 16^3; a four-step of 256- and 4096-point passes for 2^16, 2^20 and 2^24
+    switch (n)
+    {
+    case 256:
+    case 4096: break;
+    case 1 << 16: n1_ = 256, n2_ = 256; break;
+    case 1 << 20: n1_ = 256, n2_ = 4096; break;
+    case 1 << 24: n1_ = 4096, n2_ = 4096; break;
+    default:
+        throw std::invalid_argument(
+            "tensor-core plans support lengths 256, 4096, 65536, 2^20 and 2^24 (radix-16 passes only)");
+    }
     std::vector<float> cs(512);
     for (int k = 0; k < 16; k++)
         for (int r = 0; r < 16; r++)
@@ -523,6 +555,37 @@ complex_engine<T>::complex_engine(long long n, int tensor_mode) : n_(n)
             cs[256 + k * 16 + r] = float(-w.imag());
         }
     tc_cs_.upload(cs.data(), cs.size() * sizeof(float));
+    const auto upload_tw = [](dbuf& b, int L)
+    {
+        const auto tw = tc_pass_twiddles(L);
+        b.upload(tw.data(), std::max<size_t>(1, tw.size()) * sizeof(std::complex<float>));
+    };
+    if (!n1_)
+        upload_tw(tc_tw1_, int(n));
+    else
+    {
+        upload_tw(tc_tw1_, int(n1_));
+        upload_tw(tc_tw2_, int(n2_));
+        // two-level table for W_N^m, m < N, as for the CUDA-core four-step
+        int lb = 0;
+        while ((1LL << (2 * lb)) < n)
+            lb++;
+        lbits_             = lb;
+        const long long nb = 1LL << lb, na = (n + nb - 1) / nb;
+        std::vector<std::complex<T>> A(na), B(nb);
+        for (long long i = 0; i < na; i++)
+        {
+            const auto w = twiddle(i * nb, n);
+            A[i]         = std::complex<T>(T(w.real()), T(w.imag()));
+        }
+        for (long long j = 0; j < nb; j++)
+        {
+            const auto w = twiddle(j, n);
+            B[j]         = std::complex<T>(T(w.real()), T(w.imag()));
+        }
+        twA_.upload(A.data(), A.size() * sizeof(std::complex<T>));
+        twB_.upload(B.data(), B.size() * sizeof(std::complex<T>));
+    }
     tc_mode_ = tensor_mode;
     k_       = kind::tensor;
 }
@@ -886,6 +949,7 @@ long long complex_engine<T>::scratch_elems(long long batch) const
     switch (k_)
     {
     case kind::fourstep: return batch * n_;
+    case kind::tensor: return n1_ ? batch * n_ : 0;
     case kind::bluestein_multi: return batch * m_ + inner_->scratch_elems(batch);
     default: return 0;
     }
@@ -902,7 +966,7 @@ int complex_engine<T>::launches(long long batch) const
     case kind::fourstep: return 2 * int((batch + 65534) / 65535);
     case kind::bluestein_multi: return 3 + 2 * inner_->launches(batch);
     case kind::rader_smem: return 1;
-    case kind::tensor: return 1;
+    case kind::tensor: return n1_ ? 2 * int((batch + 65534) / 65535) : 1;
     }
     return 0;
 }
@@ -918,16 +982,44 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
     {
     case kind::tensor:
     {
-        c2c_args a{};
-        a.in      = in;
-        a.out     = out;
-        a.batch   = batch;
-        a.istride = istride;
-        a.ostride = ostride;
-        a.inverse = inverse;
-        a.tw      = prog_.tw.get();
-        check(launch_c2c_tc_f32(a, int(n_), tc_mode_, static_cast<const float*>(tc_cs_.get()), st),
-              "launch tensor-core DFT");
+        if (!n1_)
+        {
+            c2c_args a{};
+            a.in      = in;
+            a.out     = out;
+            a.batch   = batch;
+            a.istride = istride;
+            a.ostride = ostride;
+            a.inverse = inverse;
+            a.tw      = tc_tw1_.get();
+            check(launch_c2c_tc_f32(a, int(n_), tc_mode_, static_cast<const float*>(tc_cs_.get()), st),
+                  "launch tensor-core DFT");
+            return;
+        }
+        if (istride != n_ || ostride != n_ || !scratch)
+            throw std::invalid_argument("tensor-core four-step plans need contiguous signals and scratch");
+        // batches of at most 65535 signals (the grid's second dimension)
+        for (long long b0 = 0; b0 < batch; b0 += 65535)
+        {
+            const long long nb = std::min<long long>(65535, batch - b0);
+            tc_fs_args a{};
+            a.batch   = nb;
+            a.n1      = int(n1_);
+            a.n2      = int(n2_);
+            a.inverse = inverse;
+            a.tw1     = tc_tw1_.get();
+            a.tw2     = tc_tw2_.get();
+            a.twA     = twA_.get();
+            a.twB     = twB_.get();
+            a.lbits   = lbits_;
+            a.cs      = static_cast<const float*>(tc_cs_.get());
+            a.in      = static_cast<const char*>(in) + b0 * n_ * esz;
+            a.out     = scratch;
+            check(launch_tc_fourstep_pass_f32(a, true, tc_mode_, st), "launch tensor-core column pass");
+            a.in  = scratch;
+            a.out = static_cast<char*>(out) + b0 * n_ * esz;
+            check(launch_tc_fourstep_pass_f32(a, false, tc_mode_, st), "launch tensor-core row pass");
+        }
         return;
     }
     case kind::trivial:
@@ -1159,8 +1251,12 @@ std::string complex_engine<T>::describe() const
     {
     case kind::trivial: s << "trivial n=" << n_; break;
     case kind::tensor:
-        s << "tensor-core n=" << n_ << " radix-16 passes as mma.sync contractions, "
-          << (tc_mode_ == TC_BF16 ? "BF16" : "FP16") << " hi+lo operands, FP32 accumulation";
+        s << "tensor-core n=" << n_;
+        if (n1_)
+            s << " = " << n1_ << " x " << n2_ << " four-step";
+        s << ", radix-16 passes as mma.sync contractions, "
+          << (tc_mode_ == TC_BF16 ? "BF16 hi+mid+lo" : "FP16 hi+lo per-butterfly scaled")
+          << " operands, FP32 accumulation";
         break;
     case kind::smem:
         s << "smem " << prog_.describe();
@@ -1188,6 +1284,21 @@ std::string complex_engine<T>::describe() const
 // ------------------------------------------------------------------------------------------------------
 // real_engine
 // ------------------------------------------------------------------------------------------------------
+
+template <typename T>
+void real_engine<T>::check_device_error() const
+{
+    ceng_.check_device_error();
+    if (!err_.get())
+        return;
+    int v = 0;
+    check(cudaMemcpy(&v, err_.get(), sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+    if (v)
+    {
+        cudaMemset(err_.get(), 0, sizeof(int));
+        throw cuda_error("a real DFT kernel gave up waiting for its input copy (device error flag set)");
+    }
+}
 
 template <typename T>
 real_engine<T>::real_engine(long long n) : n_(n), c_(n / 2), ceng_(n / 2)

@@ -145,8 +145,9 @@ public:
     };
 
     explicit complex_engine(long long n);
-    // Tensor-core form (single precision, n = 256 or 4096): every radix-16 pass as a contraction on the tensor
-    // cores with operands split into two 16-bit parts (mode: TC_BF16 or TC_FP16, tensor.hpp).
+    // Tensor-core form (single precision, n = 256, 4096, 2^16, 2^20 or 2^24): every radix-16 pass as a
+    // contraction on the tensor cores with operands split into 16-bit parts (mode: TC_BF16 or TC_FP16,
+    // tensor.hpp); lengths above 4096 run as a four-step of 256- and 4096-point passes.
     complex_engine(long long n, int tensor_mode);
 
     // Device scratch (in complex elements) that execute() needs for `batch` signals.
@@ -190,9 +191,9 @@ private:
     void init_rader(long long n);
     bool plan_fourstep(long long n);
     void plan_pipe();
-    // tensor-core form
+    // tensor-core form (n1_, n2_, twA_, twB_, lbits_ as for the four-step when n > 4096)
     int tc_mode_ = 0;
-    dbuf tc_cs_;
+    dbuf tc_cs_, tc_tw1_, tc_tw2_;
     // Rader
     dbuf pin_, qof_, gp_, rtw2_;
     int rader_spc_ = 0; // signals per tile of the pipelined kernel, 0 = not used
@@ -211,6 +212,8 @@ public:
     std::string describe() const;
     long long size() const { return n_; }
     int launches(long long batch) const;
+    // Throws if a kernel of this engine recorded a device-side error (a bounded wait that ran out).
+    void check_device_error() const;
 
 private:
     long long n_, c_;
@@ -233,6 +236,7 @@ public:
     std::string describe() const;
     long long size() const { return n_; }
     int launches(long long batch) const;
+    void check_device_error() const { ceng_.check_device_error(); }
 
 private:
     long long n_;

@@ -1,8 +1,8 @@
 // Bulk asynchronous copies (TMA, cp.async.bulk) and mbarriers, as inline PTX for sm_103a.
 //
-// Every wait is bounded: mbar_wait gives up after kMbarSpins try_wait rounds (each of which itself
-// suspends for a bounded, hardware-defined time) and reports failure, so a kernel can record an error and
-// return instead of spinning forever.
+// Every wait is bounded: mbar_wait gives up after a given number of try_wait rounds (each of which itself
+// suspends for a bounded, hardware-defined time; kMbarSpins by default) and reports failure, so a kernel can
+// record an error, let its own copies in flight land and return instead of spinning forever.
 #pragma once
 
 #include <cstdint>
@@ -39,10 +39,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// Bounded wait for the phase with the given parity to complete (at most `spins` try_wait rounds).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t spins = kMbarSpins)
 {
-    for (uint32_t i = 0; i < kMbarSpins; i++)
+    for (uint32_t i = 0; i < spins; i++)
         if (mbar_try_wait(bar, parity))
             return true;
     return false;

@@ -16,8 +16,6 @@ namespace kfr_gpu
 // kernel
 // ------------------------------------------------------------------------------------------------------
 
-constexpr uint32_t kUnevenWaitSpins = 1u << 22; // x 256 ns sleeps: about a second
-
 __device__ __forceinline__ int ld_acquire(const int* p)
 {
     int v;
@@ -85,14 +83,14 @@ __global__ void __launch_bounds__(kUnevenThreads, 1) k_uneven(const uneven_launc
                     // every tile of the stage waited for was dequeued before this one and runs on a resident
                     // CTA, so the counter reaches `need`; the bound only guards against a fault elsewhere
                     uint32_t spins = 0;
-                    while (ld_acquire(a.counters + J.wait) < J.need)
+                    while (ld_acquire(a.counters + J.wait) < J.need + a.stage_bias)
                     {
-                        __nanosleep(256);
-                        if (++spins > kUnevenWaitSpins)
+                        if (spins++ >= a.wait_spins)
                         {
-                            atomicExch(a.err, 1);
+                            atomicExch(a.err, 1); // carry on: the tile's loads stay inside its buffers
                             break;
                         }
+                        __nanosleep(256);
                     }
                 }
             }
@@ -730,13 +728,15 @@ void uneven_plan::enqueue(void* out, const void* in, bool inverse, cudaStream_t 
     uneven_launch L{ static_cast<uneven_fft*>(dffts_.get()), static_cast<uneven_job*>(djobs_.get()),
                      static_cast<uneven_item*>(ditems_.get()), static_cast<long long*>(doffsets_.get()), nitems_,
                      static_cast<int*>(dqueue_.get()), static_cast<int*>(dcounters_.get()),
-                     static_cast<int*>(derr_.get()), in, out, scratch_.get(), inverse ? 1 : 0 };
+                     static_cast<int*>(derr_.get()), in, out, scratch_.get(), inverse ? 1 : 0, wait_limit(),
+                     unreachable_ ? 1 : 0 };
     check(launch_uneven_f32(L, smem_, grid_, st), "launch uneven batch");
 }
 
 void uneven_plan::execute(void* out, const void* in, bool inverse, cudaStream_t st)
 {
-    if (!gexec_ || gin_ != in || gout_ != out || ginv_ != inverse)
+    if (!gexec_ || gin_ != in || gout_ != out || ginv_ != inverse || gspins_ != wait_limit() ||
+        gunreach_ != unreachable_)
     {
         if (gexec_)
         {
@@ -763,9 +763,11 @@ void uneven_plan::execute(void* out, const void* in, bool inverse, cudaStream_t 
         const cudaError_t e = cudaGraphInstantiate(&gexec_, g, 0);
         cudaGraphDestroy(g);
         check(e, "instantiate graph");
-        gin_  = in;
-        gout_ = out;
-        ginv_ = inverse;
+        gin_      = in;
+        gout_     = out;
+        ginv_     = inverse;
+        gspins_   = wait_limit();
+        gunreach_ = unreachable_;
     }
     check(cudaGraphLaunch(gexec_, st), "launch graph");
 }

@@ -92,6 +92,8 @@ struct uneven_launch
     void* out;
     void* scratch;
     int inverse;
+    unsigned wait_spins; // polls (256 ns sleeps) before a stage wait gives up (kDefaultWaitSpins, launch.hpp)
+    int stage_bias;      // added to every stage count waited for: 0, or 1 to make every such wait run out
 };
 
 cudaError_t launch_uneven_f32(const uneven_launch& a, int smem, int grid, cudaStream_t st);
@@ -109,6 +111,9 @@ public:
     void execute_per_signal(void* out, const void* in, bool inverse, cudaStream_t st);
     // raises if a tile gave up waiting for its dependencies (call after synchronising)
     void check_device_error() const;
+    // failure-detection test: every tile that depends on an earlier stage waits for one more tile than that
+    // stage has, so its wait runs out (after the wait limit) and the device error flag is set
+    void set_unreachable_stage(bool on) { unreachable_ = on; }
     long long total() const { return total_; }
     std::string describe() const;
 
@@ -133,6 +138,9 @@ private:
     const void* gin_ = nullptr;
     void* gout_      = nullptr;
     bool ginv_       = false;
+    bool unreachable_ = false;
+    unsigned gspins_  = 0; // wait settings the captured graph was built with
+    bool gunreach_    = false;
 
     int get_shape(long long m, int max_ts, const std::vector<int>* order = nullptr);
     void enqueue(void* out, const void* in, bool inverse, cudaStream_t st);

@@ -48,3 +48,24 @@ def uneven_lengths(count=8192, lo=64, hi=65536, prime_fraction=0.1, seed=2026120
         cands = [table[j] for j in (i - 1, i) if 0 <= j < len(table)]
         out.append(min(cands, key=lambda c: abs(math.log(c) - lg)))
     return out
+
+
+def precision_signals(n, batch, seed, device="cuda"):
+    """The precision workload: each signal a sum of 64 complex sinusoids of random frequency (uniform on
+    [0, n), not on the bin grid), amplitude (uniform on [0, 1)) and phase, plus 1e-3 N(0,1) complex noise.
+    Parameters come from a seeded numpy stream; the sum is evaluated in FP64 on `device` and rounded to c32
+    once.  Returns a numpy complex64 array (batch, n)."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    t = torch.arange(n, dtype=torch.float64, device=device) / n
+    out = np.empty((batch, n), np.complex64)
+    for b in range(batch):
+        f, a, ph = rng.uniform(0, n, 64), rng.uniform(0, 1, 64), rng.uniform(0, 2 * np.pi, 64)
+        x = torch.zeros(n, dtype=torch.complex128, device=device)
+        for i in range(64):
+            x += float(a[i]) * torch.exp(1j * (2 * math.pi * float(f[i]) * t + float(ph[i])))
+        noise = rng.standard_normal((2, n))
+        x += 1e-3 * torch.complex(torch.from_numpy(noise[0]), torch.from_numpy(noise[1])).to(device)
+        out[b] = x.to(torch.complex64).cpu().numpy()
+    return out

@@ -321,6 +321,17 @@ static void orc_parallel(orc_job_fn fn, void* ctx, size_t count, int threads)
     {                                                                                                    \
         ORC_CAT(filt_free, SFXT)((ORC_CAT(orc_filter, SFXT)*)f);                                         \
     }                                                                                                    \
+    /* fir_filter: direct-form streaming FIR (real samples) */                                          \
+    EXPORT void* ORC_CAT(orc_fir_create, SFXT)(const REALT* taps, size_t ntaps)                          \
+    {                                                                                                    \
+        return ORC_CAT(fir_create, SFXT)(taps, ntaps);                                                   \
+    }                                                                                                    \
+    EXPORT void ORC_CAT(orc_fir_process, SFXT)(void* f, REALT* out, const REALT* in, size_t n)           \
+    {                                                                                                    \
+        ORC_CAT(fir_process, SFXT)((ORC_CAT(orc_fir, SFXT)*)f, out, in, n);                              \
+    }                                                                                                    \
+    EXPORT void ORC_CAT(orc_fir_reset, SFXT)(void* f) { ORC_CAT(fir_reset, SFXT)((ORC_CAT(orc_fir, SFXT)*)f); } \
+    EXPORT void ORC_CAT(orc_fir_delete, SFXT)(void* f) { ORC_CAT(fir_free, SFXT)((ORC_CAT(orc_fir, SFXT)*)f); } \
     /* fft_multiply (acc NULL) / three-operand fft_multiply_accumulate over n complex values */          \
     EXPORT void ORC_CAT(orc_fft_multiply, SFXT)(REALT * dst, const REALT* acc, const REALT* a,           \
                                                 const REALT* b, size_t n, int perm)                      \

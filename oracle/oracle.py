@@ -230,6 +230,10 @@ class Oracle:
     def filter(self, taps, block=1024, precision="f64"):
         return _Filter(self, taps, block, precision)
 
+    def fir(self, taps, precision="f64"):
+        """Streaming direct-form FIR (fir_filter<T>): y[n] = sum_k taps[k] x[n - k], state across calls."""
+        return _Fir(self, taps, precision)
+
 
 class _Filter:
     """Streaming convolve_filter state (reset, process)."""
@@ -275,3 +279,36 @@ def c32_tolerance(n: int) -> float:
 def c64_tolerance(n: int) -> float:
     """Relative-RMS bound for double-precision complex results: 4 * log2(N) * 2^-53."""
     return 4.0 * max(np.log2(max(n, 2)), 1.0) * 2.0 ** -53
+
+
+class _Fir:
+    """Streaming fir_filter state (reset, process); real samples."""
+
+    def __init__(self, orc: Oracle, taps, precision):
+        self.orc = orc
+        self.rdt = Oracle._rdt(precision)
+        sfx = "_f64" if self.rdt == np.float64 else "_f32"
+        self.fns = {}
+        for name, res, args in (("create", _ptr, [_ptr, _c_size]), ("process", None, [_ptr, _ptr, _ptr, _c_size]),
+                                ("reset", None, [_ptr]), ("delete", None, [_ptr])):
+            f = getattr(orc.lib, orc.pre + "fir_" + name + sfx)
+            f.restype = res
+            f.argtypes = args
+            self.fns[name] = f
+        t = np.ascontiguousarray(taps, dtype=self.rdt)
+        self.h = self.fns["create"](_p(t), len(t))
+
+    def process(self, x):
+        x = np.ascontiguousarray(x, dtype=self.rdt)
+        out = np.empty_like(x)
+        self.fns["process"](self.h, _p(out), _p(x), len(x))
+        return out
+
+    def reset(self):
+        self.fns["reset"](self.h)
+
+    def __del__(self):
+        try:
+            self.fns["delete"](self.h)
+        except Exception:
+            pass

@@ -15,6 +15,7 @@
  *   - fft_multiply(_accumulate) .................. include/kfr/dft/fft.hpp:983-1020
  *   - convolve / correlate ....................... src/dft/convolution-impl.cpp:106-128
  *   - convolve_filter (streaming, partitioned) ... src/dft/convolution-impl.cpp:37-84, 134-228
+ *   - fir_filter (direct form, delay line) ....... include/kfr/dsp/fir.hpp:64-113, src/dsp/fir.cpp:54-57
  *
  * The stage structure is a self-sorting (Stockham) sweep over the factor list rather than KFR's in-place
  * stages plus digit-reverse permutation: the arithmetic of each radix-r butterfly and of each twiddle is
@@ -747,3 +748,52 @@ static void FN(filt_process)(FILT* f, CPX* output, const CPX* input, size_t size
 #undef CPX
 #undef PLAN
 #undef FILT
+
+/* fir_filter<T> (include/kfr/dsp/fir.hpp:64-113, src/dsp/fir.cpp:54-57): direct form
+ * y[n] = sum_k taps[k] x[n - k] with a delay line of the last ntaps inputs, zero after creation and after
+ * reset, kept across process calls. */
+typedef struct FN(orc_fir)
+{
+    size_t ntaps;
+    REAL* taps;
+    REAL* hist; /* the last ntaps inputs, oldest first */
+} FN(orc_fir);
+
+static FN(orc_fir) * FN(fir_create)(const REAL* taps, size_t ntaps)
+{
+    FN(orc_fir)* f = (FN(orc_fir)*)calloc(1, sizeof(FN(orc_fir)));
+    f->ntaps       = ntaps;
+    f->taps        = (REAL*)calloc(ntaps + 1, sizeof(REAL));
+    f->hist        = (REAL*)calloc(ntaps + 1, sizeof(REAL));
+    for (size_t i = 0; i < ntaps; i++)
+        f->taps[i] = taps[i];
+    return f;
+}
+
+static void FN(fir_reset)(FN(orc_fir) * f) { memset(f->hist, 0, sizeof(REAL) * (f->ntaps + 1)); }
+
+static void FN(fir_process)(FN(orc_fir) * f, REAL* out, const REAL* in, size_t n)
+{
+    const size_t m = f->ntaps;
+    for (size_t i = 0; i < n; i++)
+    {
+        if (m)
+        {
+            memmove(f->hist, f->hist + 1, sizeof(REAL) * (m - 1));
+            f->hist[m - 1] = in[i];
+        }
+        REAL acc = 0;
+        for (size_t k = 0; k < m; k++)
+            acc += f->taps[k] * f->hist[m - 1 - k];
+        out[i] = acc;
+    }
+}
+
+static void FN(fir_free)(FN(orc_fir) * f)
+{
+    if (!f)
+        return;
+    free(f->taps);
+    free(f->hist);
+    free(f);
+}

@@ -11,8 +11,11 @@
 //   dct_plan<T>::execute            include/kfr/dft/fft.hpp:932-970
 //   convolve / correlate            include/kfr/dft/convolution.hpp:53-67
 //   convolve_filter<T>              include/kfr/dft/convolution.hpp:98-148
+//   fir_filter<T> (the fir expression over a fir_state, as its process_buffer does)
+//                                   include/kfr/dsp/fir.hpp:64-113, src/dsp/fir.cpp:54-57
 #include <kfr/dft.hpp>
 #include <kfr/dft/convolution.hpp>
+#include <kfr/dsp/fir.hpp>
 
 #include <chrono>
 #include <cstring>
@@ -341,6 +344,43 @@ extern "C" __attribute__((visibility("default"))) void ref_fft_multiply_f64(doub
 {
     run_fft_multiply<double>(dst, acc, a, b, n, perm);
 }
+
+// fir_filter<T>::process_buffer is `dest = fir(src, std::ref(state))` (src/dsp/fir.cpp:54-57); the same
+// expression over the same state type is evaluated here, header-only.
+template <typename T>
+void* fir_create(const T* taps, size_t ntaps)
+{
+    return new fir_state<T, T>(make_univector(taps, ntaps));
+}
+template <typename T>
+void fir_process(void* f, T* out, const T* in, size_t n)
+{
+    make_univector(out, n) = fir(make_univector(in, n), std::ref(*static_cast<fir_state<T, T>*>(f)));
+}
+template <typename T>
+void fir_reset(void* f)
+{
+    auto* s             = static_cast<fir_state<T, T>*>(f);
+    s->delayline        = scalar(T(0));
+    s->delayline_cursor = 0;
+}
+#define REF_FIR(T, SFX)                                                                                          \
+    extern "C" __attribute__((visibility("default"))) void* ref_fir_create##SFX(const T* taps, size_t ntaps)     \
+    {                                                                                                            \
+        return fir_create<T>(taps, ntaps);                                                                       \
+    }                                                                                                            \
+    extern "C" __attribute__((visibility("default"))) void ref_fir_process##SFX(void* f, T* out, const T* in,    \
+                                                                              size_t n)                          \
+    {                                                                                                            \
+        fir_process<T>(f, out, in, n);                                                                           \
+    }                                                                                                            \
+    extern "C" __attribute__((visibility("default"))) void ref_fir_reset##SFX(void* f) { fir_reset<T>(f); }      \
+    extern "C" __attribute__((visibility("default"))) void ref_fir_delete##SFX(void* f)                          \
+    {                                                                                                            \
+        delete static_cast<fir_state<T, T>*>(f);                                                                 \
+    }
+REF_FIR(float, _f32)
+REF_FIR(double, _f64)
 
 extern "C" __attribute__((visibility("default"))) void ref_dft_dump_f32(size_t n)
 {

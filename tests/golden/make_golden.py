@@ -148,7 +148,34 @@ def main() -> None:
     fm["nr"] = np.array(len(md_real_shapes))
     np.savez_compressed(os.path.join(HERE, "dft_md.npz"), **fm)
     fft_multiply_fixture(ref)
+    fir_fixture(ref)
     print("golden fixtures written to", HERE)
+
+
+FIR_TAPS = [1, 5, 31, 256, 1023, 4097]
+
+
+def fir_fixture(ref) -> None:
+    """fir_filter<double> (include/kfr/dsp/fir.hpp, src/dsp/fir.cpp:54-57) streaming over uneven chunks,
+    then reset, from its own seeded stream."""
+    rng = np.random.default_rng(SEED + 6)
+    ff = {"ntaps": np.array(FIR_TAPS)}
+    chunks = [1, 700, 3001, 64, 5000]
+    for m in FIR_TAPS:
+        taps = rng.standard_normal(m) / np.sqrt(m)
+        xs = [rng.standard_normal(c) for c in chunks]
+        xr = rng.standard_normal(2000)
+        ff[f"taps_{m}"] = taps
+        for j, x in enumerate(xs):
+            ff[f"in_{m}_{j}"] = x
+        ff[f"in_{m}_reset"] = xr
+        f = ref.fir(taps)
+        for j, x in enumerate(xs):
+            ff[f"out_{m}_{j}"] = f.process(x)
+        f.reset()
+        ff[f"out_{m}_reset"] = f.process(xr)
+    ff["nchunks"] = np.array(len(chunks))
+    np.savez_compressed(os.path.join(HERE, "fir.npz"), **ff)
 
 
 def fft_multiply_fixture(ref) -> None:
@@ -171,5 +198,8 @@ if __name__ == "__main__":
     if sys.argv[1:] == ["fft_multiply"]:
         build(ref=True)
         fft_multiply_fixture(Oracle("ref"))
+    elif sys.argv[1:] == ["fir"]:
+        build(ref=True)
+        fir_fixture(Oracle("ref"))
     else:
         main()

@@ -121,7 +121,9 @@ def test_managed_allocation(L):
 
 
 def test_out_of_scope_filters_report_errors(L):
-    assert not L.kfr_filter_create_fir_plan_f32(None, 0)
+    assert not L.kfr_filter_create_iir_plan_f32(None, 0)
+    assert b"not part of the GPU DFT path" in L.kfr_last_error()
+    assert not L.kfr_filter_create_iir_plan_f64(None, 0)
     assert b"not part of the GPU DFT path" in L.kfr_last_error()
 
 

@@ -29,7 +29,8 @@ def test_known_answers():
 def test_reference_fixtures(prec):
     g = load_golden("convolution.npz")
     rdt, cdt = (np.float32, np.complex64) if prec == "f32" else (np.float64, np.complex128)
-    tol = (lambda n: 8 * c32_tolerance(n)) if prec == "f32" else (lambda n: 64 * c64_tolerance(n))
+    # the per-transform tolerance at n = len(a) + len(b) (measured: at most 0.52 of it in f32, 0.42 in f64)
+    tol = c32_tolerance if prec == "f32" else c64_tolerance
     for i in range(int(g["npairs"])):
         a, b = g[f"a_{i}"].astype(rdt), g[f"b_{i}"].astype(rdt)
         n = len(a) + len(b)
@@ -51,7 +52,7 @@ def test_long_signal_device_and_autocorrelate():
     ad, bd = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
     got = k.convolve(ad, bd)
     assert got.is_cuda
-    assert rel_rms(got.cpu().numpy(), want) <= 8 * c32_tolerance(len(want))
+    assert rel_rms(got.cpu().numpy(), want) <= c32_tolerance(len(want))  # measured 0.21 of it
     x = rng.standard_normal(5000)
     full = np.correlate(x, x, mode="full")
     assert rel_rms(k.autocorrelate(x), full[len(x) - 1:]) <= 1e-12

@@ -368,9 +368,9 @@ def test_dct_reference_fixtures(sfx):
         x = g[f"x_{n}"].astype(rdt)
         y = np.zeros_like(x)
         plan.execute_batch(y, x, x.shape[0])
-        assert rel_rms(y, g[f"fwd_{n}"]) <= 2 * tol(max(n, 2), sfx), n
+        assert rel_rms(y, g[f"fwd_{n}"]) <= tol(max(n, 2), sfx), n  # measured at most 0.37 of it
         plan.execute_batch(y, x, x.shape[0], inverse=True)
-        assert rel_rms(y, g[f"inv_{n}"]) <= 2 * tol(max(n, 2), sfx), n
+        assert rel_rms(y, g[f"inv_{n}"]) <= tol(max(n, 2), sfx), n
 
 
 def test_dct_known_answer_16():
@@ -400,9 +400,9 @@ def test_dct_batched_documented_formula(n, batch):
         o = Oracle("orc")
         r2, r3 = o.dct(x64), o.dct(x64, inverse=True)
     plan.execute_batch(yd, xd, batch)
-    assert rel_rms(yd.cpu().numpy(), r2) <= 2 * c32_tolerance(max(n, 2)), n
+    assert rel_rms(yd.cpu().numpy(), r2) <= c32_tolerance(max(n, 2)), n
     plan.execute_batch(yd, xd, batch, inverse=True)
-    assert rel_rms(yd.cpu().numpy(), r3) <= 2 * c32_tolerance(max(n, 2)), n
+    assert rel_rms(yd.cpu().numpy(), r3) <= c32_tolerance(max(n, 2)), n
 
 
 # ------------------------------------------------------------------------------------------------------
@@ -430,12 +430,12 @@ def test_convolve_filter_streaming_fixtures(sfx):
             x = g[f"fin_real_{i}_{j}"].astype(rdt)
             y = np.zeros_like(x)
             f.apply(y, x)
-            assert rel_rms(y, g[f"fout_real_{i}_{j}"]) <= 8 * tol(len(taps) + len(x), sfx), (i, j)
+            assert rel_rms(y, g[f"fout_real_{i}_{j}"]) <= tol(len(taps) + len(x), sfx), (i, j)
         f.reset()
         x = g[f"fin_real_{i}_reset"].astype(rdt)
         y = np.zeros_like(x)
         f.apply(y, x)
-        assert rel_rms(y, g[f"fout_real_{i}_reset"]) <= 8 * tol(len(taps) + len(x), sfx), i
+        assert rel_rms(y, g[f"fout_real_{i}_reset"]) <= tol(len(taps) + len(x), sfx), i
 
 
 def test_convolve_filter_channels_match_single_channel(orc):
@@ -455,7 +455,7 @@ def test_convolve_filter_channels_match_single_channel(orc):
     got = np.concatenate(outs, axis=1)
     for c in range(chans):
         ref = orc.filter(taps.astype(np.float64), 512).process(x[c].astype(np.float64))
-        assert rel_rms(got[c], ref) <= 8 * c32_tolerance(2 * n), c
+        assert rel_rms(got[c], ref) <= c32_tolerance(2 * n), c
     multi.reset()
     xd = dev(np.ascontiguousarray(x[:, :n]))
     yd = torch.empty_like(xd)
@@ -483,12 +483,12 @@ def test_convolve_filter_taps_longer_than_one_fft(orc, sfx, ntaps):
     tol_f = c32_tolerance if sfx == "f32" else c64_tolerance
     for c in range(chans):
         ref = orc.filter(taps.astype(np.float64), 1024).process(x[c].astype(np.float64))
-        assert rel_rms(got[c], ref) <= 8 * tol_f(2 * n + ntaps), c
+        assert rel_rms(got[c], ref) <= tol_f(2 * n + ntaps), c
     f.reset()
     xd = dev(np.ascontiguousarray(x[:, :n]))
     yd = torch.empty_like(xd)
     f.apply(yd, xd)
-    assert rel_rms(yd.cpu().numpy(), outs[0]) <= 8 * tol_f(n + ntaps)
+    assert rel_rms(yd.cpu().numpy(), outs[0]) <= tol_f(n + ntaps)
 
 
 def test_convolve_filter_long_signal_device(orc):
@@ -501,9 +501,9 @@ def test_convolve_filter_long_signal_device(orc):
     xd = dev(x)
     yd = torch.empty_like(xd)
     f.apply(yd, xd)
-    assert rel_rms(yd.cpu().numpy(), ref) <= 8 * c32_tolerance(1 << 18)
+    assert rel_rms(yd.cpu().numpy(), ref) <= c32_tolerance(1 << 18)  # measured 0.09 of it
     # in place on the device
     f.reset()
     zd = xd.clone()
     f.apply(zd, zd)
-    assert rel_rms(zd.cpu().numpy(), ref) <= 8 * c32_tolerance(1 << 18)
+    assert rel_rms(zd.cpu().numpy(), ref) <= c32_tolerance(1 << 18)

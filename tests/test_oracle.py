@@ -189,3 +189,15 @@ def test_fft_multiply_matches_reference_fixtures(orc):
             if perm:
                 want0 = a[:, 0].real * b[:, 0].real + 1j * a[:, 0].imag * b[:, 0].imag
                 assert np.allclose(f[f"mul_{fmt}_{prec}"][:, 0], want0, rtol=4 * eps)
+
+
+def test_fir_matches_reference_fixtures(orc):
+    """The direct-form FIR restatement against KFR's own fir_filter<double> (src/dsp/fir.cpp:54-57):
+    streaming over uneven chunks with the delay line kept across calls, then reset."""
+    g = load_golden("fir.npz")
+    for m in g["ntaps"]:
+        f = orc.fir(g[f"taps_{m}"])
+        for j in range(int(g["nchunks"])):
+            assert rel_rms(f.process(g[f"in_{m}_{j}"]), g[f"out_{m}_{j}"]) <= TIGHT, (m, j)
+        f.reset()
+        assert rel_rms(f.process(g[f"in_{m}_reset"]), g[f"out_{m}_reset"]) <= TIGHT, m
