@@ -297,6 +297,24 @@ KFR_API_SPEC void kfr_fft_multiply_accumulate_f64(kfr_c64* dest, const kfr_c64* 
                                                   const kfr_c64* src2, size_t size, size_t batch,
                                                   kfr_bool src2_shared, KFR_DFT_PACK_FORMAT fmt, void* stream);
 
+/* Progressive execution (dft_plan<T>::progressive_*, include/kfr/dft/fft.hpp:393-439): the reference runs
+ * one stage per step; here one step is one kernel launch of the plan, run to completion.
+ *   total_steps: the steps of one execution with device buffers aligned as cudaMalloc aligns them;
+ *   start:       records the plan's launches for these buffers (nothing runs yet; host buffers are staged:
+ *                the input is copied now, the result after the last step) and returns the number of steps
+ *                of this execution (it can differ from total_steps for misaligned device pointers);
+ *   step:        runs step `step` (0, 1, ... in order) and waits for it; returns nonzero while steps remain.
+ *                `out` holds the result after the last step.
+ * One progressive execution per plan at a time. */
+KFR_API_SPEC size_t kfr_dft_progressive_total_steps_f32(KFR_DFT_PLAN_F32* plan);
+KFR_API_SPEC size_t kfr_dft_progressive_total_steps_f64(KFR_DFT_PLAN_F64* plan);
+KFR_API_SPEC size_t kfr_dft_progressive_start_f32(KFR_DFT_PLAN_F32* plan, kfr_c32* out, const kfr_c32* in,
+                                                  uint8_t* temp, kfr_bool inverse);
+KFR_API_SPEC size_t kfr_dft_progressive_start_f64(KFR_DFT_PLAN_F64* plan, kfr_c64* out, const kfr_c64* in,
+                                                  uint8_t* temp, kfr_bool inverse);
+KFR_API_SPEC kfr_bool kfr_dft_progressive_step_f32(KFR_DFT_PLAN_F32* plan, size_t step);
+KFR_API_SPEC kfr_bool kfr_dft_progressive_step_f64(KFR_DFT_PLAN_F64* plan, size_t step);
+
 /* Number of kernel launches one batched execute of this plan issues (forward direction). */
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f32(KFR_DFT_PLAN_F32* plan, size_t batch);
 KFR_API_SPEC size_t kfr_dft_get_launch_count_f64(KFR_DFT_PLAN_F64* plan, size_t batch);

@@ -75,6 +75,12 @@ struct api<float>
                                   nullptr);
     }
     static void dump(plan_t* p) { kfr_dft_dump_f32(p); }
+    static size_t prog_total(plan_t* p) { return kfr_dft_progressive_total_steps_f32(p); }
+    static size_t prog_start(plan_t* p, complex<float>* o, const complex<float>* i, u8* t, bool inv)
+    {
+        return kfr_dft_progressive_start_f32(p, reinterpret_cast<kfr_c32*>(o), reinterpret_cast<const kfr_c32*>(i), t, inv);
+    }
+    static void prog_step(plan_t* p, size_t step) { kfr_dft_progressive_step_f32(p, step); }
     static rplan_t* rcreate(size_t n, dft_pack_format f)
     {
         return kfr_dft_real_create_plan_f32(n, static_cast<KFR_DFT_PACK_FORMAT>(f));
@@ -134,6 +140,12 @@ struct api<double>
                                   nullptr);
     }
     static void dump(plan_t* p) { kfr_dft_dump_f64(p); }
+    static size_t prog_total(plan_t* p) { return kfr_dft_progressive_total_steps_f64(p); }
+    static size_t prog_start(plan_t* p, complex<double>* o, const complex<double>* i, u8* t, bool inv)
+    {
+        return kfr_dft_progressive_start_f64(p, reinterpret_cast<kfr_c64*>(o), reinterpret_cast<const kfr_c64*>(i), t, inv);
+    }
+    static void prog_step(plan_t* p, size_t step) { kfr_dft_progressive_step_f64(p, step); }
     static rplan_t* rcreate(size_t n, dft_pack_format f)
     {
         return kfr_dft_real_create_plan_f64(n, static_cast<KFR_DFT_PACK_FORMAT>(f));
@@ -231,28 +243,38 @@ struct dft_plan
         gpu_detail::check();
     }
 
-    /// Progressive execution (include/kfr/dft/fft.hpp:393-439): the GPU runs the whole transform as one
-    /// stream-ordered step, so there is a single step; `out` holds the result after it.
+    /// Progressive execution (include/kfr/dft/fft.hpp:393-439): one step is one kernel launch of the plan
+    /// (the reference runs one stage per step); `out` holds the result after the last step.  One
+    /// progressive execution per plan at a time.
     struct progressive
     {
         bool inverse;
         complex<T>* out;
         const complex<T>* in;
         u8* temp;
-        size_t step = 0;
+        size_t step  = 0;
+        size_t total = 0; // steps of this execution
     };
-    size_t progressive_total_steps() const { return 1; }
+    size_t progressive_total_steps() const
+    {
+        const size_t n = gpu_detail::api<T>::prog_total(h_.get());
+        gpu_detail::check();
+        return n;
+    }
     progressive progressive_start(bool inverse, complex<T>* out, const complex<T>* in, u8* temp) const
     {
         if (!is_initialized())
             throw logic_error("dft_plan is not initialized");
-        return progressive{ inverse, out, in, temp, 0 };
+        progressive p{ inverse, out, in, temp, 0, 0 };
+        p.total = gpu_detail::api<T>::prog_start(h_.get(), out, in, temp, inverse);
+        gpu_detail::check();
+        return p;
     }
     bool progressive_step(progressive& p) const
     {
-        if (p.step == 0)
-            execute(p.out, p.in, p.temp, p.inverse);
-        return ++p.step < progressive_total_steps();
+        gpu_detail::api<T>::prog_step(h_.get(), p.step);
+        gpu_detail::check();
+        return ++p.step < p.total;
     }
 
 protected:

@@ -112,6 +112,12 @@ _SIGS.update({
     "kfr_allocated_size": (_S, [_P]),
     "kfr_dft_describe_f64": (_S, [_P, ctypes.c_char_p, _S]),
     "kfr_set_wait_limit": (ctypes.c_uint32, [ctypes.c_uint32]),
+    "kfr_dft_progressive_total_steps_f32": (_S, [_P]),
+    "kfr_dft_progressive_total_steps_f64": (_S, [_P]),
+    "kfr_dft_progressive_start_f32": (_S, [_P, _P, _P, _P, _B]),
+    "kfr_dft_progressive_start_f64": (_S, [_P, _P, _P, _P, _B]),
+    "kfr_dft_progressive_step_f32": (_B, [_P, _S]),
+    "kfr_dft_progressive_step_f64": (_B, [_P, _S]),
     "kfr_dft_uneven_set_unreachable_stage_f32": (None, [_P, _B]),
     "kfr_fft_multiply_f32": (None, [_P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
     "kfr_fft_multiply_f64": (None, [_P, _P, _P, _S, _S, _B, ctypes.c_int, _P]),
@@ -271,6 +277,19 @@ class dft_plan(_plan):
         buf = ctypes.create_string_buffer(512)
         _call("kfr_dft_describe_f32", self.handle, buf, 512)
         return buf.value.decode()
+
+    def progressive_total_steps(self) -> int:
+        """Steps of a progressive execution: one kernel launch each (include/kfr/dft/fft.hpp:403-405)."""
+        return _call(self._fn("progressive_total_steps"), self.handle)
+
+    def progressive_start(self, out, inp, temp=None, inverse=False) -> int:
+        """Records one execution for these buffers; returns its number of steps."""
+        self._prog = (out, inp, temp)  # keep the buffers alive until the last step
+        return _call(self._fn("progressive_start"), self.handle, _addr(out), _addr(inp), _addr(temp), inverse)
+
+    def progressive_step(self, step: int) -> bool:
+        """Runs one step; True while steps remain."""
+        return bool(_call(self._fn("progressive_step"), self.handle, step))
 
     def launch_count(self, batch=1):
         return _call("kfr_dft_get_launch_count_f32", self.handle, batch) if self.sfx == "f32" else None

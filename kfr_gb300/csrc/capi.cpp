@@ -134,6 +134,148 @@ struct tags<double>
     static constexpr uint32_t dft = TAG_DFT_F64, real = TAG_REAL_F64, dct = TAG_DCT_F64, flt = TAG_FLT_F64;
 };
 
+// Progressive execution (include/kfr/dft/fft.hpp:393-439; src/dft/fft-impl.hpp:2025-2064): the reference
+// runs one stage per step; here a step is one kernel launch of the plan.  progressive_start records one
+// execution with the given buffers by stream capture (nothing runs) and orders the recorded nodes; step i
+// replays the i-th kernel launch (and any copy or memset recorded before it) and waits for it.
+struct recorded_launches
+{
+    cudaGraph_t graph = nullptr;
+    std::vector<std::vector<cudaGraphNode_t>> steps; // per step: the nodes before a kernel, then the kernel
+
+    recorded_launches() = default;
+    recorded_launches(const recorded_launches&) = delete;
+    recorded_launches& operator=(const recorded_launches&) = delete;
+    ~recorded_launches()
+    {
+        if (graph)
+            cudaGraphDestroy(graph);
+    }
+
+    // Records fn(stream) by capture on `st` and splits the nodes (a chain) into steps.
+    template <typename Fn>
+    void record(cudaStream_t st, Fn&& fn)
+    {
+        check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+        try
+        {
+            fn(st);
+        }
+        catch (...)
+        {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(st, &g);
+            if (g)
+                cudaGraphDestroy(g);
+            throw;
+        }
+        check(cudaStreamEndCapture(st, &graph), "end capture");
+        size_t count = 0;
+        check(cudaGraphGetNodes(graph, nullptr, &count), "graph nodes");
+        std::vector<cudaGraphNode_t> nodes(count);
+        if (count)
+            check(cudaGraphGetNodes(graph, nodes.data(), &count), "graph nodes");
+        // topological order of the recorded chain
+        std::vector<cudaGraphNode_t> order;
+        std::vector<char> done(count, 0);
+        while (order.size() < count)
+        {
+            bool progress = false;
+            for (size_t i = 0; i < count; i++)
+            {
+                if (done[i])
+                    continue;
+                size_t nd = 0;
+                check(cudaGraphNodeGetDependencies(nodes[i], nullptr, nullptr, &nd), "graph dependencies");
+                std::vector<cudaGraphNode_t> deps(nd);
+                if (nd)
+                    check(cudaGraphNodeGetDependencies(nodes[i], deps.data(), nullptr, &nd), "graph dependencies");
+                bool ready = true;
+                for (auto d : deps)
+                    ready = ready && std::find(order.begin(), order.end(), d) != order.end();
+                if (ready)
+                {
+                    order.push_back(nodes[i]);
+                    done[i]  = 1;
+                    progress = true;
+                }
+            }
+            if (!progress)
+                throw std::logic_error("progressive execution: recorded launches are not ordered");
+        }
+        std::vector<cudaGraphNode_t> cur;
+        for (auto nd : order)
+        {
+            cur.push_back(nd);
+            cudaGraphNodeType t;
+            check(cudaGraphNodeGetType(nd, &t), "graph node type");
+            if (t == cudaGraphNodeTypeKernel)
+            {
+                steps.push_back(cur);
+                cur.clear();
+            }
+        }
+        if (!cur.empty())
+        {
+            if (steps.empty())
+                steps.push_back(cur);
+            else
+                steps.back().insert(steps.back().end(), cur.begin(), cur.end());
+        }
+        if (steps.empty())
+            steps.emplace_back();
+    }
+
+    // Runs step i's nodes on st.
+    void replay(size_t i, cudaStream_t st) const
+    {
+        for (auto nd : steps.at(i))
+        {
+            cudaGraphNodeType t;
+            check(cudaGraphNodeGetType(nd, &t), "graph node type");
+            if (t == cudaGraphNodeTypeKernel)
+            {
+                cudaKernelNodeParams p{};
+                check(cudaGraphKernelNodeGetParams(nd, &p), "kernel node");
+                check(cudaLaunchKernel(p.func, p.gridDim, p.blockDim, p.kernelParams, p.sharedMemBytes, st),
+                      "progressive step launch");
+            }
+            else if (t == cudaGraphNodeTypeMemcpy)
+            {
+                cudaMemcpy3DParms p{};
+                check(cudaGraphMemcpyNodeGetParams(nd, &p), "copy node");
+                check(cudaMemcpy3DAsync(&p, st), "progressive step copy");
+            }
+            else if (t == cudaGraphNodeTypeMemset)
+            {
+                cudaMemsetParams p{};
+                check(cudaGraphMemsetNodeGetParams(nd, &p), "memset node");
+                if (p.elementSize != 1 && p.value != 0)
+                    throw std::logic_error("progressive execution: unsupported memset");
+                check(cudaMemset2DAsync(p.dst, p.pitch, int(p.value), p.width * p.elementSize, p.height, st),
+                      "progressive step memset");
+            }
+            else if (t != cudaGraphNodeTypeEmpty)
+                throw std::logic_error("progressive execution: unsupported recorded operation");
+        }
+    }
+};
+
+struct progressive_run
+{
+    cudaStream_t st = nullptr;
+    recorded_launches rec;
+    void* host_out = nullptr; // where the last step copies the result (host output), else null
+    const void* dev_out = nullptr;
+    size_t out_bytes = 0;
+    progressive_run() { check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "create stream"); }
+    ~progressive_run()
+    {
+        if (st)
+            cudaStreamDestroy(st);
+    }
+};
+
 // A complex plan is one-dimensional (complex_engine) or multi-dimensional (md_engine), like the reference's
 // var_dft_plan over dft_plan / dft_plan_md (src/capi/capi.cpp:93-156).
 template <typename T>
@@ -142,6 +284,8 @@ struct dft_obj : plan_base
     size_t n; // total number of complex values
     std::unique_ptr<complex_engine<T>> eng1;
     std::unique_ptr<md_engine<T>> md;
+    std::unique_ptr<progressive_run> prog; // the progressive execution in progress, if any
+    size_t prog_steps = 0;                 // steps of a progressive execution (0: not counted yet)
     explicit dft_obj(size_t n_) : plan_base(tags<T>::dft), n(n_), eng1(new complex_engine<T>((long long)n_)) {}
     dft_obj(size_t n_, int tensor_mode)
         : plan_base(tags<T>::dft), n(n_), eng1(new complex_engine<T>((long long)n_, tensor_mode))
@@ -783,6 +927,103 @@ size_t autocorrelate_any(T* out, const T* a, size_t n)
 
 namespace
 {
+// A device address that is never dereferenced: progressive_total_steps records one execution with it to
+// count the launches (recording runs nothing).  Aligned like a cudaMalloc allocation.
+void* unused_device_address(int i) { return reinterpret_cast<void*>((uintptr_t(0x7f00) + uintptr_t(i)) << 32); }
+
+template <typename T>
+size_t progressive_total(void* plan)
+{
+    auto* p = as<dft_obj<T>>(plan, tags<T>::dft);
+    std::unique_lock<std::mutex> lock(p->mu);
+    if (!p->prog_steps)
+    {
+        cudaStream_t st = nullptr;
+        check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "create stream");
+        try
+        {
+            recorded_launches rec;
+            void* scr = p->scratch_elems(1) ? unused_device_address(2) : nullptr;
+            rec.record(st, [&](cudaStream_t s)
+                       { p->execute(unused_device_address(0), unused_device_address(1), 1, false, scr, s); });
+            p->prog_steps = rec.steps.size();
+        }
+        catch (...)
+        {
+            cudaStreamDestroy(st);
+            throw;
+        }
+        cudaStreamDestroy(st);
+    }
+    return p->prog_steps;
+}
+
+template <typename T>
+size_t progressive_start(void* plan, void* out, const void* in, uint8_t* temp, bool inverse)
+{
+    auto* p = as<dft_obj<T>>(plan, tags<T>::dft);
+    if (!out || !in)
+        throw std::invalid_argument("NULL data pointer");
+    const size_t bytes = p->n * 2 * sizeof(T);
+    std::unique_lock<std::mutex> lock(p->mu);
+    p->prog.reset(new progressive_run);
+    progressive_run& r = *p->prog;
+    const void* din    = in;
+    void* dout         = out;
+    if (!is_device_ptr(in))
+    {
+        p->stage_in.ensure(bytes);
+        check(cudaMemcpy(p->stage_in.get(), in, bytes, cudaMemcpyHostToDevice), "copy input to device");
+        din = p->stage_in.get();
+    }
+    if (!is_device_ptr(out))
+    {
+        p->stage_out.ensure(bytes);
+        dout        = p->stage_out.get();
+        r.host_out  = out;
+        r.dev_out   = dout;
+        r.out_bytes = bytes;
+    }
+    void* scr = nullptr;
+    if (const size_t sb = size_t(p->scratch_elems(1)) * 2 * sizeof(T))
+    {
+        if (temp && is_device_ptr(temp))
+            scr = temp;
+        else
+        {
+            p->scratch.ensure(sb);
+            scr = p->scratch.get();
+        }
+    }
+    r.rec.record(r.st, [&](cudaStream_t st) { p->execute(dout, din, 1, inverse, scr, st); });
+    return r.rec.steps.size();
+}
+
+template <typename T>
+bool progressive_step(void* plan, size_t step)
+{
+    auto* p = as<dft_obj<T>>(plan, tags<T>::dft);
+    std::unique_lock<std::mutex> lock(p->mu);
+    if (!p->prog)
+        throw std::logic_error("progressive_step before progressive_start");
+    progressive_run& r = *p->prog;
+    if (step >= r.rec.steps.size())
+        throw std::invalid_argument("progressive step " + std::to_string(step) + " of " +
+                                    std::to_string(r.rec.steps.size()));
+    r.rec.replay(step, r.st);
+    check(cudaStreamSynchronize(r.st), "progressive step");
+    const bool more = step + 1 < r.rec.steps.size();
+    if (!more)
+    {
+        if (r.host_out)
+            check(cudaMemcpy(r.host_out, r.dev_out, r.out_bytes, cudaMemcpyDeviceToHost), "copy result to host");
+        p->prog.reset();
+        lock.unlock();
+        p->check_device_error();
+    }
+    return more;
+}
+
 template <typename T>
 void fft_multiply_dev(void* dest, const void* acc, const void* src1, const void* src2, size_t size, size_t batch,
                       bool shared, bool perm, void* stream)
@@ -1042,6 +1283,32 @@ KFR_API_SPEC void kfr_fft_multiply_accumulate_f64(kfr_c64* dest, const kfr_c64* 
                 throw std::invalid_argument("fft_multiply_accumulate: NULL accumulator");
             fft_multiply_dev<double>(dest, acc, src1, src2, size, batch, src2_shared, fmt == Perm, stream);
         });
+}
+KFR_API_SPEC size_t kfr_dft_progressive_total_steps_f32(KFR_DFT_PLAN_F32* plan)
+{
+    return try_fn([&] { return progressive_total<float>(plan); }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_progressive_total_steps_f64(KFR_DFT_PLAN_F64* plan)
+{
+    return try_fn([&] { return progressive_total<double>(plan); }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_progressive_start_f32(KFR_DFT_PLAN_F32* plan, kfr_c32* out, const kfr_c32* in,
+                                                  uint8_t* temp, kfr_bool inverse)
+{
+    return try_fn([&] { return progressive_start<float>(plan, out, in, temp, inverse != 0); }, size_t(0));
+}
+KFR_API_SPEC size_t kfr_dft_progressive_start_f64(KFR_DFT_PLAN_F64* plan, kfr_c64* out, const kfr_c64* in,
+                                                  uint8_t* temp, kfr_bool inverse)
+{
+    return try_fn([&] { return progressive_start<double>(plan, out, in, temp, inverse != 0); }, size_t(0));
+}
+KFR_API_SPEC kfr_bool kfr_dft_progressive_step_f32(KFR_DFT_PLAN_F32* plan, size_t step)
+{
+    return try_fn([&] { return kfr_bool(progressive_step<float>(plan, step)); }, kfr_bool(0));
+}
+KFR_API_SPEC kfr_bool kfr_dft_progressive_step_f64(KFR_DFT_PLAN_F64* plan, size_t step)
+{
+    return try_fn([&] { return kfr_bool(progressive_step<double>(plan, step)); }, kfr_bool(0));
 }
 KFR_API_SPEC size_t kfr_dft_describe_f32(KFR_DFT_PLAN_F32* plan, char* buf, size_t size)
 {

@@ -961,7 +961,11 @@ int complex_engine<T>::launches(long long batch) const
     switch (k_)
     {
     case kind::trivial: return 1;
-    case kind::smem: return (pipe_spc_ && batch % pipe_spc_) ? 2 : 1;
+    case kind::smem:
+        // the pipelined kernel takes the whole tiles (if any), the per-tile kernel the rest
+        if (pipe_spc_)
+            return (batch / pipe_spc_ > 0 ? 1 : 0) + (batch % pipe_spc_ ? 1 : 0);
+        return 1;
     case kind::bluestein_smem: return 1;
     case kind::fourstep: return 2 * int((batch + 65534) / 65535);
     case kind::bluestein_multi: return 3 + 2 * inner_->launches(batch);
