@@ -1,4 +1,6 @@
 // Elementwise kernels of the multi-kernel paths (see launch.hpp: ew_op).
+#include <algorithm>
+
 #include "fft_device.cuh"
 #include "launch.hpp"
 
@@ -177,6 +179,58 @@ template cudaError_t launch_fft_multiply<float>(void*, const void*, const void*,
                                                 long long, bool, cudaStream_t);
 template cudaError_t launch_fft_multiply<double>(void*, const void*, const void*, const void*, long long,
                                                  long long, long long, bool, cudaStream_t);
+
+// Batched complex transpose through a 32 x 32 shared-memory tile (one padding column, so the column reads
+// of the tile fall into distinct banks); each thread moves 4 elements per direction.  blockIdx.y walks the
+// batch (more than 65535 matrices take several launches).
+template <typename T>
+__global__ void __launch_bounds__(256) k_transpose(cpx<T>* out, const cpx<T>* in, const long long rows,
+                                                   const long long cols, const long long b0)
+{
+    __shared__ cpx<T> tile[32][33];
+    const long long b  = b0 + blockIdx.y;
+    const long long gx = (cols + 31) / 32; // tiles along a row; blockIdx.x = row tile * gx + column tile
+    const long long c0 = ((long long)blockIdx.x % gx) * 32, r0 = ((long long)blockIdx.x / gx) * 32;
+    const cpx<T>* src  = in + b * rows * cols;
+    cpx<T>* dst        = out + b * rows * cols;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 32; i += 8)
+    {
+        const long long r = r0 + ty + i, c = c0 + tx;
+        if (r < rows && c < cols)
+            tile[ty + i][tx] = src[r * cols + c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 32; i += 8)
+    {
+        const long long c = c0 + ty + i, r = r0 + tx;
+        if (r < rows && c < cols)
+            dst[c * rows + r] = tile[tx][ty + i];
+    }
+}
+
+template <typename T>
+cudaError_t launch_transpose(void* out, const void* in, long long batch, long long rows, long long cols,
+                             cudaStream_t st)
+{
+    if (batch <= 0 || rows <= 0 || cols <= 0)
+        return cudaSuccess;
+    const long long tiles = ((cols + 31) / 32) * ((rows + 31) / 32);
+    if (tiles > 2147483647LL)
+        return cudaErrorInvalidValue;
+    for (long long b0 = 0; b0 < batch; b0 += 65535)
+    {
+        const unsigned gb = unsigned(std::min<long long>(65535, batch - b0));
+        k_transpose<T><<<dim3(unsigned(tiles), gb), 256, 0, st>>>(static_cast<cpx<T>*>(out),
+                                                                   static_cast<const cpx<T>*>(in), rows, cols, b0);
+    }
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_transpose<float>(void*, const void*, long long, long long, long long, cudaStream_t);
+template cudaError_t launch_transpose<double>(void*, const void*, long long, long long, long long, cudaStream_t);
 
 template cudaError_t launch_elementwise<float>(int, const ew_args&, cudaStream_t);
 template cudaError_t launch_elementwise<double>(int, const ew_args&, cudaStream_t);

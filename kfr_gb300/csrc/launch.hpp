@@ -191,6 +191,11 @@ enum ew_op
 template <typename T>
 cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st);
 
+// Batched transpose of complex matrices: out[b][c][r] = in[b][r][c] (b < batch, r < rows, c < cols).
+template <typename T>
+cudaError_t launch_transpose(void* out, const void* in, long long batch, long long rows, long long cols,
+                             cudaStream_t st);
+
 // fft_multiply / fft_multiply_accumulate over `batch` spectra of `size` elements stored back to back:
 // dest = (acc ? acc : 0) + src1 * src2, with the Perm format's element 0 formed from the real and the
 // imaginary parts separately.  src2_stride: 0 (one spectrum shared by every signal) or size.  acc may alias

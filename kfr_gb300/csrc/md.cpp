@@ -19,35 +19,68 @@ template <typename T>
 md_axes<T>::md_axes(const std::vector<long long>& cshape)
 {
     const size_t d = cshape.size();
+    total_         = product(cshape, 0, d);
     for (size_t i = 0; i + 1 < d; i++)
     {
         const long long n = cshape[i];
         if (n <= 1)
             continue;
-        if (!block_program<T>::feasible(n))
-            throw std::invalid_argument("multi-dimensional DFT: axis length " + std::to_string(n) +
-                                        " of a non-last axis is not supported by this build");
         axis a;
         a.n     = n;
         a.inner = product(cshape, i + 1, d);
         a.outer = product(cshape, 0, i);
-        a.prog.reset(new block_program<T>());
-        a.prog->build(int(n), CT_FOURSTEP);
-        int t = tile_for(*a.prog);
-        if (t == 0)
-            throw std::invalid_argument("multi-dimensional DFT: axis too long for one CTA");
-        while (t > 1 && t / 2 >= a.inner)
-            t /= 2;
-        a.tile = t;
+        a.tile  = 0;
+        if (block_program<T>::feasible(n))
+        {
+            a.prog.reset(new block_program<T>());
+            a.prog->build(int(n), CT_FOURSTEP);
+            int t = tile_for(*a.prog);
+            while (t > 1 && t / 2 >= a.inner)
+                t /= 2;
+            a.tile = t;
+            if (t == 0)
+                a.prog.reset();
+        }
+        if (!a.prog) // longer than one CTA: transposed 1-D pass
+            a.eng.reset(new complex_engine<T>(n));
         axes_.push_back(std::move(a));
     }
 }
 
 template <typename T>
-void md_axes<T>::run(void* data, long long batch, bool inverse, cudaStream_t st) const
+long long md_axes<T>::scratch_elems(long long batch) const
+{
+    long long need = 0;
+    for (const axis& a : axes_)
+        if (a.eng)
+            need = std::max(need, batch * total_ + a.eng->scratch_elems(batch * a.outer * a.inner));
+    return need;
+}
+
+template <typename T>
+int md_axes<T>::launches(long long batch) const
+{
+    int n = 0;
+    for (const axis& a : axes_)
+        n += a.eng ? 2 + a.eng->launches(batch * a.outer * a.inner) : int((batch * a.outer + 65534) / 65535);
+    return n;
+}
+
+template <typename T>
+void md_axes<T>::run(void* data, long long batch, bool inverse, void* scratch, cudaStream_t st) const
 {
     for (const axis& ax : axes_)
     {
+        if (ax.eng)
+        {
+            // [batch outer][n][inner] -> [batch outer][inner][n], n-point DFTs of the rows, and back
+            char* tr  = static_cast<char*>(scratch);
+            char* scr = tr + batch * total_ * 2 * sizeof(T);
+            check(launch_transpose<T>(tr, data, batch * ax.outer, ax.n, ax.inner, st), "transpose axis");
+            ax.eng->execute(tr, tr, batch * ax.outer * ax.inner, ax.n, ax.n, inverse, scr, st);
+            check(launch_transpose<T>(data, tr, batch * ax.outer, ax.inner, ax.n, st), "transpose axis back");
+            continue;
+        }
         const long long sigs = batch * ax.outer;
         for (long long b0 = 0; b0 < sigs; b0 += 65535)
         {
@@ -88,7 +121,12 @@ std::string md_axes<T>::describe() const
 {
     std::ostringstream s;
     for (const axis& a : axes_)
-        s << " axis{n=" << a.n << " inner=" << a.inner << " tile=" << a.tile << " " << a.prog->describe() << "}";
+    {
+        if (a.eng)
+            s << " axis{n=" << a.n << " inner=" << a.inner << " transposed [" << a.eng->describe() << "]}";
+        else
+            s << " axis{n=" << a.n << " inner=" << a.inner << " tile=" << a.tile << " " << a.prog->describe() << "}";
+    }
     return s.str();
 }
 
@@ -118,13 +156,13 @@ md_engine<T>::md_engine(const std::vector<long long>& shape)
 template <typename T>
 long long md_engine<T>::scratch_elems(long long batch) const
 {
-    return last_ ? last_->scratch_elems(batch * (total_ / shape_.back())) : 0;
+    return std::max(last_ ? last_->scratch_elems(batch * (total_ / shape_.back())) : 0LL, axes_.scratch_elems(batch));
 }
 
 template <typename T>
 int md_engine<T>::launches(long long batch) const
 {
-    return (last_ ? last_->launches(batch * (total_ / shape_.back())) : 1) + axes_.launches();
+    return (last_ ? last_->launches(batch * (total_ / shape_.back())) : 1) + axes_.launches(batch);
 }
 
 template <typename T>
@@ -138,7 +176,7 @@ void md_engine<T>::execute(void* out, const void* in, long long batch, bool inve
         last_->execute(out, in, batch * (total_ / nl), nl, nl, inverse, scratch, st);
     else if (out != in)
         check(cudaMemcpyAsync(out, in, batch * total_ * 2 * sizeof(T), cudaMemcpyDeviceToDevice, st), "copy");
-    axes_.run(out, batch, inverse, st);
+    axes_.run(out, batch, inverse, scratch, st);
 }
 
 template <typename T>
@@ -175,17 +213,18 @@ md_real_engine<T>::md_real_engine(const std::vector<long long>& shape, bool real
     last_.reset(new real_engine<T>(shape_.back()));
 }
 
+// Scratch: [W: batch complex arrays (inverse only)][R: the last axis's or the other axes' scratch].
 template <typename T>
 long long md_real_engine<T>::scratch_elems(long long batch) const
 {
     const long long rows = batch * (total_real_ / shape_.back());
-    return batch * total_cplx_ + last_->scratch_elems(rows);
+    return batch * total_cplx_ + std::max(last_->scratch_elems(rows), axes_.scratch_elems(batch));
 }
 
 template <typename T>
 int md_real_engine<T>::launches(long long batch) const
 {
-    return last_->launches(batch * (total_real_ / shape_.back())) + axes_.launches();
+    return last_->launches(batch * (total_real_ / shape_.back())) + axes_.launches(batch);
 }
 
 template <typename T>
@@ -196,7 +235,7 @@ void md_real_engine<T>::forward(void* out, const void* in, long long batch, void
     const long long rows = batch * (total_real_ / shape_.back());
     char* inner          = static_cast<char*>(scratch) + batch * total_cplx_ * 2 * sizeof(T);
     last_->forward(out, in, rows, true, inner, st);
-    axes_.run(out, batch, false, st);
+    axes_.run(out, batch, false, inner, st);
 }
 
 template <typename T>
@@ -209,7 +248,7 @@ void md_real_engine<T>::inverse(void* out, const void* in, long long batch, void
     char* inner          = W + batch * total_cplx_ * 2 * sizeof(T);
     check(cudaMemcpyAsync(W, in, batch * total_cplx_ * 2 * sizeof(T), cudaMemcpyDeviceToDevice, st),
           "copy spectrum");
-    axes_.run(W, batch, true, st);
+    axes_.run(W, batch, true, inner, st);
     last_->inverse(out, W, rows, true, inner, st);
 }
 

@@ -1,11 +1,13 @@
 // Multi-dimensional DFTs: dft_plan_md<T> and dft_plan_md_real<T> (include/kfr/dft/fft.hpp:568-924).
 //
 // The reference transforms the last axis of a row-major array, transposes, and repeats for every axis.  On
-// the GPU no transpose is needed: the last axis runs as a batched 1-D transform over contiguous rows, and
-// every other axis i runs in place as a column pass over the [outer][n_i][inner] view (tiles of adjacent
-// columns are staged in shared memory, transformed, and written back to the same places).  The real
-// variant does the CCs real DFT along the last axis first (forward) or last (inverse), like the reference,
-// so the complex array has the reference's complex_size() shape (last axis N/2 + 1).
+// the GPU the last axis runs as a batched 1-D transform over contiguous rows, and every other axis i whose
+// length fits one CTA runs in place as a column pass over the [outer][n_i][inner] view (tiles of adjacent
+// columns are staged in shared memory, transformed, and written back to the same places).  A longer axis
+// (any length: four-step, Rader, Bluestein) is transposed to [outer][inner][n_i] in scratch, transformed
+// there by the 1-D engine as outer x inner contiguous signals, and transposed back.  The real variant does
+// the CCs real DFT along the last axis first (forward) or last (inverse), like the reference, so the
+// complex array has the reference's complex_size() shape (last axis N/2 + 1).
 #pragma once
 
 #include "plan.hpp"
@@ -19,19 +21,29 @@ class md_axes
 public:
     // Axes 0 .. dims-2 of `cshape` (complex element shape) with length > 1.
     explicit md_axes(const std::vector<long long>& cshape);
-    // In place on `data` (batch arrays of the complex shape back to back).
-    void run(void* data, long long batch, bool inverse, cudaStream_t st) const;
-    int launches() const { return int(axes_.size()); }
+    // In place on `data` (batch arrays of the complex shape back to back); scratch: scratch_elems(batch)
+    // complex elements (none unless an axis is longer than one CTA).
+    void run(void* data, long long batch, bool inverse, void* scratch, cudaStream_t st) const;
+    long long scratch_elems(long long batch) const;
+    int launches(long long batch) const;
     std::string describe() const;
+    void check_device_error() const
+    {
+        for (const axis& a : axes_)
+            if (a.eng)
+                a.eng->check_device_error();
+    }
 
 private:
     struct axis
     {
         long long n, inner, outer;
         int tile;
-        std::unique_ptr<block_program<T>> prog;
+        std::unique_ptr<block_program<T>> prog; // column pass (axes that fit one CTA)
+        std::unique_ptr<complex_engine<T>> eng; // transposed 1-D pass (longer axes)
     };
     std::vector<axis> axes_;
+    long long total_ = 1;
 };
 
 template <typename T>
@@ -49,6 +61,7 @@ public:
     {
         if (last_)
             last_->check_device_error();
+        axes_.check_device_error();
     }
 
 private:
@@ -73,8 +86,8 @@ public:
     int launches(long long batch) const;
     void check_device_error() const
     {
-        if (last_)
-            last_->check_device_error();
+        last_->check_device_error();
+        axes_.check_device_error();
     }
 
 private:

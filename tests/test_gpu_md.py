@@ -82,3 +82,50 @@ def test_2d_3d_creators_and_large_shapes():
     # odd last axis of a real plan is rejected like the reference
     with pytest.raises(k.KfrError, match="even"):
         k.dft_plan_md_real((4, 7))
+
+
+def _oracle_fftn(orc, x, inverse=False):
+    """The oracle's FP64 1-D DFT applied along every axis (a multi-dimensional DFT is separable)."""
+    y = x.astype(np.complex128)
+    for ax in range(y.ndim):
+        moved = np.ascontiguousarray(np.moveaxis(y, ax, -1))
+        y = np.moveaxis(orc.dft(moved, inverse=inverse, threads=8), -1, ax)
+    return y
+
+
+@pytest.mark.parametrize("shape", [(65536, 64), (30720, 3, 4), (40009, 2), (8191, 5, 6), (2, 65537, 3)])
+def test_md_long_non_last_axes(orc, shape):
+    """Non-last axes longer than one CTA (four-step 65536 and 30720, Bluestein 40009 and 65537, Rader 8191):
+    transposed, transformed by the 1-D engine and transposed back (include/kfr/dft/fft.hpp:570-924 accepts
+    any shape)."""
+    rng = np.random.default_rng(sum(shape))
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    plan = k.dft_plan_md(shape)
+    assert "transposed" in plan.describe()
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    plan.execute(yd, xd)
+    assert rel_rms(yd.cpu().numpy(), _oracle_fftn(orc, x)) <= c32_tolerance(x.size)
+    plan.execute(yd, xd, inverse=True)
+    assert rel_rms(yd.cpu().numpy(), _oracle_fftn(orc, x, inverse=True)) <= c32_tolerance(x.size)
+    # host buffers and the plan's own scratch
+    y = np.zeros_like(x)
+    plan.execute(y, x)
+    assert rel_rms(y, _oracle_fftn(orc, x)) <= c32_tolerance(x.size)
+
+
+def test_md_real_long_first_axis(orc):
+    """A real 2-D plan whose first axis (65536) needs the transposed pass: forward against the oracle's
+    per-axis transform of the real input, and the round trip."""
+    shape = (65536, 16)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(shape).astype(np.float32)
+    plan = k.dft_plan_md_real(shape)
+    Xd = torch.empty(plan.complex_shape, dtype=torch.complex64, device="cuda")
+    xd = torch.from_numpy(x).cuda()
+    plan.execute(Xd, xd)
+    full = _oracle_fftn(orc, x.astype(np.complex128))
+    assert rel_rms(Xd.cpu().numpy(), full[:, : shape[1] // 2 + 1]) <= c32_tolerance(x.size)
+    yd = torch.empty_like(xd)
+    plan.execute(yd, Xd, inverse=True)
+    assert rel_rms(yd.cpu().numpy() / x.size, x) <= 2 * c32_tolerance(x.size)  # two transforms
