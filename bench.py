@@ -589,10 +589,33 @@ def main():
         ms_p = timed(lambda: up.execute(uy, ux, stream=stream), 10)
         up.execute_per_signal(uy, ux, stream=stream)
         ms_s = timed(lambda: up.execute_per_signal(uy, ux, stream=stream), 2)
+        # the batched plain form: the signals of each length stored contiguously (as if the caller had sorted
+        # them by length) and one batched plan execution per distinct length
+        classes = {}
+        for n in lengths:
+            classes[n] = classes.get(n, 0) + 1
+        cplans, cbufs = [], []
+        for n, c in sorted(classes.items()):
+            pl = k.dft_plan(n)
+            xb = torch.randn(c, n, dtype=torch.complex64, device=dev, generator=g)
+            tb = torch.empty(max(1, pl.temp_size_batch(c)), dtype=torch.uint8, device=dev)
+            cplans.append((pl, c))
+            cbufs.append((xb, torch.empty_like(xb), tb))
+
+        def per_class():
+            for (pl, c), (xb, yb, tb) in zip(cplans, cbufs):
+                pl.execute_batch(yb, xb, c, temp=tb, stream=stream)
+
+        per_class()
+        ms_c = timed(per_class, 3)
+        del cplans, cbufs
         ub = 16 * total
         uneven = {"signals": len(lengths), "elements": total, "persistent_ms": round(ms_p, 4),
                   "persistent_gbs": round(ub / (ms_p * 1e-3) / 1e9, 1), "per_signal_ms": round(ms_s, 3),
                   "per_signal_gbs": round(ub / (ms_s * 1e-3) / 1e9, 1), "speedup": round(ms_s / ms_p, 2),
+                  "length_classes": len(classes), "per_class_batched_ms": round(ms_c, 4),
+                  "per_class_batched_gbs": round(ub / (ms_c * 1e-3) / 1e9, 1),
+                  "frac": round(ub / (ms_p * 1e-3) / 1e9 / hbm, 4),
                   "plan": up.describe()}
         del ux, uy, up
 

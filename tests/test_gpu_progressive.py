@@ -22,6 +22,7 @@ def test_progressive_steps_are_launches_and_match_one_shot(orc, n):
     x = torch.randn(n, dtype=torch.complex64, device="cuda", generator=g)
     want = torch.empty_like(x)
     tmp = torch.empty(max(1, plan.temp_size_batch(1)), dtype=torch.uint8, device="cuda")
+    x64 = x.cpu().numpy().astype(np.complex128).reshape(1, n)
     for inverse in (False, True):
         plan.execute_batch(want, x, 1, temp=tmp, inverse=inverse)
         got = torch.full_like(x, float("nan"))
@@ -32,8 +33,8 @@ def test_progressive_steps_are_launches_and_match_one_shot(orc, n):
             done += 1
         assert done + 1 == total
         assert torch.equal(got, want), inverse
-    ref = orc.dft(x.cpu().numpy().astype(np.complex128).reshape(1, n))[0]
-    assert rel_rms(want.cpu().numpy(), ref) <= c32_tolerance(n)
+        ref = orc.dft(x64, inverse=inverse)[0]
+        assert rel_rms(got.cpu().numpy(), ref) <= c32_tolerance(n), inverse
 
 
 @pytest.mark.parametrize("n,sfx", [(30720, "f64"), (1 << 18, "f32"), (4096, "f64")])
