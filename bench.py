@@ -429,6 +429,28 @@ def run_reference(args):
     return 0
 
 
+def run_case(spec: str) -> int:
+    """One plan on device-resident c32 signals, three executions, for a profiler to capture: form "plain"
+    (the default plan) or "fp16" / "bf16" (the tensor-core plans), length n, `MiB` of signals (default 128)."""
+    import torch
+
+    import kfr_gb300 as k
+
+    parts = spec.split(":")
+    form, n = parts[0], int(parts[1])
+    mib = int(parts[2]) if len(parts) > 2 else 128
+    b = max(1, (mib << 20) // (8 * n))
+    plan = k.dft_plan(n) if form == "plain" else k.dft_plan_tensor(n, form)
+    x = torch.randn(b, n, dtype=torch.complex64, device="cuda")
+    y = torch.empty_like(x)
+    tmp = torch.empty(max(1, plan.temp_size_batch(b)), dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        plan.execute_batch(y, x, b, temp=tmp)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": spec, "batch": b, "plan": plan.describe()}))
+    return 0
+
+
 def config_dict():
     return {"workload": "c32 forward DFT, N in {1000,1536,2187,30720,127,8191}, 256 MiB batch per N",
             "sizes": SIZES, "batches": [batch_for(n) for n in SIZES], "bytes_per_n": BYTES_PER_SIZE,
@@ -447,7 +469,11 @@ def main():
     ap.add_argument("--no-rows", action="store_true", help="skip the real / DCT / filter / large-single rows")
     ap.add_argument("--sizes", type=str, default=None, help="comma-separated subset of the lengths (profiling)")
     ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
+    ap.add_argument("--case", type=str, default=None,
+                    help="profiling: run one plan `form:n[:MiB]` three times and exit (form: plain, fp16, bf16)")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case)
     global SIZES, BYTES_PER_SIZE
     if args.sizes:
         SIZES = [int(v) for v in args.sizes.split(",")]

@@ -272,10 +272,8 @@ class dft_plan(_plan):
               _stream_addr(stream))
 
     def describe(self) -> str:
-        if self.sfx != "f32":
-            return ""
         buf = ctypes.create_string_buffer(512)
-        _call("kfr_dft_describe_f32", self.handle, buf, 512)
+        _call(f"kfr_dft_describe_{self.sfx}", self.handle, buf, 512)
         return buf.value.decode()
 
     def progressive_total_steps(self) -> int:
@@ -292,7 +290,7 @@ class dft_plan(_plan):
         return bool(_call(self._fn("progressive_step"), self.handle, step))
 
     def launch_count(self, batch=1):
-        return _call("kfr_dft_get_launch_count_f32", self.handle, batch) if self.sfx == "f32" else None
+        return _call(f"kfr_dft_get_launch_count_{self.sfx}", self.handle, batch)
 
 
 class dft_plan_tensor(dft_plan):
