@@ -489,7 +489,10 @@ def main():
     rank, world, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # a stream of our own: the C ABI runs calls on a NULL stream (the default stream's handle) synchronously,
+    # and the timed steps are stream-ordered enqueues
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     hbm, peak_kind = peaks()
 
     plans, xs, ys = {}, {}, {}
