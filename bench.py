@@ -437,6 +437,19 @@ def run_case(spec: str) -> int:
     import kfr_gb300 as k
 
     parts = spec.split(":")
+    if parts[0] == "uneven":
+        # the uneven batch: `n` signals of log-uniform lengths on [64, 65536] in one persistent launch
+        from kfr_gb300.workloads import uneven_lengths
+
+        lengths = uneven_lengths(int(parts[1]))
+        up = k.dft_plan_uneven(lengths, autotune=True)
+        x = torch.randn(int(sum(lengths)), dtype=torch.complex64, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(3):
+            up.execute(y, x)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": spec, "elements": int(sum(lengths)), "plan": up.describe()}))
+        return 0
     form, n = parts[0], int(parts[1])
     mib = int(parts[2]) if len(parts) > 2 else 128
     b = max(1, (mib << 20) // (8 * n))
@@ -470,7 +483,8 @@ def main():
     ap.add_argument("--sizes", type=str, default=None, help="comma-separated subset of the lengths (profiling)")
     ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
     ap.add_argument("--case", type=str, default=None,
-                    help="profiling: run one plan `form:n[:MiB]` three times and exit (form: plain, fp16, bf16)")
+                    help="profiling: run one plan `form:n[:MiB]` three times and exit (form: plain, fp16, bf16; "
+                         "or uneven:count)")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case)

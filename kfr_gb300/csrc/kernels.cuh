@@ -1116,6 +1116,133 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_dct3(const dct_args a, co
 }
 
 // ---------------------------------------------------------------------------------------------------
+// DCT-II / DCT-III, contiguous batch, persistent and pipelined (compile-time n): tiles of `spc` signals of n
+// reals.  Three tile buffers rotate as in k_r2c_pipe: the input tile (bulk copy of spc n reals, then the
+// passes' A buffer), the scratch tile (B) and the spare tile, into which the next tile's copy is issued
+// after the first pass.  DCT-II (include/kfr/dft/fft.hpp:938-950): the first pass reads the even/odd mirror
+// of the reals straight from the input tile, the last pass writes Re(V[k]) cos + Im(V[k]) sin as reals into
+// the buffer it does not read.  DCT-III (fft.hpp:951-969): the first pass reads x[k] e^{-i pi k / 2n} (x[0]
+// halved), the last pass un-mirrors the real parts.  One bulk copy stores the tile.  Whole tiles only (the
+// host runs the remainder with k_dct2 / k_dct3).  A wait that runs out sets *err and the CTA returns.
+// ---------------------------------------------------------------------------------------------------
+template <typename T, class F>
+__host__ __device__ constexpr int dct_stage_elems(int spc)
+{
+    // complex elements: the real tiles (spc n / 2) and the padded work layout
+    const int a = spc * F::n / 2, b = spc * F::gstride(F::n);
+    return ((a > b ? a : b) + 15) / 16 * 16;
+}
+
+template <typename T, class F, bool INV>
+__global__ void __launch_bounds__(F::max_threads, 1)
+    k_dct_pipe(const dct_args a, const long long ntiles, const int spc, int* err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int N      = F::n;
+    constexpr int STRIDE = F::gstride(N);
+    const F fft(nullptr, a.d, F::ts);
+    const int slen       = dct_stage_elems<T, F>(spc);
+    cpx<T>* const tiles  = reinterpret_cast<cpx<T>*>(smem_raw);
+    uint64_t* bars       = reinterpret_cast<uint64_t*>(tiles + 3 * slen);
+    const uint32_t bytes = uint32_t(spc) * uint32_t(N) * uint32_t(sizeof(T));
+    const T* in          = reinterpret_cast<const T*>(a.in);
+    T* out               = reinterpret_cast<T*>(a.out);
+    const cpx<T>* tw     = reinterpret_cast<const cpx<T>*>(a.tw);
+    const cpx<T>* __restrict__ dtw = reinterpret_cast<const cpx<T>*>(a.dtw);
+    const group_map gm(F::ts, spc);
+    if (threadIdx.x == 0)
+    {
+        for (int b = 0; b < 3; b++)
+            mbar_init(&bars[b], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles)
+    {
+        mbar_arrive_expect_tx(&bars[0], bytes);
+        bulk_g2s(tiles, in + t * spc * N, bytes, &bars[0]);
+    }
+    uint32_t phase = 0;         // bit b: parity to wait for on tile buffer b
+    int bi = 0, bs = 1, bn = 2; // input, scratch and spare tile buffers
+    for (; t < ntiles; t += gridDim.x)
+    {
+        cpx<T>* in_t   = tiles + bi * slen;
+        cpx<T>* scr_t  = tiles + bs * slen;
+        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1, a.wait_spins);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicExch(err, 1);
+                // the copy waited for is the only load in flight (the next one is issued after this wait):
+                // give it a bounded chance to land in this CTA's shared memory before the CTA exits
+                mbar_wait(&bars[bi], (phase >> bi) & 1);
+                bulk_wait_all();
+            }
+            return;
+        }
+        phase ^= 1u << bi;
+        const long long tn  = t + gridDim.x;
+        const auto prefetch = [&]()
+        {
+            if (threadIdx.x == 0 && tn < ntiles)
+            {
+                // the spare buffer holds the previous tile's output: wait until its bulk store has read it
+                bulk_wait_read();
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bars[bn], bytes);
+                bulk_g2s(tiles + bn * slen, in + tn * spc * N, bytes, &bars[bn]);
+            }
+        };
+        // pass i writes B (i even) or A (i odd): with an odd pass count the last pass reads A and writes B
+        constexpr bool odd = F::npass % 2 == 1;
+        T* ob              = reinterpret_cast<T*>(odd ? scr_t : in_t);
+        const T* xs        = reinterpret_cast<const T*>(in_t) + gm.g * N;
+        T* os              = ob + gm.g * N;
+        const auto nothing = []() {};
+        if constexpr (!INV)
+            fft.run_pp(
+                [&](int p)
+                {
+                    const int i = p < N / 2 ? 2 * p : 2 * (N - 1 - p) + 1;
+                    return mk<T>(xs[i], T(0));
+                },
+                [&](int q, cpx<T> x)
+                {
+                    const cpx<T> w = ldg(dtw + q);
+                    os[q]          = x.x * w.x + x.y * w.y;
+                },
+                prefetch, nothing, in_t + gm.g * STRIDE, scr_t + gm.g * STRIDE, tw, gm.lt);
+        else
+            fft.run_pp(
+                [&](int p)
+                {
+                    const T x      = xs[p];
+                    const cpx<T> w = ldg(dtw + p);
+                    const cpx<T> v = mk<T>(x * w.x, -(x * w.y));
+                    return p == 0 ? scale(v, T(0.5)) : v;
+                },
+                [&](int q, cpx<T> x) { os[q < N / 2 ? 2 * q : 2 * (N - 1 - q) + 1] = x.x; }, prefetch, nothing,
+                in_t + gm.g * STRIDE, scr_t + gm.g * STRIDE, tw, gm.lt);
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            bulk_s2g(out + t * spc * N, ob, bytes);
+            bulk_commit();
+        }
+        // next: input = spare, scratch = the buffer the last pass read, spare = the buffer being stored
+        const int oi = odd ? bs : bi, ri = odd ? bi : bs;
+        bi = bn;
+        bs = ri;
+        bn = oi;
+    }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------------------------------
 // Four-step passes for lengths beyond one CTA (N = n1 * n2).  grid = (tiles, batch).
 // ---------------------------------------------------------------------------------------------------
 template <typename T>

@@ -150,6 +150,25 @@ cudaError_t launch_ct_c2r_pipe_f32(const real_args& a0, const block_cfg& c, long
 #undef KFR_GPU_C2R_PIPE_CASE
 }
 
+cudaError_t launch_ct_dct_pipe_f32(const dct_args& a0, const block_cfg& c, long long ntiles, int* err, bool inverse,
+                                   cudaStream_t st)
+{
+    dct_args a   = a0;
+    a.wait_spins = wait_limit();
+#define KFR_GPU_DCT_PIPE_CASE(N, TS, ...)                                                                  \
+    case N:                                                                                                \
+        return inverse ? go_persistent(k_dct_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>, true>, c, ntiles, st, a, \
+                                       ntiles, c.spc, err)                                                 \
+                       : go_persistent(k_dct_pipe<float, ct_fft<float, N, TS, __VA_ARGS__>, false>, c, ntiles, st, a, \
+                                       ntiles, c.spc, err);
+    switch (c.ct)
+    {
+        KFR_CT_DCT_F32(KFR_GPU_DCT_PIPE_CASE)
+    default: return cudaErrorInvalidValue;
+    }
+#undef KFR_GPU_DCT_PIPE_CASE
+}
+
 cudaError_t launch_ct_rader_tile_f32(const rader_args& a0, const block_cfg& c, long long ntiles, int* err,
                                      cudaStream_t st)
 {

@@ -112,6 +112,7 @@ struct dct_args
     const void* tw;
     fast_div div_n;
     fft_desc d;
+    unsigned wait_spins = kDefaultWaitSpins; // pipelined kernels: see kDefaultWaitSpins
 };
 
 // One pass of the four-step decomposition of N = n1 * n2 (x viewed as n1 rows by n2 columns).
@@ -214,6 +215,10 @@ cudaError_t launch_ct_c2c_pipe_f32(const c2c_args& a, const block_cfg& c, long l
 cudaError_t launch_ct_r2c_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st);
 // real inverse DFT, persistent and pipelined over tiles of c.spc (even) signals (compile-time c = n / 2)
 cudaError_t launch_ct_c2r_pipe_f32(const real_args& a, const block_cfg& c, long long ntiles, int* err, cudaStream_t st);
+// DCT-II (inverse = false) or DCT-III, persistent and pipelined over tiles of c.spc signals (compile-time n;
+// in and out 16-byte aligned, a.stride == n)
+cudaError_t launch_ct_dct_pipe_f32(const dct_args& a, const block_cfg& c, long long ntiles, int* err, bool inverse,
+                                   cudaStream_t st);
 // one signal per CTA, persistent, signal in registers between the passes (compile-time lengths >= 8192)
 cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st);
 cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c, cudaStream_t st);

@@ -1534,6 +1534,49 @@ dct_engine<T>::dct_engine(long long n) : n_(n), ceng_(n)
     fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
     if (fused_)
         prog_.build(int(n), CT_DCT);
+    // Pipelined kernels (compile-time n, single precision): the most resident threads per SM with at least
+    // two CTAs, then the smallest tile.
+    if (fused_ && prog_.ct && sizeof(T) == 4 && n % 4 == 0)
+    {
+        int best = 0, best_thr = 0;
+        for (int spc = 1; spc <= 32; spc++)
+        {
+            const int threads = ((spc * prog_.ts + 31) / 32) * 32;
+            if (threads > 1024)
+                break;
+            const int slen = (std::max(spc * int(n) / 2, spc * prog_.gstride) + 15) / 16 * 16;
+            const int smem = 3 * slen * int(2 * sizeof(T)) + 64;
+            if (smem > smem_budget())
+                break;
+            const int ctas = std::min((max_smem_bytes() + 1024) / (smem + 1024), 1024 / threads);
+            if (ctas >= 2 && ctas * threads > best_thr)
+            {
+                best_thr = ctas * threads;
+                best     = spc;
+            }
+        }
+        if (best)
+        {
+            pipe_spc_ = best;
+            err_.alloc(sizeof(int));
+            check(cudaMemset(err_.get(), 0, sizeof(int)), "clear error flag");
+        }
+    }
+}
+
+template <typename T>
+void dct_engine<T>::check_device_error() const
+{
+    ceng_.check_device_error();
+    if (!err_.get())
+        return;
+    int v = 0;
+    check(cudaMemcpy(&v, err_.get(), sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+    if (v)
+    {
+        cudaMemset(err_.get(), 0, sizeof(int));
+        throw cuda_error("a DCT kernel gave up waiting for its input copy (device error flag set)");
+    }
 }
 
 template <typename T>
@@ -1547,6 +1590,8 @@ long long dct_engine<T>::scratch_elems(long long batch) const
 template <typename T>
 int dct_engine<T>::launches(long long batch) const
 {
+    if (fused_ && pipe_spc_)
+        return (batch / pipe_spc_ > 0 ? 1 : 0) + (batch % pipe_spc_ ? 1 : 0);
     return fused_ ? 1 : 2 + ceng_.launches(batch);
 }
 
@@ -1568,7 +1613,28 @@ void dct_engine<T>::execute(void* out, const void* in, long long batch, bool inv
         a.tw     = p.tw.get();
         a.div_n  = make_fast_div(uint32_t(n_));
         a.d      = p.desc;
-        check(inverse ? launch_dct3<T>(a, p.cfg(batch), st) : launch_dct2<T>(a, p.cfg(batch), st), "launch dct");
+        long long done = 0;
+        if (pipe_spc_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 && (reinterpret_cast<uintptr_t>(out) % 16) == 0)
+        {
+            const long long ntiles = batch / pipe_spc_;
+            if (ntiles > 0)
+            {
+                block_cfg pc = p.cfg_tile(pipe_spc_);
+                pc.smem = 3 * ((std::max(pipe_spc_ * int(n_) / 2, pipe_spc_ * p.gstride) + 15) / 16 * 16) *
+                              int(2 * sizeof(T)) + 64;
+                check(launch_ct_dct_pipe_f32(a, pc, ntiles, static_cast<int*>(err_.get()), inverse, st),
+                      "launch dct (pipelined)");
+                done = ntiles * pipe_spc_;
+            }
+        }
+        if (done < batch)
+        {
+            a.in    = static_cast<const T*>(in) + done * n_;
+            a.out   = static_cast<T*>(out) + done * n_;
+            a.batch = batch - done;
+            check(inverse ? launch_dct3<T>(a, p.cfg(batch - done), st) : launch_dct2<T>(a, p.cfg(batch - done), st),
+                  "launch dct");
+        }
         return;
     }
     char* V     = static_cast<char*>(scratch);
@@ -1595,7 +1661,10 @@ template <typename T>
 std::string dct_engine<T>::describe() const
 {
     std::ostringstream s;
-    s << "dct n=" << n_ << (fused_ ? " fused" : " separate pre/post") << " complex{" << ceng_.describe() << "}";
+    s << "dct n=" << n_ << (fused_ ? " fused" : " separate pre/post");
+    if (pipe_spc_)
+        s << " pipelined spc=" << pipe_spc_;
+    s << " complex{" << ceng_.describe() << "}";
     return s.str();
 }
 

@@ -236,7 +236,7 @@ public:
     std::string describe() const;
     long long size() const { return n_; }
     int launches(long long batch) const;
-    void check_device_error() const { ceng_.check_device_error(); }
+    void check_device_error() const;
 
 private:
     long long n_;
@@ -244,6 +244,8 @@ private:
     block_program<T> prog_; // fused kernels: n-point program
     dbuf dtw_;
     bool fused_ = false;
+    int pipe_spc_ = 0; // signals per tile of the pipelined kernels, 0 = not used
+    dbuf err_;
 };
 
 } // namespace kfr_gpu

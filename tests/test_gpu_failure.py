@@ -96,3 +96,22 @@ def test_uneven_stage_wait_runs_out_within_a_second(restore_limit, orc):
         ref = orc.dft(xs[off:off + n].astype(np.complex128).reshape(1, n))[0]
         assert rel_rms(ys[off:off + n], ref) <= c32_tolerance(n), n
         off += n
+
+
+@pytest.mark.parametrize("inverse", [False, True])
+def test_dct_pipelined_wait_reported(restore_limit, inverse):
+    """k_dct_pipe (DCT-II and DCT-III, N = 512, 4096 signals)."""
+    n, batch = 512, 4096
+    plan = k.dct_plan(n)
+    g = torch.Generator(device="cuda").manual_seed(6)
+    x = torch.rand(batch, n, device="cuda", generator=g) * 2 - 1
+    y = torch.empty_like(x)
+    want = torch.empty_like(x)
+    plan.execute_batch(want, x, batch, inverse=inverse)
+    L = k.lib()
+    L.kfr_set_wait_limit(0)
+    with pytest.raises(k.KfrError, match="gave up waiting"):
+        plan.execute_batch(y, x, batch, inverse=inverse)
+    L.kfr_set_wait_limit(DEFAULT)
+    plan.execute_batch(y, x, batch, inverse=inverse)
+    assert torch.equal(y, want)

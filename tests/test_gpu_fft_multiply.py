@@ -65,3 +65,14 @@ def test_fft_multiply_rejects_host_pointers():
     L = k.lib()
     L.kfr_fft_multiply_f32(x.ctypes.data, x.ctypes.data, x.ctypes.data, 16, 1, False, 1, None)
     assert b"device pointers" in L.kfr_last_error()
+
+
+def test_fft_multiply_empty_is_a_no_op():
+    """size 0 or batch 0: nothing runs and no error is reported (the reference's empty univectors)."""
+    x = torch.ones(4, dtype=torch.complex64, device="cuda")
+    L = k.lib()
+    L.kfr_fft_multiply_f32(x.data_ptr(), x.data_ptr(), x.data_ptr(), 0, 1, False, 1, None)
+    assert L.kfr_last_error() == b""
+    L.kfr_fft_multiply_accumulate_f32(x.data_ptr(), x.data_ptr(), x.data_ptr(), x.data_ptr(), 4, 0, False, 1, None)
+    assert L.kfr_last_error() == b""
+    assert torch.equal(x, torch.ones_like(x))

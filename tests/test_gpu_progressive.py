@@ -13,7 +13,7 @@ import kfr_gb300 as k  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n", [4096, 1000, 127, 8191, 30720, 1 << 16, 1 << 20, 40009, 3 * 65537])
+@pytest.mark.parametrize("n", [1, 2, 4096, 1000, 127, 8191, 30720, 1 << 16, 1 << 20, 40009, 3 * 65537])
 def test_progressive_steps_are_launches_and_match_one_shot(orc, n):
     plan = k.dft_plan(n)
     total = plan.progressive_total_steps()
