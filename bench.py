@@ -442,7 +442,7 @@ def run_case(spec: str) -> int:
         from kfr_gb300.workloads import uneven_lengths
 
         lengths = uneven_lengths(int(parts[1]))
-        up = k.dft_plan_uneven(lengths, autotune=True)
+        up = k.dft_plan_uneven(lengths, autotune=not (len(parts) > 2 and parts[2] == "fixed"))
         x = torch.randn(int(sum(lengths)), dtype=torch.complex64, device="cuda")
         y = torch.empty_like(x)
         for _ in range(3):
@@ -484,7 +484,7 @@ def main():
     ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
     ap.add_argument("--case", type=str, default=None,
                     help="profiling: run one plan `form:n[:MiB]` three times and exit (form: plain, fp16, bf16; "
-                         "or uneven:count)")
+                         "or uneven:count[:fixed], fixed = no autotuning)")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case)
