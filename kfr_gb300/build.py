@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = [
     "kernels_f32.cu", "kernels_f64.cu", "kernels_ct_a.cu", "kernels_ct_b.cu", "kernels_ct_c.cu", "elementwise.cu",
-    "conv.cu", "convolve.cu", "adjoint.cu", "uneven.cu", "tensor.cu", "static_scratch.cu",
+    "conv.cu", "convolve.cu", "adjoint.cu", "uneven.cu", "tensor.cu", "static_scratch.cu", "rader_pfa.cu",
 ]
 CPP_SOURCES = ["plan.cpp", "md.cpp", "capi.cpp"]
 

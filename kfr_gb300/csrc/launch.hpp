@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstddef>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "fft_desc.hpp"
@@ -83,6 +84,26 @@ struct rader_args
     fft_desc d;
     unsigned wait_spins = kDefaultWaitSpins; // persistent pipelined kernels: see kDefaultWaitSpins
 };
+
+// Rader's algorithm with prime-factor convolution DFTs (rader_pfa.cu): in and out 16-byte aligned, signals
+// contiguous (stride n); tin / tout / bphys: the gather, scatter and kernel-spectrum tables over the
+// prime-factor array of L = n - 1 points (see rader_pfa.cu).
+struct rader_pfa_args
+{
+    const void* in;
+    void* out;
+    long long batch;
+    int inverse;
+    const int* tin;
+    const int* tout;
+    const void* bphys;
+    int* err; // set when a wait for a tile copy runs out
+    unsigned wait_spins = kDefaultWaitSpins;
+};
+// Whether a compile-time prime-factor Rader kernel exists for n (single precision): its axes (axis 0 first,
+// the fused axis last) and signals per tile.
+bool rader_pfa_shape(long long n, std::vector<int>& axes, int& spc);
+cudaError_t launch_rader_pfa_f32(const rader_pfa_args& a, long long n, cudaStream_t st);
 
 // Real DFT of even length 2c through a c-point complex DFT (d.n = c).
 // Forward: in = reals (istride reals apart), out = c+1 (CCs) or c (Perm) complex (ostride complex apart).

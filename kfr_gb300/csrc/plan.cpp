@@ -675,6 +675,49 @@ void complex_engine<T>::init_rader(long long n)
         rtw2_.upload(t2.data(), t2.size() * sizeof(std::complex<T>));
     }
     k_ = kind::rader_smem;
+    // The prime-factor kernel (rader_pfa.cu) where one is compiled for n: its gather, scatter and
+    // kernel-spectrum tables over the row-major array of the coprime axes r_i (L_i = L / r_i): position pos
+    // with coordinates c_i holds a[p] for the p with p = c_i (mod r_i) (CRT) on input, A[k] for
+    // k = sum c_i L_i (mod L) (Ruritanian) between the two DFTs, and C[p] for the CRT p on output.
+    pfa_spc_ = 0;
+    std::vector<int> ax;
+    int pspc = 0;
+    if (sizeof(T) == 4 && rader_pfa_shape(n, ax, pspc))
+    {
+        const int D = int(ax.size());
+        std::vector<long long> stride(D, 1), crt(D);
+        for (int i = D - 2; i >= 0; i--)
+            stride[i] = stride[i + 1] * ax[i + 1];
+        for (int i = 0; i < D; i++)
+        {
+            // crt[i] = L_i * (L_i^-1 mod r_i): 1 mod r_i, 0 mod the other axes
+            const long long Li = L / ax[i];
+            long long inv = 1;
+            while ((Li % ax[i]) * inv % ax[i] != 1)
+                inv++;
+            crt[i] = Li * inv % L;
+        }
+        std::vector<int> tin(L), tout(L);
+        std::vector<std::complex<T>> bph(L);
+        for (long long pos = 0; pos < L; pos++)
+        {
+            long long p = 0, k = 0;
+            for (int i = 0; i < D; i++)
+            {
+                const long long c = (pos / stride[i]) % ax[i];
+                p                 = (p + c * crt[i]) % L;
+                k                 = (k + c * (L / ax[i])) % L;
+            }
+            tin[pos]  = gpow[p];
+            tout[pos] = gpow[(L - p) % L];
+            bph[pos]  = bh[k];
+        }
+        tin_.upload(tin.data(), tin.size() * sizeof(int));
+        tout_.upload(tout.data(), tout.size() * sizeof(int));
+        bphys_.upload(bph.data(), bph.size() * sizeof(std::complex<T>));
+        pfa_spc_  = pspc;
+        pfa_axes_ = ax;
+    }
     // Signals per tile of the pipelined kernel: one signal when it takes half a CTA's threads or more,
     // otherwise as many as leave room for two CTAs per SM (each holding two stage tiles and a work tile).
     rader_spc_ = 0;
@@ -1100,6 +1143,22 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
     }
     case kind::rader_smem:
     {
+        if (pfa_spc_ && err_.get() && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 &&
+            (reinterpret_cast<uintptr_t>(out) % 16) == 0)
+        {
+            // the prime-factor kernel takes every signal (its last tile may be shorter)
+            rader_pfa_args p;
+            p.in      = in;
+            p.out     = out;
+            p.batch   = batch;
+            p.inverse = inverse;
+            p.tin     = static_cast<const int*>(tin_.get());
+            p.tout    = static_cast<const int*>(tout_.get());
+            p.bphys   = bphys_.get();
+            p.err     = static_cast<int*>(err_.get());
+            check(launch_rader_pfa_f32(p, n_, st), "launch rader (prime factor)");
+            return;
+        }
         rader_args a;
         a.in      = in;
         a.out     = out;
@@ -1277,6 +1336,14 @@ std::string complex_engine<T>::describe() const
         break;
     case kind::bluestein_multi: s << "bluestein_multi n=" << n_ << " m=" << m_ << " inner{" << inner_->describe() << "}"; break;
     case kind::rader_smem:
+        if (pfa_spc_)
+        {
+            s << "rader n=" << n_ << " prime-factor axes=";
+            for (size_t i = 0; i < pfa_axes_.size(); i++)
+                s << (i ? "x" : "") << pfa_axes_[i];
+            s << " in place, spc=" << pfa_spc_;
+            break;
+        }
         s << "rader n=" << n_ << " [" << prog_.describe() << "]";
         if (rader_spc_)
             s << " tiled spc=" << rader_spc_;

@@ -197,6 +197,11 @@ private:
     // Rader
     dbuf pin_, qof_, gp_, rtw2_;
     int rader_spc_ = 0; // signals per tile of the pipelined kernel, 0 = not used
+    // Rader with prime-factor convolution DFTs (rader_pfa.cu): signals per tile (0 = not used), its axes and
+    // its gather / scatter / kernel-spectrum tables
+    int pfa_spc_ = 0;
+    std::vector<int> pfa_axes_;
+    dbuf tin_, tout_, bphys_;
     int rader_tile_smem(int spc) const;
 };
 
