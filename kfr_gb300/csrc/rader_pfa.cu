@@ -1,5 +1,5 @@
 // Rader's algorithm with prime-factor (Good-Thomas) convolution DFTs, for primes N whose L = N - 1 splits
-// into pairwise coprime compile-time radices (8191: 8190 = 13 * 2 * 7 * 9 * 5; 127: 126 = 14 * 9).
+// into pairwise coprime compile-time radices (8191: 8190 = 13 * 5 * 9 * 14; 127: 126 = 14 * 9).
 //
 // Rader (as in the tiled kernel): a[p] = x[g^p] (p < L), A = DFT_L(a), A'[k] = conj(A[k] bhat[k]) with
 // bhat = DFT_L(b) / L, b[m] = W_N^{g^-m}; C = DFT_L(A'); X[g^-q] = x[0] + conj(C[q]); X[0] = x[0] + A[0].
@@ -19,13 +19,15 @@
 // butterfly in place (it reads and writes its own r_i elements only), so one buffer per signal suffices and
 // only the gather and the scatter need a barrier between their reads and their writes.
 //
-// Kernel: persistent over tiles of SPC contiguous signals; one shared buffer per CTA holds a tile.  A bulk
-// copy brings the tile's enclosing 16-byte range in; pass 1 (axis 0) gathers into registers, a barrier,
-// then writes the array; the middle axes run in place; the last axis of the first DFT and the same axis of
-// the second are fused around the multiplication by bphys; the second DFT's axis-0 pass reads into
-// registers, a barrier, then scatters X in natural order into the buffer, which one bulk copy stores (the
-// tile's edge elements beyond the 16-byte interior by plain stores).  The next tile's copy waits until that
-// store has read the buffer; the other CTA on the SM covers the gap.
+// Kernel: persistent over tiles of SPC contiguous signals; a shared buffer per tile in flight (NBUF = 2: the
+// next tile's copy lands in the second buffer while this one is transformed).  A bulk copy brings the tile's
+// enclosing 16-byte range in; pass 1 (axis 0) gathers into registers, a barrier, then writes the array; the
+// middle axes run in place; the last axis of the first DFT and the same axis of the second are fused around
+// the multiplication by bphys; the second DFT's axis-0 pass reads into registers, a barrier, then scatters X
+// in natural order into the buffer, which one bulk copy stores (the tile's edge elements beyond the 16-byte
+// interior by plain stores).  Measured on 256 MiB batches (N=8191: 640 threads, one CTA per SM; N=127: 24
+// signals per tile, four CTAs per SM), two buffers beat one by 16% to 20%, and the tiled ping-pong kernel
+// (three buffers, twiddled passes) by 12% (8191) and 22% (127).
 #include "kernels.cuh"
 
 namespace kfr_gpu
@@ -114,7 +116,7 @@ __host__ __device__ constexpr int pfa_buflen()
     return ((SPC * N + 2 > SPC * (N - 1) ? SPC * N + 2 : SPC * (N - 1)) + 15) / 16 * 16;
 }
 
-template <typename T, int N, int SPC, int THREADS, int MINB, int... R>
+template <typename T, int N, int SPC, int THREADS, int MINB, int NBUF, int... R>
 __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_args a, const long long ntiles)
 {
     using AX          = axes<R...>;
@@ -128,52 +130,77 @@ __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_arg
     static_assert(AX::len() == L, "the axes multiply to N - 1");
     static_assert(SPC * NB0 <= THREADS, "one axis-0 butterfly per thread in the gather and scatter passes");
     static_assert(D >= 2, "at least the gather axis and the fused axis");
+    static_assert(NBUF == 1 || NBUF == 2, "one buffer, or two with the next tile's copy overlapping");
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    cpx<T>* const buf = reinterpret_cast<cpx<T>*>(smem_raw);
-    cpx<T>* x0s       = buf + pfa_buflen<N, SPC>();
-    cpx<T>* a0s       = x0s + SPC;
-    uint64_t* bar     = reinterpret_cast<uint64_t*>(a0s + SPC);
+    cpx<T>* const bufs = reinterpret_cast<cpx<T>*>(smem_raw);
+    cpx<T>* x0s        = bufs + NBUF * pfa_buflen<N, SPC>();
+    cpx<T>* a0s        = x0s + SPC;
+    uint64_t* bars     = reinterpret_cast<uint64_t*>(a0s + SPC);
     // kernel parameters are read where they are used (from the parameter bank), and the tile's byte range is
     // recomputed after the passes, so that little stays live across the passes' register-heavy codelets
     constexpr long long tile_bytes = (long long)SPC * N * ESZ;
+    // thread 0 issues tile tt's copy into buffer b (after the store that last read it, which is the only
+    // store outstanding then); the final 8-byte element of the last tile, beyond its 16-byte interior (the
+    // enclosing range could reach past the batch), is loaded by a plain load
+    const auto load = [&](long long tt, int b)
+    {
+        const int nt       = int(a.batch - tt * SPC < SPC ? a.batch - tt * SPC : SPC);
+        const long long s0 = tt * tile_bytes, e = s0 + (long long)nt * N * ESZ;
+        const long long a0 = s0 & ~15LL;
+        const long long a1 = tt == ntiles - 1 ? (e & ~15LL) : ((e + 15) & ~15LL);
+        const char* inb    = reinterpret_cast<const char*>(a.in);
+        cpx<T>* dst        = bufs + b * pfa_buflen<N, SPC>();
+        bulk_wait_read();
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bars[b], uint32_t(a1 - a0));
+        bulk_g2s(dst, inb + a0, uint32_t(a1 - a0), &bars[b]);
+        if (a1 < e)
+            *reinterpret_cast<cpx<T>*>(reinterpret_cast<char*>(dst) + (e - ESZ - a0)) =
+                *reinterpret_cast<const cpx<T>*>(inb + e - ESZ);
+    };
     if (threadIdx.x == 0)
     {
-        mbar_init(bar, 1);
+        for (int b = 0; b < NBUF; b++)
+            mbar_init(&bars[b], 1);
         mbar_fence_init();
     }
     __syncthreads();
-    uint32_t phase = 0;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, phase ^= 1)
+    if (threadIdx.x == 0 && blockIdx.x < ntiles)
+        load(blockIdx.x, 0);
+    uint32_t phase   = 0; // bit b: parity to wait for on buffer b
+    uint32_t pending = blockIdx.x < ntiles ? 1u : 0u; // bit b: a copy into buffer b is in flight
+    int cur          = 0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x)
     {
-        const int ns = int(a.batch - t * SPC < SPC ? a.batch - t * SPC : SPC);
-        if (threadIdx.x == 0)
-        {
-            const long long s0 = t * tile_bytes, e = s0 + (long long)ns * N * ESZ;
-            const long long a0 = s0 & ~15LL;
-            // the last tile's enclosing range could reach past the batch: its final 8-byte element beyond
-            // the 16-byte interior is loaded separately
-            const long long a1 = t == ntiles - 1 ? (e & ~15LL) : ((e + 15) & ~15LL);
-            const char* inb    = reinterpret_cast<const char*>(a.in);
-            bulk_wait_read(); // the previous tile's store has read the buffer
-            fence_proxy_async_smem();
-            mbar_arrive_expect_tx(bar, uint32_t(a1 - a0));
-            bulk_g2s(buf, inb + a0, uint32_t(a1 - a0), bar);
-            if (a1 < e)
-                *reinterpret_cast<cpx<T>*>(reinterpret_cast<char*>(buf) + (e - ESZ - a0)) =
-                    *reinterpret_cast<const cpx<T>*>(inb + e - ESZ);
-        }
-        const bool got = mbar_wait(bar, phase, a.wait_spins);
+        const int ns      = int(a.batch - t * SPC < SPC ? a.batch - t * SPC : SPC);
+        cpx<T>* const buf = bufs + cur * pfa_buflen<N, SPC>();
+        const bool got    = mbar_wait(&bars[cur], (phase >> cur) & 1, a.wait_spins);
         if (!__syncthreads_and(got))
         {
             if (threadIdx.x == 0)
             {
                 atomicExch(a.err, 1);
-                // the copy waited for is the only load in flight: give it a bounded chance to land in this
-                // CTA's shared memory before the CTA exits
-                mbar_wait(bar, phase);
+                // give every copy in flight into this CTA's shared memory a bounded chance to land before the
+                // CTA exits
+                for (int b = 0; b < NBUF; b++)
+                    if ((pending >> b) & 1)
+                        mbar_wait(&bars[b], (phase >> b) & 1);
                 bulk_wait_all();
             }
             return;
+        }
+        phase ^= 1u << cur;
+        pending &= ~(1u << cur);
+        const long long tn = t + gridDim.x;
+        if constexpr (NBUF == 2)
+        {
+            // the next tile streams into the other buffer while this one is transformed
+            if (tn < ntiles)
+            {
+                pending |= 1u << (cur ^ 1);
+                if (threadIdx.x == 0)
+                    load(tn, cur ^ 1);
+            }
         }
         const int off = int(((t * tile_bytes) & 15) / ESZ); // the tile's first element in the buffer
         const bool inv = a.inverse != 0;
@@ -249,16 +276,27 @@ __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_arg
             *reinterpret_cast<cpx<T>*>(outb + s0) = buf[off];
         if (threadIdx.x == 64 % THREADS && c1 != e)
             *reinterpret_cast<cpx<T>*>(outb + e - ESZ) = buf[off + ns * N - 1];
-        __syncthreads(); // the edge stores have read the buffer before the next tile's copy is issued
+        __syncthreads(); // the edge stores have read the buffer before a later copy overwrites it
+        if constexpr (NBUF == 1)
+        {
+            if (tn < ntiles)
+            {
+                pending |= 1u;
+                if (threadIdx.x == 0)
+                    load(tn, 0);
+            }
+        }
+        else
+            cur ^= 1;
     }
     if (threadIdx.x == 0)
         bulk_wait_all();
 }
 
-template <int N, int SPC>
+template <int N, int SPC, int NBUF>
 constexpr int pfa_smem()
 {
-    return (pfa_buflen<N, SPC>() + 2 * SPC) * 8 + 16;
+    return (NBUF * pfa_buflen<N, SPC>() + 2 * SPC) * 8 + 16;
 }
 
 template <class K>
@@ -280,16 +318,17 @@ cudaError_t go_pfa(K kernel, int threads, int smem, long long ntiles, const rade
     return cudaGetLastError();
 }
 
-// The compile-time instances: X(N, signals per tile, threads, CTAs per SM, axes: gather axis first, fused last)
+// The compile-time instances: X(N, signals per tile, threads, CTAs per SM, buffers, axes: gather axis first,
+// fused axis last)
 #define KFR_RADER_PFA_F32(X)                                                                               \
-    X(8191, 1, 640, 2, 13, 2, 7, 9, 5)                                                                         \
-    X(127, 56, 512, 2, 14, 9)
+    X(8191, 1, 640, 1, 2, 13, 5, 9, 14)                                                                      \
+    X(127, 24, 224, 4, 2, 14, 9)
 
 } // namespace
 
 bool rader_pfa_shape(long long n, std::vector<int>& axes_out, int& spc)
 {
-#define KFR_RADER_PFA_SHAPE(N, SPC, TH, MB, ...)                                                           \
+#define KFR_RADER_PFA_SHAPE(N, SPC, TH, MB, NB, ...)                                                           \
     if (n == N)                                                                                            \
     {                                                                                                      \
         axes_out = { __VA_ARGS__ };                                                                        \
@@ -305,9 +344,9 @@ cudaError_t launch_rader_pfa_f32(const rader_pfa_args& a0, long long n, cudaStre
 {
     rader_pfa_args a = a0;
     a.wait_spins     = wait_limit();
-#define KFR_RADER_PFA_CASE(N, SPC, TH, MB, ...)                                                            \
+#define KFR_RADER_PFA_CASE(N, SPC, TH, MB, NB, ...)                                                        \
     if (n == N)                                                                                            \
-        return go_pfa(k_rader_pfa<float, N, SPC, TH, MB, __VA_ARGS__>, TH, pfa_smem<N, SPC>(),            \
+        return go_pfa(k_rader_pfa<float, N, SPC, TH, MB, NB, __VA_ARGS__>, TH, pfa_smem<N, SPC, NB>(),    \
                       (a.batch + SPC - 1) / SPC, a, st);
     KFR_RADER_PFA_F32(KFR_RADER_PFA_CASE)
 #undef KFR_RADER_PFA_CASE
