@@ -43,15 +43,15 @@ FALLBACK_HBM_GBS = 6800.0
 
 # DRAM bytes per signal measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided
 # by the signals it processed; one-pass metrics captured on the full 256 MiB batches of this workload), from
-# the k_c2c_pipe, k_fspt_cols / k_fspt_rows and k_rader_tile launches summarised under profiles/.  Writes fall
+# the k_c2c_pipe, k_fspt_cols / k_fspt_rows and k_rader_pfa launches summarised under profiles/.  Writes fall
 # short of the algorithmic bytes by the output still in L2 when a launch ends.
 NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float] = {
-    1000: (268_458_752 + 220_087_808) / 33554,
-    1536: (268_478_976 + 213_590_016) / 21845,
-    2187: (268_478_464 + 216_733_952) / 15342,
-    30720: (268_411_904 + 216_763_648 + 268_468_480 + 212_934_144) / 1092,
-    127: (268_505_088 + 213_239_040) / 264208,
-    8191: (268_732_928 + 214_331_648) / 4096,
+    1000: (268_458_240 + 221_152_000) / 33554,
+    1536: (268_477_440 + 213_674_240) / 21845,
+    2187: (268_476_672 + 216_896_512) / 15342,
+    30720: (268_411_904 + 216_671_488 + 268_498_176 + 213_238_528) / 1092,
+    127: (268_488_960 + 213_872_128) / 264208,
+    8191: (268_600_064 + 213_764_096) / 4096,
 }
 
 

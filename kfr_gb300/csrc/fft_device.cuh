@@ -791,113 +791,6 @@ __device__ __forceinline__ void ct_block_fft_pp(const LD& ld, const ST& st, cons
     pp_chain<T, N, TS, 1, 0, 0, LD, ST, H, P, Rs...>(ld, st, hook, pre_last, A, B, tw, lta, post);
 }
 
-// ---------------------------------------------------------------------------------------------------
-// Cyclic convolution core of Rader's algorithm in 2K - 1 ping-pong passes (K radices R_1..R_K):
-//   forward L-point DFT, pointwise map, forward L-point DFT.
-// With Stockham passes, butterfly j of the first transform's last pass (radix R_K, stride L / R_K) produces
-// its outputs j + r L / R_K, which are exactly the inputs of butterfly j of a first pass of radix R_K of the
-// second transform.  So the second transform runs its radices in reverse order (R_K, ..., R_1, twiddles in
-// tw2) and its first pass is done in registers, inside the first transform's last pass:
-//   v = DFT_RK(twiddled inputs);  z[r] = mid(q = j + r L / R_K, v[r]);  DFT_RK(z) -> outputs j R_K + r.
-// ld(p) fetches input p of the first pass, mid(q, x) maps output q of the first transform to input q of the
-// second, st(q, x) stores output q of the second transform.  Pass i (i = 0 .. 2K - 2) writes B (i even)
-// or A (i odd); the last pass (even) reads A.  hook() runs after the first pass.  Ends with a barrier.
-// ---------------------------------------------------------------------------------------------------
-template <int... Rs>
-struct radix_seq
-{
-    // the second transform's passes after its first (radices R_{K-1}, ..., R_1 starting at stride R_K)
-    template <typename T, int N, int TS, int NS, int I, class LD, class ST>
-    static __device__ __forceinline__ void tail(const LD& ld, const ST& st, cpx<T>* A, cpx<T>* B,
-                                                const cpx<T>* __restrict__ tw, const int lt)
-    {
-        const auto nothing = []() {};
-        pp_chain<T, N, TS, NS, 0, I, LD, ST, decltype(nothing), decltype(nothing), Rs...>(ld, st, nothing, nothing,
-                                                                                           A, B, tw, lt);
-    }
-};
-
-// radix_seq of R_{K-1}, ..., R_1 for the list R_1, ..., R_K (all but the last, reversed)
-template <class Acc, int... Rs>
-struct rev_init;
-template <int... A, int R>
-struct rev_init<radix_seq<A...>, R>
-{
-    using type = radix_seq<A...>;
-};
-template <int... A, int R, int R2, int... Rs>
-struct rev_init<radix_seq<A...>, R, R2, Rs...>
-{
-    using type = typename rev_init<radix_seq<R, A...>, R2, Rs...>::type;
-};
-
-template <typename T, int N, int TS, int R, int NS, int TWOFF, class LD, class MID, class ST>
-__device__ __forceinline__ void pp_pass_fused(const LD& ld, const MID& mid, const ST& st,
-                                              const cpx<T>* __restrict__ tw, const int lt)
-{
-    static_assert(NS * R == N && NS > 1, "the fused pass is the last pass of a chain of two or more");
-    constexpr int NBF = N / R;
-    constexpr int NB  = (NBF + TS - 1) / TS;
-#pragma unroll
-    for (int b = 0; b < NB; b++)
-    {
-        const int j = lt + b * TS;
-        if (j < NBF)
-        {
-            cpx<T> v[R];
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                v[r] = ld(j + r * NBF);
-            twiddle_powers<T, R>(v, ldg(tw + TWOFF + j));
-            dft_codelet<T, R>(v);
-            cpx<T> z[R];
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                z[r] = mid(j + r * NS, v[codelet_out<R>(r)]);
-            dft_codelet<T, R>(z);
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                st(j * R + r, z[codelet_out<R>(r)]);
-        }
-    }
-    __syncthreads();
-}
-
-template <typename T, int N, int TS, int NS, int TWOFF, int I, class Tail, class LD, class MID, class ST, class H,
-          int R, int... Rest>
-__device__ __forceinline__ void pp_conv_chain(const LD& ld, const MID& mid, const ST& st, const H& hook, cpx<T>* A,
-                                              cpx<T>* B, const cpx<T>* __restrict__ tw,
-                                              const cpx<T>* __restrict__ tw2, const int lt)
-{
-    cpx<T>* dst     = (I % 2 == 0) ? B : A;
-    const auto d_st = [dst](int q, cpx<T> x) { dst[pidx_s<ct_ps<T>(N, TS)>(q)] = x; };
-    const auto d_ld = [dst](int p) { return dst[pidx_s<ct_ps<T>(N, TS)>(p)]; };
-    if constexpr (sizeof...(Rest) == 0)
-    {
-        pp_pass_fused<T, N, TS, R, NS, TWOFF>(ld, mid, d_st, tw, lt);
-        Tail::template tail<T, N, TS, R, I + 1>(d_ld, st, A, B, tw2, lt);
-    }
-    else
-    {
-        constexpr int TN = TWOFF + (NS > 1 ? NS * (R - 1) : 0);
-        pp_pass<T, N, TS, R, NS, TWOFF>(ld, d_st, tw, lt);
-        if constexpr (NS == 1)
-            hook();
-        pp_conv_chain<T, N, TS, NS * R, TN, I + 1, Tail, decltype(d_ld), MID, ST, H, Rest...>(d_ld, mid, st, hook, A,
-                                                                                               B, tw, tw2, lt);
-    }
-}
-
-template <typename T, int N, int TS, int... Rs, class LD, class MID, class ST, class H>
-__device__ __forceinline__ void ct_conv_pp(const LD& ld, const MID& mid, const ST& st, const H& hook, cpx<T>* A,
-                                           cpx<T>* B, const cpx<T>* __restrict__ tw,
-                                           const cpx<T>* __restrict__ tw2, const int lt)
-{
-    static_assert(sizeof...(Rs) >= 2, "two or more passes");
-    const int lta = lt < TS ? lt : N;
-    using Tail    = typename rev_init<radix_seq<>, Rs...>::type;
-    pp_conv_chain<T, N, TS, 1, 0, 0, Tail, LD, MID, ST, H, Rs...>(ld, mid, st, hook, A, B, tw, tw2, lta);
-}
 
 // In-place compile-time block FFT with the signal in registers between the passes (EPT values per thread)
 // and its loads and stores given as functors: the first pass reads ld(p), the passes exchange through the

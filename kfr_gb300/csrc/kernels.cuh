@@ -88,14 +88,6 @@ struct ct_fft
         const auto nothing = []() {};
         ct_block_fft_pp<T, N, TS, Rs...>(ld, st, nothing, nothing, A, B, tw, lt, post);
     }
-    // forward DFT, mid(q, x), forward DFT with the radices reversed (twiddles tw2) in 2 npass - 1 passes
-    template <class LD, class MID, class ST, class H>
-    __device__ __forceinline__ void run_conv_pp(const LD& ld, const MID& mid, const ST& st, const H& hook, cpx<T>* A,
-                                                cpx<T>* B, const cpx<T>* __restrict__ tw,
-                                                const cpx<T>* __restrict__ tw2, int lt) const
-    {
-        ct_conv_pp<T, N, TS, Rs...>(ld, mid, st, hook, A, B, tw, tw2, lt);
-    }
 };
 
 __device__ __forceinline__ uint32_t div_by(uint32_t x, const fast_div f) { return fdiv(x, f); }
@@ -493,160 +485,6 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_rader(const rader_args a,
     }
 }
 
-// ---------------------------------------------------------------------------------------------------
-// Rader over tiles of `spc` whole signals, persistent and pipelined (compile-time L).  A tile's bytes are
-// contiguous: one bulk copy (TMA) brings the enclosing 16-byte-aligned range into a tile buffer and the
-// tile's output leaves the same way.  Per signal, in 2K - 1 ping-pong passes (K radices, one barrier each):
-//   first DFT:   pass 1 gathers a[p] = x[g^p] straight from the staged input;
-//   middle:      the first DFT's last pass and the second DFT's first pass run in registers, with
-//                A[q] -> conj(A[q] * bhat[q]) between them (A[0] = sum of x[1..n-1] is kept);
-//   second DFT:  radices reversed; its last pass scatters X[g^-q] = x[0] + conj(C[q]) into the output
-//                tile in the input's layout (g^-q = gp[L - q]);
-//   X[0] = x[0] + A[0].
-// Three tile buffers rotate: the input tile (then the passes' A buffer), the scratch tile (the passes' B
-// buffer, then the output in natural layout, read by the bulk store) and the spare tile, into which the
-// next tile is loaded as soon as the first pass is done, once the bulk store that last read it (the
-// previous tile's output) has finished reading.  The next tile's input is this one's spare; its scratch
-// is this one's input buffer.
-// ---------------------------------------------------------------------------------------------------
-template <typename T, class F>
-__host__ __device__ constexpr int rader_stage_elems(int spc)
-{
-    return pipe_stage_len(spc, F::n + 1, F::gstride(F::n));
-}
-
-template <typename T, class F>
-__global__ void __launch_bounds__(F::max_threads, 1)
-    k_rader_tile(const rader_args a, const long long ntiles, const int spc, int* err)
-{
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    constexpr int L      = F::n;
-    constexpr int N      = L + 1;
-    constexpr int STRIDE = F::gstride(L);
-    constexpr int ESZ    = int(sizeof(cpx<T>));
-    const int stage_elems = rader_stage_elems<T, F>(spc);
-    cpx<T>* const tiles = reinterpret_cast<cpx<T>*>(smem_raw);
-    cpx<T>* x0s         = tiles + 3 * stage_elems;
-    cpx<T>* dcs         = x0s + spc;
-    uint64_t* bars      = reinterpret_cast<uint64_t*>(dcs + spc);
-    const F fft(nullptr, a.d, F::ts);
-    const long long tile_bytes      = (long long)spc * N * ESZ;
-    const char* inb                 = reinterpret_cast<const char*>(a.in);
-    char* outb                      = reinterpret_cast<char*>(a.out);
-    const cpx<T>* __restrict__ bhat = reinterpret_cast<const cpx<T>*>(a.bhat);
-    const cpx<T>* __restrict__ tw   = reinterpret_cast<const cpx<T>*>(a.tw);
-    const cpx<T>* __restrict__ tw2  = reinterpret_cast<const cpx<T>*>(a.tw2);
-    const int* __restrict__ gp      = a.gp;
-    const bool inv                  = a.inverse != 0;
-    const group_map gm(F::ts, spc);
-    if (threadIdx.x == 0)
-    {
-        for (int b = 0; b < 3; b++)
-            mbar_init(&bars[b], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    // Tile t holds signals [t spc, t spc + ns), ns = spc except for a shorter last tile.  Its bytes
-    // [s0, e) are loaded as the enclosing 16-byte-aligned range; for the last tile, whose range could
-    // reach past the batch, only the aligned part [s0 & ~15, e & ~15) goes by bulk copy and a final
-    // 8-byte element beyond it by a plain load (visible to the CTA after the barrier that follows the wait).
-    const auto tile_sigs = [&](long long tt) { return int(a.batch - tt * spc < spc ? a.batch - tt * spc : spc); };
-    const auto load_tile = [&](long long tt, cpx<T>* buf, uint64_t* bar)
-    {
-        const long long s0 = tt * tile_bytes, e = s0 + (long long)tile_sigs(tt) * N * ESZ;
-        const long long a0 = s0 & ~15LL, a1 = tt == ntiles - 1 ? (e & ~15LL) : ((e + 15) & ~15LL);
-        mbar_arrive_expect_tx(bar, uint32_t(a1 - a0));
-        bulk_g2s(buf, inb + a0, uint32_t(a1 - a0), bar);
-        if (a1 < e)
-            *reinterpret_cast<cpx<T>*>(reinterpret_cast<char*>(buf) + (e - ESZ - a0)) =
-                *reinterpret_cast<const cpx<T>*>(inb + e - ESZ);
-    };
-    long long t = blockIdx.x;
-    if (threadIdx.x == 0 && t < ntiles)
-        load_tile(t, tiles, &bars[0]);
-    uint32_t phase   = 0;                  // bit b: parity to wait for on tile buffer b
-    uint32_t pending = t < ntiles ? 1 : 0; // bit b: a copy into tile buffer b is in flight
-    int bi           = 0;                  // tile buffer holding the current input
-    for (; t < ntiles; t += gridDim.x)
-    {
-        const int bs   = bi == 2 ? 0 : bi + 1; // scratch, then output
-        const int bn   = bs == 2 ? 0 : bs + 1; // spare: receives the next tile
-        cpx<T>* in_t   = tiles + bi * stage_elems;
-        cpx<T>* scr_t  = tiles + bs * stage_elems;
-        cpx<T>* spare  = tiles + bn * stage_elems;
-        const bool got = mbar_wait(&bars[bi], (phase >> bi) & 1, a.wait_spins);
-        if (!__syncthreads_and(got))
-        {
-            if (threadIdx.x == 0)
-            {
-                atomicExch(err, 1);
-                // give every copy in flight (the one waited for included) a bounded chance to land before
-                // the CTA exits
-                for (int b = 0; b < 3; b++)
-                    if ((pending >> b) & 1)
-                        mbar_wait(&bars[b], (phase >> b) & 1);
-                bulk_wait_all();
-            }
-            return;
-        }
-        phase ^= 1u << bi;
-        pending &= ~(1u << bi);
-        const long long s0 = t * tile_bytes;
-        const long long a0 = s0 & ~15LL;
-        const int off      = int((s0 - a0) / ESZ);
-        const cpx<T>* sig  = in_t + off + gm.g * N;  // this signal's input, in the input layout
-        cpx<T>* osig       = scr_t + off + gm.g * N; // this signal's output, in the same layout
-        if (gm.lt == 0)
-            x0s[gm.g] = conj_if(sig[0], inv);
-        const long long tn  = t + gridDim.x;
-        const auto prefetch = [&]()
-        {
-            if (tn < ntiles)
-            {
-                pending |= 1u << bn;
-                if (threadIdx.x == 0)
-                {
-                    // the spare buffer was last read by the previous tile's bulk store
-                    bulk_wait_read();
-                    fence_proxy_async_smem();
-                    load_tile(tn, spare, &bars[bn]);
-                }
-            }
-        };
-        fft.run_conv_pp([&](int p) { return conj_if(sig[__ldg(gp + p)], inv); },
-                        [&](int q, cpx<T> x)
-                        {
-                            if (q == 0)
-                                dcs[gm.g] = x;
-                            return conj(x * ldg(bhat + q));
-                        },
-                        [&](int q, cpx<T> x)
-                        { osig[__ldg(gp + (q == 0 ? 0 : L - q))] = conj_if(x0s[gm.g] + conj(x), inv); },
-                        prefetch, in_t + gm.g * STRIDE, scr_t + gm.g * STRIDE, tw, tw2, gm.lt);
-        if (gm.lt == 0)
-            osig[0] = conj_if(x0s[gm.g] + dcs[gm.g], inv);
-        fence_proxy_async_smem();
-        __syncthreads();
-        // the tile's output: its 16-byte-aligned interior by a bulk store, the (at most two) 8-byte edge
-        // elements by plain stores
-        const int ns       = tile_sigs(t);
-        const long long e1 = s0 + (long long)ns * N * ESZ;
-        const long long c0 = (s0 + 15) & ~15LL, c1 = e1 & ~15LL;
-        if (threadIdx.x == 0)
-        {
-            if (c1 > c0)
-                bulk_s2g(outb + c0, reinterpret_cast<const char*>(scr_t) + (c0 - a0), uint32_t(c1 - c0));
-            bulk_commit();
-        }
-        if (threadIdx.x == 32 % blockDim.x && c0 != s0)
-            *reinterpret_cast<cpx<T>*>(outb + s0) = scr_t[off];
-        if (threadIdx.x == 64 % blockDim.x && c1 != e1)
-            *reinterpret_cast<cpx<T>*>(outb + e1 - ESZ) = scr_t[off + ns * N - 1];
-        bi = bn;
-    }
-    if (threadIdx.x == 0)
-        bulk_wait_all();
-}
 
 // ---------------------------------------------------------------------------------------------------
 // Real forward DFT (dft_plan_real, CCs / Perm): c-point complex DFT of the reals viewed as c complex

@@ -169,20 +169,5 @@ cudaError_t launch_ct_dct_pipe_f32(const dct_args& a0, const block_cfg& c, long 
 #undef KFR_GPU_DCT_PIPE_CASE
 }
 
-cudaError_t launch_ct_rader_tile_f32(const rader_args& a0, const block_cfg& c, long long ntiles, int* err,
-                                     cudaStream_t st)
-{
-    rader_args a = a0;
-    a.wait_spins = wait_limit();
-#define KFR_GPU_RTILE_CASE(N, TS, ...)                                                                     \
-    case N:                                                                                                \
-        return go_persistent(k_rader_tile<float, ct_fft<float, N, TS, __VA_ARGS__>>, c, ntiles, st, a, ntiles, c.spc, err);
-    switch (c.ct)
-    {
-        KFR_CT_RADER_F32(KFR_GPU_RTILE_CASE)
-    default: return cudaErrorInvalidValue;
-    }
-#undef KFR_GPU_RTILE_CASE
-}
 
 } // namespace kfr_gpu

@@ -76,13 +76,10 @@ struct rader_args
     int inverse;
     const int* pin;   // pin[v] = p with g^p = v (mod n), v = 1..n-1
     const int* qof;   // qof[k] = q with g^-q = k (mod n), k = 1..n-1
-    const int* gp;    // gp[p] = g^p (mod n), p = 0..L-1 (pipelined kernel)
     const void* bhat; // L values: DFT_L(b) / L
     const void* tw;
-    const void* tw2;  // tiled kernel: twiddles of the radices in reverse order
     fast_div div_n, div_l;
     fft_desc d;
-    unsigned wait_spins = kDefaultWaitSpins; // persistent pipelined kernels: see kDefaultWaitSpins
 };
 
 // Rader's algorithm with prime-factor convolution DFTs (rader_pfa.cu): in and out 16-byte aligned, signals
@@ -244,11 +241,6 @@ cudaError_t launch_ct_dct_pipe_f32(const dct_args& a, const block_cfg& c, long l
 cudaError_t launch_ct_c2c_reg_f32(const c2c_args& a, const block_cfg& c, long long nsig, int* err, cudaStream_t st);
 cudaError_t launch_ct_bluestein_f32(const bluestein_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_rader_f32(const rader_args& a, const block_cfg& c, cudaStream_t st);
-// Persistent Rader over `ntiles` tiles of c.spc contiguous signals, each tile streamed in and out of shared
-// memory by bulk copies (in and out 16-byte aligned; the last tile's enclosing 16-byte range must lie
-// inside the batch; c.smem as rader_tile_smem).
-cudaError_t launch_ct_rader_tile_f32(const rader_args& a, const block_cfg& c, long long ntiles, int* err,
-                                     cudaStream_t st);
 cudaError_t launch_ct_r2c_f32(const real_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_c2r_f32(const real_args& a, const block_cfg& c, cudaStream_t st);
 cudaError_t launch_ct_dct2_f32(const dct_args& a, const block_cfg& c, cudaStream_t st);

@@ -659,7 +659,6 @@ void complex_engine<T>::init_rader(long long n)
         gpow[p] = int(v);
     pin_.upload(pin.data(), pin.size() * sizeof(int));
     qof_.upload(qof.data(), qof.size() * sizeof(int));
-    gp_.upload(gpow.data(), gpow.size() * sizeof(int));
     if (sizeof(T) == 4)
     {
         err_.alloc(sizeof(int));
@@ -667,13 +666,6 @@ void complex_engine<T>::init_rader(long long n)
     }
     bhat_.upload(bh.data(), bh.size() * sizeof(std::complex<T>));
     prog_.build(int(L), CT_RADER);
-    if (prog_.ct)
-    {
-        // the tiled kernel's second DFT runs the radices in reverse order
-        const std::vector<int> rev(prog_.radices.rbegin(), prog_.radices.rend());
-        const auto t2 = pass_twiddles<T>(rev, nullptr);
-        rtw2_.upload(t2.data(), t2.size() * sizeof(std::complex<T>));
-    }
     k_ = kind::rader_smem;
     // The prime-factor kernel (rader_pfa.cu) where one is compiled for n: its gather, scatter and
     // kernel-spectrum tables over the row-major array of the coprime axes r_i (L_i = L / r_i): position pos
@@ -718,30 +710,6 @@ void complex_engine<T>::init_rader(long long n)
         pfa_spc_  = pspc;
         pfa_axes_ = ax;
     }
-    // Signals per tile of the pipelined kernel: one signal when it takes half a CTA's threads or more,
-    // otherwise as many as leave room for two CTAs per SM (each holding two stage tiles and a work tile).
-    rader_spc_ = 0;
-    if (prog_.ct && sizeof(T) == 4)
-    {
-        int spc = 1;
-        if (prog_.ts < 512)
-        {
-            spc = 1024 / prog_.ts;
-            while (spc > 1 && rader_tile_smem(spc) > smem_budget() / 2)
-                spc--;
-        }
-        if (rader_tile_smem(spc) <= smem_budget())
-            rader_spc_ = spc;
-    }
-}
-
-template <typename T>
-int complex_engine<T>::rader_tile_smem(int spc) const
-{
-    // three rotating tile buffers, x[0] and A[0] per signal, three mbarriers
-    const int esz   = int(2 * sizeof(T));
-    const int stage = pipe_stage_len(spc, int(n_), prog_.gstride);
-    return (3 * stage + 2 * spc) * esz + 24;
 }
 
 template <typename T>
@@ -1169,31 +1137,13 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.inverse = inverse;
         a.pin     = static_cast<const int*>(pin_.get());
         a.qof     = static_cast<const int*>(qof_.get());
-        a.gp      = static_cast<const int*>(gp_.get());
         a.bhat    = bhat_.get();
         a.tw      = prog_.tw.get();
-        a.tw2     = rtw2_.get();
         a.div_n   = make_fast_div(uint32_t(n_));
         a.div_l   = make_fast_div(uint32_t(n_ - 1));
         a.d       = prog_.desc;
-        long long done = 0;
-        // Persistent tiled kernel over all signals (the last tile may be shorter and ends exactly at the
-        // batch's end); the plain kernel when the layout does not allow it.
-        if (rader_spc_ && err_.get() && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 &&
-            (reinterpret_cast<uintptr_t>(out) % 16) == 0)
-        {
-            const long long ntiles = (batch + rader_spc_ - 1) / rader_spc_;
-            block_cfg pc           = prog_.cfg_tile(rader_spc_);
-            pc.smem                = rader_tile_smem(rader_spc_);
-            check(launch_ct_rader_tile_f32(a, pc, ntiles, static_cast<int*>(err_.get()), st), "launch rader (tiled)");
-            done = batch;
-        }
-        if (done == batch)
-            return;
-        a.in    = static_cast<const char*>(in) + done * n_ * esz;
-        a.out   = static_cast<char*>(out) + done * n_ * esz;
-        a.batch = batch - done;
-        block_cfg c = prog_.cfg(batch - done);
+        // the per-tile kernel where the prime-factor kernel cannot run (misaligned or strided signals, c64)
+        block_cfg c = prog_.cfg(batch);
         c.smem += 2 * c.spc * int(esz);
         check(launch_rader<T>(a, c, st), "launch rader");
         return;
@@ -1345,8 +1295,6 @@ std::string complex_engine<T>::describe() const
             break;
         }
         s << "rader n=" << n_ << " [" << prog_.describe() << "]";
-        if (rader_spc_)
-            s << " tiled spc=" << rader_spc_;
         break;
     }
     return s.str();

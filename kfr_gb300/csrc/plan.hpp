@@ -195,14 +195,12 @@ private:
     int tc_mode_ = 0;
     dbuf tc_cs_, tc_tw1_, tc_tw2_;
     // Rader
-    dbuf pin_, qof_, gp_, rtw2_;
-    int rader_spc_ = 0; // signals per tile of the pipelined kernel, 0 = not used
+    dbuf pin_, qof_;
     // Rader with prime-factor convolution DFTs (rader_pfa.cu): signals per tile (0 = not used), its axes and
     // its gather / scatter / kernel-spectrum tables
     int pfa_spc_ = 0;
     std::vector<int> pfa_axes_;
     dbuf tin_, tout_, bphys_;
-    int rader_tile_smem(int spc) const;
 };
 
 // dft_plan_real<T>: N even, N/2-point complex engine plus the CCs/Perm split / merge.

@@ -1,7 +1,7 @@
 // Rader's algorithm with prime-factor (Good-Thomas) convolution DFTs, for primes N whose L = N - 1 splits
 // into pairwise coprime compile-time radices (8191: 8190 = 13 * 5 * 9 * 14; 127: 126 = 14 * 9).
 //
-// Rader (as in the tiled kernel): a[p] = x[g^p] (p < L), A = DFT_L(a), A'[k] = conj(A[k] bhat[k]) with
+// Rader (as in the per-signal kernel k_rader): a[p] = x[g^p] (p < L), A = DFT_L(a), A'[k] = conj(A[k] bhat[k]) with
 // bhat = DFT_L(b) / L, b[m] = W_N^{g^-m}; C = DFT_L(A'); X[g^-q] = x[0] + conj(C[q]); X[0] = x[0] + A[0].
 //
 // Prime-factor form of the two L-point DFTs (Good 1958, Thomas 1963): with L = r_0 r_1 ... r_{d-1} pairwise
@@ -26,7 +26,7 @@
 // the multiplication by bphys; the second DFT's axis-0 pass reads into registers, a barrier, then scatters X
 // in natural order into the buffer, which one bulk copy stores (the tile's edge elements beyond the 16-byte
 // interior by plain stores).  Measured on 256 MiB batches (N=8191: 640 threads, one CTA per SM; N=127: 24
-// signals per tile, four CTAs per SM), two buffers beat one by 16% to 20%, and the tiled ping-pong kernel
+// signals per tile, four CTAs per SM), two buffers beat one by 16% to 20%, and an earlier tiled ping-pong kernel
 // (three buffers, twiddled passes) by 12% (8191) and 22% (127).
 #include "kernels.cuh"
 

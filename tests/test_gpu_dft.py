@@ -110,7 +110,7 @@ def test_rader_tiles_many_per_cta(orc, n, batch):
     refi = orc.dft(x[pick].astype(np.complex128), inverse=True, threads=8)
     plan = k.dft_plan(n, "f32")
     d = plan.describe()
-    assert "tiled" in d or "prime-factor" in d, d  # a persistent kernel over tiles of signals
+    assert "prime-factor" in d, d  # the persistent kernel over tiles of signals
     xd = dev(x)
     yd = torch.empty_like(xd)
     plan.execute_batch(yd, xd, batch)

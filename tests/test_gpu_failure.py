@@ -30,7 +30,7 @@ def restore_limit():
 
 @pytest.mark.parametrize("n,batch", [(4096, 600), (8192, 300), (8191, 300), (65536, 40), (127, 5000)])
 def test_copy_wait_that_runs_out_is_reported_and_plan_recovers(restore_limit, orc, n, batch):
-    """k_c2c_pipe (4096), k_c2c_reg (8192), k_rader_tile (8191, 127) and the tensor-copy four-step passes
+    """k_c2c_pipe (4096), k_c2c_reg (8192), k_rader_pfa (8191, 127) and the tensor-copy four-step passes
     (65536 = 256 x 256)."""
     plan = k.dft_plan(n)
     g = torch.Generator(device="cuda").manual_seed(n)
