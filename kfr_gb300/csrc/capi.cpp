@@ -415,6 +415,21 @@ bool is_device_ptr(const void* p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Page-locked host memory mapped into the device's address space (cudaHostAlloc / cudaHostRegister): its
+// device-side address, or nullptr for any other pointer.
+void* host_mapped(const void* p)
+{
+    if (!p)
+        return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 bool overlap(const void* a, size_t an, const void* b, size_t bn)
 {
     const char* x = static_cast<const char*>(a);
@@ -530,6 +545,52 @@ void* create_dft(size_t n)
     return static_cast<plan_base*>(new dft_obj<T>(n));
 }
 
+// Synchronous call of a one-dimensional complex plan with page-locked host input and output: the kernels
+// read the input and write the output across the host link themselves (zero-copy), so the link's two
+// directions stay busy for the whole call with no staging, no chunk pipeline to fill and drain, and no
+// device copy of the data.  Taken for the one-CTA lengths up to 4096 points, whose plain-load kernels hold
+// many signals per CTA and keep the link busy (measured 256 -> 318 GB/s in + out at N=1000, 234 -> 273 at
+// 2187, 238 -> 285 at 127); longer lengths (the one-signal-per-CTA kernels, Rader at 8191, the four-step's
+// strided column reads) ran slower zero-copy than through the chunk pipeline and keep it.  False (nothing
+// done) when the call does not qualify.
+template <typename T>
+bool run_zero_copy(dft_obj<T>& p, void* out, const void* in, size_t batch, uint8_t* temp, bool inverse, void* stream)
+{
+    using kind = typename complex_engine<T>::kind;
+    if (stream || !p.eng1 || p.n < 2 || p.n > 4096)
+        return false;
+    const kind k = p.eng1->strategy();
+    if (k != kind::smem && k != kind::rader_smem && k != kind::bluestein_smem)
+        return false;
+    void* dout      = host_mapped(out);
+    const void* din = dout ? host_mapped(in) : nullptr;
+    if (!dout || !din)
+        return false;
+    std::unique_lock<std::mutex> lock(p.mu);
+    const size_t scr_bytes = size_t(p.scratch_elems((long long)batch)) * 2 * sizeof(T);
+    void* scr              = nullptr;
+    if (scr_bytes)
+    {
+        if (temp && is_device_ptr(temp))
+            scr = temp;
+        else
+        {
+            p.scratch.ensure(scr_bytes);
+            scr = p.scratch.get();
+        }
+    }
+    struct host_io_scope
+    {
+        const complex_engine<T>& e;
+        explicit host_io_scope(const complex_engine<T>& x) : e(x) { e.set_host_io(true); }
+        ~host_io_scope() { e.set_host_io(false); }
+    } scope(*p.eng1);
+    p.eng1->execute(dout, din, (long long)batch, (long long)p.n, (long long)p.n, inverse, scr, nullptr);
+    check(cudaGetLastError(), "kernel launch");
+    check(cudaStreamSynchronize(nullptr), "execute");
+    return true;
+}
+
 template <typename T>
 void exec_dft(void* h, size_t batch, void* out, const void* in, uint8_t* temp, bool inverse, void* stream)
 {
@@ -539,6 +600,11 @@ void exec_dft(void* h, size_t batch, void* out, const void* in, uint8_t* temp, b
     const size_t per   = p->n * 2 * sizeof(T);
     const size_t bytes = batch * per;
     const size_t scr   = size_t(p->scratch_elems((long long)batch)) * 2 * sizeof(T);
+    if (run_zero_copy(*p, out, in, batch, temp, inverse, stream))
+    {
+        p->check_device_error();
+        return;
+    }
     if (!run_chunked(
             *p, out, per, in, per, batch, stream,
             [&](long long nb) { return size_t(p->scratch_elems(nb)) * 2 * sizeof(T); },

@@ -1063,14 +1063,14 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         a.div_n   = make_fast_div(uint32_t(n_));
         a.d       = prog_.desc;
         long long done = 0;
-        if (reg_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
+        if (reg_ && !host_io_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
         {
             block_cfg rc = prog_.cfg_tile(1);
             rc.smem      = ((prog_.gstride + 1) / 2 * 2 + int(n_ / 2)) * int(esz) + 16;
             check(launch_ct_c2c_reg_f32(a, rc, batch, static_cast<int*>(err_.get()), st), "launch c2c (one per CTA)");
             done = batch;
         }
-        if (pipe_spc_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
+        if (pipe_spc_ && !host_io_ && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0)
         {
             const long long ntiles = batch / pipe_spc_;
             if (ntiles > 0)
@@ -1111,7 +1111,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
     }
     case kind::rader_smem:
     {
-        if (pfa_spc_ && err_.get() && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 &&
+        if (pfa_spc_ && !host_io_ && err_.get() && istride == n_ && ostride == n_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 &&
             (reinterpret_cast<uintptr_t>(out) % 16) == 0)
         {
             // the prime-factor kernel takes every signal (its last tile may be shorter)
@@ -1168,7 +1168,9 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
             char* outb          = static_cast<char*>(out) + b0 * n_ * esz;
             char* scr           = static_cast<char*>(scratch) + b0 * n_ * esz;
             fourstep_args a;
-            a.err        = pair_ ? static_cast<int*>(err_.get()) : nullptr;
+            // the tensor-copy pair kernels run only with an error flag: host-mapped buffers take the plain-load
+            // pair kernels
+            a.err        = pair_ && !host_io_ ? static_cast<int*>(err_.get()) : nullptr;
             a.batch      = nb;
             a.sig_stride = n_;
             a.n1         = int(n1_);

@@ -165,10 +165,15 @@ public:
     int launches(long long batch) const;
     // Throws if a kernel of this engine recorded a device-side error (a bounded wait that ran out).
     void check_device_error() const;
+    // While set, in and out of execute() are host memory mapped into the device's address space (zero-copy
+    // calls): the kernels that read or write through bulk and tensor copies give way to the plain-load ones.
+    // The caller holds the plan's lock around the call.
+    void set_host_io(bool on) const { host_io_ = on; }
 
 private:
     long long n_;
     kind k_ = kind::trivial;
+    mutable bool host_io_ = false;
     block_program<T> prog_; // smem: length n; bluestein_smem: length m
     // Bluestein
     long long m_ = 0;

@@ -194,6 +194,38 @@ def test_fourstep_pair_tiles_many_per_cta(orc, n, batch):
     assert rel_rms(got, full.cpu().numpy()) <= tol(n, "f32")
 
 
+@pytest.mark.parametrize("n,batch", [(1000, 3000), (4096, 700), (127, 9000), (2187, 400), (1021, 300), (1536, 1),
+                                     (8191, 300), (30720, 70), (16384, 90)])
+def test_page_locked_host_buffers(orc, n, batch):
+    """Page-locked host input and output (torch pin_memory): one-CTA lengths up to 4096 points (pipelined,
+    Rader, Bluestein) are read and written by the kernels across the host link with plain loads and stores
+    (zero-copy), longer ones go through the chunk pipeline; forward and inverse against the device call's
+    results, the oracle on a few signals, and in place."""
+    rng = np.random.default_rng(n + batch)
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    plan = k.dft_plan(n, "f32")
+    xd = dev(x)
+    hx = torch.from_numpy(x).pin_memory()
+    for inverse in (False, True):
+        yd = torch.empty_like(xd)
+        plan.execute_batch(yd, xd, batch, inverse=inverse)
+        hy = torch.empty_like(hx).pin_memory()
+        plan.execute_batch(hy, hx, batch, inverse=inverse)
+        assert rel_rms(hy.numpy(), yd.cpu().numpy()) <= tol(n, "f32") / 4, inverse
+    pick = np.unique(np.r_[0, batch // 2, batch - 1])
+    ref = orc.dft(x[pick].astype(np.complex128), threads=8)
+    assert rel_rms(plan_forward(plan, hx, batch)[pick], ref) <= tol(n, "f32")
+    hz = hx.clone().pin_memory()
+    plan.execute_batch(hz, hz, batch)
+    assert rel_rms(hz.numpy()[pick], ref) <= tol(n, "f32")
+
+
+def plan_forward(plan, hx, batch):
+    hy = torch.empty_like(hx).pin_memory()
+    plan.execute_batch(hy, hx, batch)
+    return hy.numpy()
+
+
 @pytest.mark.parametrize("n,batch", [(1000, 5000), (8191, 700), (4096, 1100)])
 def test_host_buffers_pipelined_match_device(n, batch):
     """Host input and output (the reference's calling convention) split into chunks that overlap copies with
