@@ -31,7 +31,7 @@ CU_SOURCES = [
     "kernels_f32.cu", "kernels_f64.cu", "kernels_ct_a.cu", "kernels_ct_b.cu", "kernels_ct_c.cu", "elementwise.cu",
     "conv.cu", "convolve.cu", "adjoint.cu", "uneven.cu", "tensor.cu", "static_scratch.cu", "rader_pfa.cu",
 ]
-CPP_SOURCES = ["plan.cpp", "md.cpp", "capi.cpp"]
+CPP_SOURCES = ["plan.cpp", "md.cpp", "capi.cpp", "launch_cache.cpp"]
 
 
 def _headers():

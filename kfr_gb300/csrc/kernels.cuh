@@ -1619,7 +1619,7 @@ static cudaError_t go(K kernel, dim3 grid, const block_cfg& c, cudaStream_t st, 
 {
     if (c.smem > 48 * 1024)
     {
-        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem);
+        const cudaError_t e = prepare_launch(reinterpret_cast<const void*>(kernel), c.threads, c.smem);
         if (e != cudaSuccess)
             return e;
     }

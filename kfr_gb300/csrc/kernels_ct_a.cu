@@ -51,32 +51,18 @@ cudaError_t launch_ct_rader_f32(const rader_args& a, const block_cfg& c, cudaStr
 #undef CT_ARGS
 }
 
-static int sm_count()
-{
-    static int n = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
-            v = 152;
-        return v;
-    }();
-    return n;
-}
-
 // Persistent launch: as many CTAs as fit on the device at once, capped by the number of tiles.
 template <typename K, typename... Args>
 static cudaError_t go_persistent(K kernel, const block_cfg& c, long long ntiles, cudaStream_t st, Args... args)
 {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem);
+    int per_sm    = 0;
+    cudaError_t e = prepare_launch(reinterpret_cast<const void*>(kernel), c.threads, c.smem, &per_sm);
     if (e != cudaSuccess)
         return e;
-    int per_sm = 0;
-    e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, c.threads, c.smem);
-    if (e != cudaSuccess)
-        return e;
-    if (per_sm < 1)
+    const int sms = device_sm_count();
+    if (per_sm < 1 || sms < 1)
         return cudaErrorInvalidConfiguration;
-    const long long grid = std::min<long long>(ntiles, (long long)per_sm * sm_count());
+    const long long grid = std::min<long long>(ntiles, (long long)per_sm * sms);
     kernel<<<unsigned(grid), c.threads, c.smem, st>>>(args...);
     return cudaGetLastError();
 }

@@ -63,7 +63,7 @@ bool has_ct_fsp_f32(int n1, int n2)
 template <class K>
 static cudaError_t go_fsp(K kernel, dim3 grid, int threads, int smem, cudaStream_t st, const fourstep_args& a)
 {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const cudaError_t e = prepare_launch(reinterpret_cast<const void*>(kernel), threads, smem);
     if (e != cudaSuccess)
         return e;
     kernel<<<grid, threads, smem, st>>>(a);
@@ -115,16 +115,12 @@ static bool map_rows(tensor_map& m, const void* base, long long row_elems, long 
 template <class K, class... Args>
 static cudaError_t go_fspt(K kernel, int threads, int smem, long long ntiles, cudaStream_t st, Args... args)
 {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int per_sm    = 0;
+    cudaError_t e = prepare_launch(reinterpret_cast<const void*>(kernel), threads, smem, &per_sm);
     if (e != cudaSuccess)
         return e;
-    int per_sm = 0, dev = 0, sms = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem)) != cudaSuccess)
-        return e;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
-        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-        return e;
-    if (per_sm < 1)
+    const int sms = device_sm_count();
+    if (per_sm < 1 || sms < 1)
         return cudaErrorInvalidConfiguration;
     const long long grid = std::min<long long>(ntiles, (long long)per_sm * sms);
     kernel<<<unsigned(grid), threads, smem, st>>>(args...);

@@ -253,6 +253,14 @@ bool has_ct_fsp_f32(int n1, int n2);
 cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st);
 cudaError_t launch_ct_fs_rows_f32(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
 
+// Launch bookkeeping done once per process instead of on every launch (launch_cache.cpp): the kernel's
+// dynamic shared-memory limit is raised to at least `smem` the first time it is needed, and *per_sm (if
+// given) receives how many blocks of `threads` threads and `smem` bytes of dynamic shared memory fit one SM.
+// Keyed by device, kernel, threads and smem.
+cudaError_t prepare_launch(const void* kernel, int threads, int smem, int* per_sm = nullptr);
+// SMs of the current device (0 if the query fails), queried once per device.
+int device_sm_count();
+
 // Largest thread count a block FFT kernel may be launched with (elem_bytes = sizeof(real type)).
 int max_threads_for(int elem_bytes, int ept);
 // Largest dynamic shared memory a kernel may use on this device.

@@ -302,16 +302,12 @@ constexpr int pfa_smem()
 template <class K>
 cudaError_t go_pfa(K kernel, int threads, int smem, long long ntiles, const rader_pfa_args& a, cudaStream_t st)
 {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int per_sm    = 0;
+    cudaError_t e = prepare_launch(reinterpret_cast<const void*>(kernel), threads, smem, &per_sm);
     if (e != cudaSuccess)
         return e;
-    int per_sm = 0, dev = 0, sms = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem)) != cudaSuccess)
-        return e;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
-        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-        return e;
-    if (per_sm < 1)
+    const int sms = device_sm_count();
+    if (per_sm < 1 || sms < 1)
         return cudaErrorInvalidConfiguration;
     const long long grid = std::min<long long>(ntiles, (long long)per_sm * sms);
     kernel<<<unsigned(grid), threads, smem, st>>>(a, ntiles);

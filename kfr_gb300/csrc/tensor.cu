@@ -345,7 +345,7 @@ constexpr int tc_tile(int L) { return L == 256 ? 16 : 2; }
 template <class K>
 cudaError_t go_tc(K kernel, dim3 grid, int smem, cudaStream_t st, const tc_fs_args& a)
 {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const cudaError_t e = prepare_launch(reinterpret_cast<const void*>(kernel), 512, smem);
     if (e != cudaSuccess)
         return e;
     kernel<<<grid, 512, smem, st>>>(a);
@@ -381,7 +381,7 @@ cudaError_t launch_c2c_tc_f32(const c2c_args& a, int n, int mode, const float* c
     const unsigned grid = unsigned((a.batch + spc - 1) / spc);
     auto go = [&](auto kernel) -> cudaError_t
     {
-        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        const cudaError_t e = prepare_launch(reinterpret_cast<const void*>(kernel), 512, smem);
         if (e != cudaSuccess)
             return e;
         kernel<<<grid, 512, smem, st>>>(a, cs, spc);

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kUnevenThreads, 1) k_uneven(const uneven_launc
 
 cudaError_t launch_uneven_f32(const uneven_launch& a, int smem, int grid, cudaStream_t st)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_uneven<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const cudaError_t e = prepare_launch(reinterpret_cast<const void*>(k_uneven<float>), kUnevenThreads, smem);
     if (e != cudaSuccess)
         return e;
     k_uneven<float><<<unsigned(grid), kUnevenThreads, smem, st>>>(a);
