@@ -450,6 +450,19 @@ def run_case(spec: str) -> int:
         torch.cuda.synchronize()
         print(json.dumps({"case": spec, "elements": int(sum(lengths)), "plan": up.describe()}))
         return 0
+    if parts[0] == "real":
+        # the forward real DFT (CCs) of `MiB` of f32 signals of length n
+        n = int(parts[1])
+        mib = int(parts[2]) if len(parts) > 2 else 128
+        b = max(1, (mib << 20) // (4 * n))
+        plan = k.dft_plan_real(n)
+        x = torch.randn(b, n, device="cuda")
+        y = torch.empty(b, n // 2 + 1, dtype=torch.complex64, device="cuda")
+        for _ in range(3):
+            plan.execute_batch(y, x, b)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": spec, "batch": b}))
+        return 0
     form, n = parts[0], int(parts[1])
     mib = int(parts[2]) if len(parts) > 2 else 128
     b = max(1, (mib << 20) // (8 * n))
@@ -483,8 +496,8 @@ def main():
     ap.add_argument("--sizes", type=str, default=None, help="comma-separated subset of the lengths (profiling)")
     ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
     ap.add_argument("--case", type=str, default=None,
-                    help="profiling: run one plan `form:n[:MiB]` three times and exit (form: plain, fp16, bf16; "
-                         "or uneven:count[:fixed], fixed = no autotuning)")
+                    help="profiling: run one plan `form:n[:MiB]` three times and exit (form: plain, fp16, bf16, "
+                         "real; or uneven:count[:fixed], fixed = no autotuning)")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case)

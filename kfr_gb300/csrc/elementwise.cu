@@ -131,6 +131,75 @@ cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// Real-DFT split / merge over mirror pairs: thread e of a signal (e = 0 .. c/2) reads Z[e] and Z[c - e] (or
+// X[e] and X[c - e]) once and writes both outputs; e == c - e (c even) writes one.  grid.y walks the signals.
+template <typename T, bool INV>
+__global__ void __launch_bounds__(256) k_real_pairs(const ew_args a)
+{
+    const long long c = a.n_src;
+    const cpx<T>* t0  = reinterpret_cast<const cpx<T>*>(a.t0);
+    const bool ccs    = a.flag != 0;
+    for (long long s = blockIdx.y; s < a.batch; s += gridDim.y)
+    {
+        const cpx<T>* in = reinterpret_cast<const cpx<T>*>(a.in) + s * a.istride;
+        cpx<T>* out      = reinterpret_cast<cpx<T>*>(a.out) + s * a.ostride;
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e <= c / 2;
+             e += (long long)gridDim.x * blockDim.x)
+        {
+            if (e == 0)
+            {
+                const cpx<T> z0 = in[0];
+                if constexpr (!INV)
+                {
+                    out[0] = ccs ? mk<T>(z0.x + z0.y, 0) : mk<T>(z0.x + z0.y, z0.x - z0.y);
+                    if (ccs)
+                        out[c] = mk<T>(z0.x - z0.y, 0);
+                }
+                else
+                {
+                    const T xn = ccs ? in[c].x : z0.y;
+                    out[0]     = mk<T>(z0.x + xn, z0.x - xn);
+                }
+                continue;
+            }
+            const long long m = c - e;
+            const cpx<T> u    = in[e];
+            const cpx<T> v    = in[m];
+            if constexpr (!INV)
+            {
+                // X[k] = (Z[k] + conj Z[c-k]) / 2 - i W_2c^k (Z[k] - conj Z[c-k]) / 2
+                out[e] = scale(u + conj(v), T(0.5)) + ldg(t0 + e) * scale(mul_mi(u - conj(v)), T(0.5));
+                if (m != e)
+                    out[m] = scale(v + conj(u), T(0.5)) + ldg(t0 + m) * scale(mul_mi(v - conj(u)), T(0.5));
+            }
+            else
+            {
+                // Z[k] = (X[k] + conj X[c-k]) + i conj(W_2c^k) (X[k] - conj X[c-k])
+                out[e] = (u + conj(v)) + mul_pi(conj(ldg(t0 + e)) * (u - conj(v)));
+                if (m != e)
+                    out[m] = (v + conj(u)) + mul_pi(conj(ldg(t0 + m)) * (v - conj(u)));
+            }
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_real_pairs(const ew_args& a, bool inverse, cudaStream_t st)
+{
+    const long long pairs = a.n_src / 2 + 1;
+    if (a.batch <= 0 || a.n_src < 1)
+        return cudaSuccess;
+    const unsigned bx = unsigned(std::min<long long>((pairs + 255) / 256, 1024));
+    const unsigned by = unsigned(std::min<long long>(a.batch, std::max<long long>(1, 152LL * 16 / bx)));
+    if (inverse)
+        k_real_pairs<T, true><<<dim3(bx, by), 256, 0, st>>>(a);
+    else
+        k_real_pairs<T, false><<<dim3(bx, by), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_real_pairs<float>(const ew_args&, bool, cudaStream_t);
+template cudaError_t launch_real_pairs<double>(const ew_args&, bool, cudaStream_t);
+
 // Spectral product of include/kfr/dft/fft.hpp:983-1020 over a batch: one thread per element, grid-stride.
 // The Perm format stores the DC and Nyquist bins, both real, as the real and imaginary parts of element 0, so
 // that element is multiplied part by part instead of as a complex number.

@@ -510,7 +510,13 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_r2c(const real_args a, co
         const int e = i - s * c;
         const long long sig = s0 + s;
         if (sig < a.batch)
-            sm[s * stride + F::pi(e)] = reinterpret_cast<const cpx<T>*>(inr + sig * a.istride)[e];
+        {
+            const T* xr = inr + sig * a.istride + 2 * e;
+            // reals at an odd element offset (a pointer aligned to one real only) load one by one
+            sm[s * stride + F::pi(e)] = (reinterpret_cast<uintptr_t>(xr) % sizeof(cpx<T>)) == 0
+                                            ? *reinterpret_cast<const cpx<T>*>(xr)
+                                            : mk<T>(xr[0], xr[1]);
+        }
     }
     __syncthreads();
     const group_map gm(ts, spc);
@@ -737,7 +743,18 @@ __global__ void __launch_bounds__(F::max_threads, 1) k_c2r(const real_args a, co
         const int e = i - s * c;
         const long long sig = s0 + s;
         if (sig < a.batch)
-            reinterpret_cast<cpx<T>*>(outr + sig * a.ostride)[e] = conj(sm[s * stride + F::pi(e)]);
+        {
+            T* yr          = outr + sig * a.ostride + 2 * e;
+            const cpx<T> v = conj(sm[s * stride + F::pi(e)]);
+            // reals at an odd element offset store one by one
+            if ((reinterpret_cast<uintptr_t>(yr) % sizeof(cpx<T>)) == 0)
+                *reinterpret_cast<cpx<T>*>(yr) = v;
+            else
+            {
+                yr[0] = v.x;
+                yr[1] = v.y;
+            }
+        }
     }
 }
 
@@ -1411,18 +1428,30 @@ __device__ __forceinline__ void fspt_load(void* dst, const tensor_map* tm, int x
         tensor_g2s_2d(static_cast<char*>(dst) + b * BR * S * 8, tm, x, y0 + b * BR, bar);
 }
 
-template <typename T, class FA, int N2>
+// Position of column output k1 in the real-fused layout (RP): k1 and N1 - k1 side by side at 2j and 2j + 1
+// (j = min(k1, N1 - k1) >= 1), row 0 at 0, row N1/2 (N1 even) at 1; N1 odd leaves position 1 unused.
+template <int N1>
+__device__ __forceinline__ int rp_pos(int k1)
+{
+    return k1 == 0 ? 0 : (2 * k1 < N1 ? 2 * k1 : (2 * k1 == N1 ? 1 : 2 * (N1 - k1) + 1));
+}
+
+template <typename T, class FA, int N2, bool RP = false>
 __global__ void __launch_bounds__(fspt_threads<FA>(), fspt_min_ctas<FA>())
     k_fspt_cols(const fourstep_args a, const __grid_constant__ tensor_map tm_in, const long long ntiles, int* err)
 {
     static_assert(fspt_ok<FA>(), "two or three passes on tiles of 16 to 2 columns");
     constexpr int N1 = FA::n, GA = FA::gstride(), TS = FA::ts, S = fspt_tile<FA>();
+    // RP: the real-fused layout, columns P1 apart (N1 rounded up to even) with outputs at rp_pos(k1)
+    constexpr int P1 = RP ? N1 + (N1 & 1) : N1;
+    const auto pos   = [](int k1) { return RP ? rp_pos<N1>(k1) : k1; };
     constexpr int NTC = (N2 + S - 1) / S;
     constexpr int SE  = fspt_stage_elems<FA>(S);
     constexpr int LB  = lbits_for<N1 * N2>();
     constexpr int NSL = N1 / FA::rlast; // last pass: butterfly j makes outputs j + r NSL
     constexpr bool three = FA::npass == 3;
-    static_assert(three || (N1 * 8) % 16 == 0, "whole columns are bulk-copied");
+    static_assert(three || (P1 * 8) % 16 == 0, "whole columns are bulk-copied");
+    static_assert(three || S * P1 <= SE, "the tile's output columns fit the stage");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T>* st0    = reinterpret_cast<cpx<T>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     cpx<T>* B      = st0 + 2 * SE;
@@ -1473,7 +1502,7 @@ __global__ void __launch_bounds__(fspt_threads<FA>(), fspt_min_ctas<FA>())
         const long long b = t / NTC;
         const int c0      = int(t % NTC) * S;
         const int col     = c0 + g;
-        cpx<T>* y         = reinterpret_cast<cpx<T>*>(a.out) + b * (long long)N1 * N2;
+        cpx<T>* y         = reinterpret_cast<cpx<T>*>(a.out) + b * (long long)P1 * N2;
         // four-step twiddle W_N^{col k1} on the last pass's outputs k1 = j + r NSL: W_N^{col j} times powers
         // of the tile's step W_N^{col NSL}
         const cpx<T> step = twiddle_2level(twA, twB, (long long)(col * NSL), LB);
@@ -1493,21 +1522,21 @@ __global__ void __launch_bounds__(fspt_threads<FA>(), fspt_min_ctas<FA>())
                            [&](int k1, cpx<T> v)
                            {
                                if (N2 % S == 0 || col < N2)
-                                   y[(long long)col * N1 + k1] = conj_if(v, cout);
+                                   y[(long long)col * P1 + pos(k1)] = conj_if(v, cout);
                            },
                            stage + g * GA, B + g * GA, tw, lt);
         }
         else
         {
             // pass 1 reads the box; pass 2 writes the tile's S output columns (contiguous in y) over it
-            fa.run_pp_post(ld, post, [&](int k1, cpx<T> v) { stage[g * N1 + k1] = conj_if(v, cout); }, stage,
+            fa.run_pp_post(ld, post, [&](int k1, cpx<T> v) { stage[g * P1 + pos(k1)] = conj_if(v, cout); }, stage,
                            B + g * GA, tw, lt);
             fence_proxy_async_smem();
             __syncthreads();
             if (threadIdx.x == 0)
             {
                 const int ncols = N2 % S == 0 ? S : (N2 - c0 < S ? N2 - c0 : S);
-                bulk_s2g(y + (long long)c0 * N1, stage, uint32_t(ncols * N1 * 8));
+                bulk_s2g(y + (long long)c0 * P1, stage, uint32_t(ncols * P1 * 8));
                 bulk_commit();
             }
         }
@@ -1607,6 +1636,133 @@ __global__ void __launch_bounds__(fspt_threads<FB>(), fspt_min_ctas<FB>())
     }
     if (threadIdx.x == 0)
         bulk_wait_all();
+}
+
+// The row pass of a real forward DFT on the real-fused column layout (k_fspt_cols with RP): a tile is S
+// positions of the P1 per column, that is S/2 mirror pairs of rows k1 and N1 - k1 (or rows 0 and N1/2), so
+// after the row FFTs Z[k] and Z[c - k] (c = N1 N2) of every output lie in the same tile and the split
+//   X[k] = (Z[k] + conj Z[c-k]) / 2 - i W_2c^k (Z[k] - conj Z[c-k]) / 2
+// writes the real spectrum directly: X[k] for row k1 at k2 and X[c - k] for row N1 - k1 at N2 - 1 - k2.
+// Two passes only (the row FFT writes back into the box, the split reads it).
+template <typename T, class FB, int N1>
+__global__ void __launch_bounds__(fspt_threads<FB>(), fspt_min_ctas<FB>())
+    k_fspt_rows_r2c(const fourstep_args a, const __grid_constant__ tensor_map tm_in, const long long ntiles, int* err)
+{
+    static_assert(fspt_ok<FB>() && FB::npass == 2, "two passes on tiles of 16 to 2 rows");
+    constexpr int N2 = FB::n, GB = FB::gstride(), TS = FB::ts, S = fspt_tile<FB>();
+    static_assert(S % 2 == 0, "whole mirror pairs per tile");
+    constexpr int P1  = N1 + (N1 & 1);
+    constexpr int NTR = (P1 + S - 1) / S;
+    constexpr int SE  = fspt_stage_elems<FB>(S);
+    constexpr int THREADS = fspt_threads<FB>();
+    constexpr long long C = (long long)N1 * N2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T>* st0    = reinterpret_cast<cpx<T>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    cpx<T>* B      = st0 + 2 * SE;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(B + S * GB);
+    const int g    = int(threadIdx.x) / TS;
+    const int lt   = int(threadIdx.x) - g * TS;
+    const cpx<T>* tw  = reinterpret_cast<const cpx<T>*>(a.tw);
+    // W_2c^k for k = k1 + N1 k2 as W_2c^k1 (rtw[k1]) times W_2c^(N1 k2) (rtw[N1 + k2]); W_2c^(c - k) is
+    // -conj(W_2c^k)
+    const cpx<T>* rtw = reinterpret_cast<const cpx<T>*>(a.rtw);
+    const bool ccs    = a.ccs != 0;
+    const long long olen = ccs ? C + 1 : C;
+    const auto nothing = []() {};
+    const FB fb(nullptr, a.d, TS);
+    // X[k] from Z[k] = u and Z[c - k] = v, w = W_2c^k
+    const auto split = [](cpx<T> u, cpx<T> v, cpx<T> w)
+    { return scale(u + conj(v), T(0.5)) + w * scale(mul_mi(u - conj(v)), T(0.5)); };
+    const auto mirror = [](cpx<T> w) { return mk<T>(-w.x, w.y); }; // W_2c^(c - k) = -conj(W_2c^k)
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    long long t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles)
+        fspt_load<S, N2>(st0, &tm_in, int(t % NTR) * 2 * S, int(t / NTR) * N2, &bars[0]);
+    for (int it = 0; t < ntiles; t += gridDim.x, it++)
+    {
+        const int s    = it & 1;
+        cpx<T>* stage  = st0 + s * SE;
+        const bool got = mbar_wait(&bars[s], (it >> 1) & 1, a.wait_spins);
+        if (!__syncthreads_and(got))
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicExch(err, 1);
+                // the copy waited for is the only load in flight (the next one is issued after this wait):
+                // give it a bounded chance to land before the CTA exits
+                mbar_wait(&bars[s], (it >> 1) & 1);
+            }
+            return;
+        }
+        const long long tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < ntiles)
+        {
+            // the other stage was last read by the previous tile's split, before this tile's first barrier
+            fence_proxy_async_smem();
+            fspt_load<S, N2>(st0 + (s ^ 1) * SE, &tm_in, int(tn % NTR) * 2 * S, int(tn / NTR) * N2, &bars[s ^ 1]);
+        }
+        // pass 1 reads the box, pass 2 writes the transformed rows back into it (same swizzled layout)
+        fb.run_pp([&](int p) { return stage[swz_8b<S>(p, g)]; },
+                  [&](int k2, cpx<T> v) { stage[swz_8b<S>(k2, g)] = v; }, nothing, nothing, stage, B + g * GB, tw, lt);
+        // run_pp ends with a barrier: every row of the tile is transformed
+        const long long b = t / NTR;
+        const int pb      = int(t % NTR) * S;
+        cpx<T>* X         = reinterpret_cast<cpx<T>*>(a.out) + b * olen;
+        for (int i = threadIdx.x; i < (S / 2) * N2; i += THREADS)
+        {
+            const int q = i % (S / 2), k2 = i / (S / 2);
+            const int p0 = pb + 2 * q; // even position: rows p0 / 2 and N1 - p0 / 2, or rows 0 and N1 / 2
+            if (p0 >= P1)
+                continue;
+            if (p0 > 0)
+            {
+                const long long ka = p0 / 2 + (long long)N1 * k2;
+                const cpx<T> u     = stage[swz_8b<S>(k2, 2 * q)];
+                const cpx<T> v     = stage[swz_8b<S>(N2 - 1 - k2, 2 * q + 1)];
+                const cpx<T> w     = ldg(rtw + p0 / 2) * ldg(rtw + N1 + k2);
+                X[ka]              = split(u, v, w);
+                X[C - ka]          = split(v, u, mirror(w));
+                continue;
+            }
+            // row 0: Z[N1 k2] pairs with Z[N1 (N2 - k2)] in the same row; Z[0] gives X[0] and X[c]
+            if (2 * k2 <= N2)
+            {
+                const cpx<T> u = stage[swz_8b<S>(k2, 2 * q)];
+                if (k2 == 0)
+                {
+                    X[0] = ccs ? mk<T>(u.x + u.y, T(0)) : mk<T>(u.x + u.y, u.x - u.y);
+                    if (ccs)
+                        X[C] = mk<T>(u.x - u.y, T(0));
+                }
+                else
+                {
+                    const cpx<T> v     = stage[swz_8b<S>(N2 - k2, 2 * q)];
+                    const long long ka = (long long)N1 * k2;
+                    const cpx<T> w     = ldg(rtw + N1 + k2);
+                    X[ka]              = split(u, v, w);
+                    if (2 * k2 != N2)
+                        X[C - ka] = split(v, u, mirror(w));
+                }
+            }
+            // row N1/2 (N1 even, position 1): Z[N1/2 + N1 k2] pairs with k2' = N2 - 1 - k2 in the same row
+            if (N1 % 2 == 0 && 2 * k2 <= N2 - 1)
+            {
+                const cpx<T> u     = stage[swz_8b<S>(k2, 2 * q + 1)];
+                const cpx<T> v     = stage[swz_8b<S>(N2 - 1 - k2, 2 * q + 1)];
+                const long long ka = N1 / 2 + (long long)N1 * k2;
+                const cpx<T> w     = ldg(rtw + N1 / 2) * ldg(rtw + N1 + k2);
+                X[ka]              = split(u, v, w);
+                if (2 * k2 != N2 - 1)
+                    X[C - ka] = split(v, u, mirror(w));
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------

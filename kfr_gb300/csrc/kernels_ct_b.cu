@@ -129,7 +129,7 @@ static cudaError_t go_fspt(K kernel, int threads, int smem, long long ntiles, cu
 
 // The persistent tensor-copy pair kernels where the length and the buffers allow them; done = false
 // otherwise (the caller then launches k_fsp_cols / k_fsp_rows).
-template <class FA, int N2>
+template <class FA, int N2, bool RP = false>
 static cudaError_t try_fspt_cols(const fourstep_args& a, cudaStream_t st, bool& done)
 {
     done = false;
@@ -142,7 +142,26 @@ static cudaError_t try_fspt_cols(const fourstep_args& a, cudaStream_t st, bool& 
             return cudaSuccess;
         done = true;
         const long long ntiles = a.batch * ((N2 + S - 1) / S);
-        return go_fspt(k_fspt_cols<float, FA, N2>, fspt_threads<FA>(), fspt_smem<FA>(), ntiles, st, a, m, ntiles,
+        return go_fspt(k_fspt_cols<float, FA, N2, RP>, fspt_threads<FA>(), fspt_smem<FA>(), ntiles, st, a, m, ntiles,
+                       a.err);
+    }
+    return cudaSuccess;
+}
+
+// The fused real row pass over the real-fused column layout (rows N1 rounded up to even values apart).
+template <class FB, int N1>
+static cudaError_t try_fspt_rows_r2c(const fourstep_args& a, cudaStream_t st, bool& done)
+{
+    done = false;
+    if constexpr (fspt_ok<FB>() && FB::npass == 2 && fspt_tile<FB>() % 2 == 0)
+    {
+        constexpr int N2 = FB::n, S = fspt_tile<FB>(), BR = N2 < 256 ? N2 : 256, P1 = N1 + (N1 & 1);
+        tensor_map mi;
+        if (!a.err || !a.rtw || !map_rows(mi, a.in, P1, N2 * a.batch, BR, S))
+            return cudaSuccess;
+        done = true;
+        const long long ntiles = a.batch * ((P1 + S - 1) / S);
+        return go_fspt(k_fspt_rows_r2c<float, FB, N1>, fspt_threads<FB>(), fspt_smem<FB>(), ntiles, st, a, mi, ntiles,
                        a.err);
     }
     return cudaSuccess;
@@ -190,6 +209,34 @@ static cudaError_t go_fsp_pair(const fourstep_args& a, bool cols, cudaStream_t s
                       (SB * FB::ts + 31) / 32 * 32, 2 * SB * FB::gstride() * 8, st, a);
     else
         return cudaErrorNotSupported;
+}
+
+bool has_ct_fsp_r2c_f32(int n1, int n2)
+{
+#define KFR_GPU_FSP_R2C_HAS(A, B)                                                                          \
+    if (n1 == A && n2 == B)                                                                                \
+        return fspt_ok<fs_len<A>::type>() && fspt_ok<fs_len<B>::type>() && fs_len<B>::type::npass == 2 &&    \
+               fspt_tile<fs_len<B>::type>() % 2 == 0 && (B * 8) % 16 == 0;
+    KFR_CT_FSPAIR_F32(KFR_GPU_FSP_R2C_HAS)
+#undef KFR_GPU_FSP_R2C_HAS
+    return false;
+}
+
+cudaError_t launch_ct_fsp_r2c_f32(const fourstep_args& a0, bool cols, cudaStream_t st)
+{
+    fourstep_args a = a0;
+    a.wait_spins    = wait_limit();
+#define KFR_GPU_FSP_R2C_CASE(A, B)                                                                         \
+    if (a.n1 == A && a.n2 == B)                                                                            \
+    {                                                                                                      \
+        bool done = false;                                                                                 \
+        const cudaError_t te = cols ? try_fspt_cols<fs_len<A>::type, B, true>(a, st, done)                   \
+                                    : try_fspt_rows_r2c<fs_len<B>::type, A>(a, st, done);                    \
+        return te != cudaSuccess ? te : (done ? cudaSuccess : cudaErrorNotSupported);                     \
+    }
+    KFR_CT_FSPAIR_F32(KFR_GPU_FSP_R2C_CASE)
+#undef KFR_GPU_FSP_R2C_CASE
+    return cudaErrorNotSupported;
 }
 
 cudaError_t launch_ct_fsp_f32(const fourstep_args& a0, bool cols, cudaStream_t st)

@@ -157,6 +157,12 @@ struct fourstep_args
     fast_div div_n;  // divides by the FFT length of this pass
     int* err;        // persistent pair kernels: set when a wait for a tile copy runs out (may be null)
     unsigned wait_spins = kDefaultWaitSpins;
+    // real forward DFT fused into the pair kernels (launch_ct_fsp_r2c_f32): x is the real signal viewed as
+    // n = n1 n2 complex values; the cols pass writes out[col*p1 + pos(k1)] with p1 = n1 rounded up to even and
+    // pos() placing k1 and n1 - k1 side by side; the rows pass writes the real spectrum (n + 1 bins for CCs,
+    // n for Perm) from both rows of each pair, with rtw = W_2n^k1 (k1 < n1) followed by W_2n^(n1 k2) (k2 < n2)
+    const void* rtw = nullptr;
+    int ccs         = 1;
 };
 
 template <typename T>
@@ -209,6 +215,11 @@ enum ew_op
 
 template <typename T>
 cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st);
+// The real-DFT split (forward, EW_R2C's arithmetic) or merge (inverse, EW_C2R's) with one thread per mirror
+// pair (e, c - e) of each c-point spectrum, so that every spectrum element is read once: a.n_src = c,
+// a.flag = CCs, strides as for launch_elementwise.
+template <typename T>
+cudaError_t launch_real_pairs(const ew_args& a, bool inverse, cudaStream_t st);
 
 // Batched transpose of complex matrices: out[b][c][r] = in[b][r][c] (b < batch, r < rows, c < cols).
 template <typename T>
@@ -251,6 +262,12 @@ cudaError_t launch_ct_fs_cols_f32(const fourstep_args& a, const block_cfg& c, cu
 // has no kernel.
 bool has_ct_fsp_f32(int n1, int n2);
 cudaError_t launch_ct_fsp_f32(const fourstep_args& a, bool cols, cudaStream_t st);
+// The real forward DFT of length 2 n1 n2 on the tensor-copy pair kernels with its split fused into the row
+// pass (two HBM round trips instead of three): whether the split n1 x n2 has them, and the two launches
+// (cols: the permuted column pass into a.out = scratch of batch n2 p1 values; rows: the fused row pass into
+// the spectrum).  The caller checks the alignment first: a.in and the scratch 16-byte aligned.
+bool has_ct_fsp_r2c_f32(int n1, int n2);
+cudaError_t launch_ct_fsp_r2c_f32(const fourstep_args& a, bool cols, cudaStream_t st);
 cudaError_t launch_ct_fs_rows_f32(const fourstep_args& a, const block_cfg& c, cudaStream_t st);
 
 // Launch bookkeeping done once per process instead of on every launch (launch_cache.cpp): the kernel's

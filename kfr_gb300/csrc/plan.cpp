@@ -13,6 +13,15 @@
 namespace kfr_gpu
 {
 
+// Scratch regions after the first start on a 256-byte boundary (the bulk and tensor copies of the kernels
+// that use them need 16-byte-aligned bases); each such boundary costs at most kAlignSlack elements.
+template <typename T>
+constexpr long long kAlignSlack = 256 / (2 * (long long)sizeof(T));
+inline char* align_scratch(char* p)
+{
+    return reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
+}
+
 namespace
 {
 std::atomic<unsigned> g_wait_spins{ kDefaultWaitSpins };
@@ -955,13 +964,31 @@ bool complex_engine<T>::plan_fourstep(long long n)
 }
 
 template <typename T>
+bool complex_engine<T>::pair_view_of(pair_view& v) const
+{
+    if (k_ != kind::fourstep || !pair_ || !err_.get())
+        return false;
+    v.n1      = n1_;
+    v.n2      = n2_;
+    v.tw_cols = pcols_.tw.get();
+    v.tw_rows = prows_.tw.get();
+    v.twA     = twA_.get();
+    v.twB     = twB_.get();
+    v.lbits   = lbits_;
+    v.dcols   = pcols_.desc;
+    v.drows   = prows_.desc;
+    v.err     = static_cast<int*>(err_.get());
+    return true;
+}
+
+template <typename T>
 long long complex_engine<T>::scratch_elems(long long batch) const
 {
     switch (k_)
     {
     case kind::fourstep: return batch * n_;
     case kind::tensor: return n1_ ? batch * n_ : 0;
-    case kind::bluestein_multi: return batch * m_ + inner_->scratch_elems(batch);
+    case kind::bluestein_multi: return batch * m_ + kAlignSlack<T> + inner_->scratch_elems(batch);
     default: return 0;
     }
 }
@@ -1225,7 +1252,7 @@ void complex_engine<T>::execute(void* out, const void* in, long long batch, long
         if (istride != n_ || ostride != n_)
             throw std::invalid_argument("internal: Bluestein needs contiguous signals");
         char* A     = static_cast<char*>(scratch);
-        char* inner = A + batch * m_ * esz;
+        char* inner = align_scratch(A + batch * m_ * esz);
         ew_args e;
         e.batch   = batch;
         e.t1      = nullptr;
@@ -1337,6 +1364,23 @@ real_engine<T>::real_engine(long long n) : n_(n), c_(n / 2), ceng_(n / 2)
     fused_ = ceng_.strategy() == complex_engine<T>::kind::smem;
     if (fused_)
         prog_.build(int(c_), CT_REAL);
+    typename complex_engine<T>::pair_view pv;
+    rfsp_ = sizeof(T) == 4 && !fused_ && ceng_.pair_view_of(pv) && has_ct_fsp_r2c_f32(int(pv.n1), int(pv.n2));
+    if (rfsp_)
+    {
+        std::vector<std::complex<T>> r2(pv.n1 + pv.n2);
+        for (long long k1 = 0; k1 < pv.n1; k1++)
+        {
+            const auto w = twiddle(k1, n);
+            r2[k1]       = std::complex<T>(T(w.real()), T(w.imag()));
+        }
+        for (long long k2 = 0; k2 < pv.n2; k2++)
+        {
+            const auto w     = twiddle(pv.n1 * k2, n);
+            r2[pv.n1 + k2] = std::complex<T>(T(w.real()), T(w.imag()));
+        }
+        rtw2_.upload(r2.data(), r2.size() * sizeof(std::complex<T>));
+    }
     // Pipelined forward and inverse kernels (compile-time c, single precision): an even number of signals
     // per tile, the most resident threads per SM with at least two CTAs, then the smallest tile.
     if (fused_ && prog_.ct && sizeof(T) == 4)
@@ -1372,12 +1416,14 @@ long long real_engine<T>::scratch_elems(long long batch) const
 {
     if (fused_)
         return 0;
-    return batch * (c_ + 1) + ceng_.scratch_elems(batch);
+    return batch * (c_ + 1) + kAlignSlack<T> + ceng_.scratch_elems(batch);
 }
 
 template <typename T>
 int real_engine<T>::launches(long long batch) const
 {
+    if (rfsp_)
+        return 2 * int((batch + 65534) / 65535); // forward (the inverse merges separately)
     return fused_ ? ((pipe_spc_ && batch % pipe_spc_) ? 2 : 1) : 1 + ceng_.launches(batch);
 }
 
@@ -1442,8 +1488,49 @@ void real_engine<T>::forward(void* out, const void* in, long long batch, bool cc
         }
         return;
     }
+    typename complex_engine<T>::pair_view pv;
+    if (rfsp_ && (reinterpret_cast<uintptr_t>(in) % 16) == 0 && ceng_.pair_view_of(pv))
+    {
+        // column pass into the real-fused layout (scratch), row pass with the split into out
+        char* y = align_scratch(static_cast<char*>(scratch));
+        for (long long b0 = 0; b0 < batch; b0 += 65535)
+        {
+            const long long nb = std::min<long long>(65535, batch - b0);
+            fourstep_args a{};
+            a.err         = pv.err;
+            a.batch       = nb;
+            a.sig_stride  = c_;
+            a.n1          = int(pv.n1);
+            a.n2          = int(pv.n2);
+            a.twA         = pv.twA;
+            a.twB         = pv.twB;
+            a.lbits       = pv.lbits;
+            a.rtw         = rtw2_.get();
+            a.ccs         = ccs;
+            a.in          = static_cast<const T*>(in) + b0 * n_;
+            a.out         = y;
+            a.tw          = pv.tw_cols;
+            a.d           = pv.dcols;
+            a.div_n       = make_fast_div(uint32_t(pv.n1));
+            check(launch_ct_fsp_r2c_f32(a, true, st), "launch r2c four-step columns");
+            a.in    = y;
+            a.out   = static_cast<std::complex<T>*>(out) + b0 * olen;
+            a.tw    = pv.tw_rows;
+            a.d     = pv.drows;
+            a.div_n = make_fast_div(uint32_t(pv.n2));
+            check(launch_ct_fsp_r2c_f32(a, false, st), "launch r2c four-step rows with the split");
+        }
+        return;
+    }
     char* Z     = static_cast<char*>(scratch);
-    char* inner = Z + batch * (c_ + 1) * 2 * sizeof(T);
+    char* inner = align_scratch(Z + batch * (c_ + 1) * 2 * sizeof(T));
+    if (reinterpret_cast<uintptr_t>(in) % (2 * sizeof(T)))
+    {
+        // the complex kernels read the reals in pairs: stage an input that is not aligned to a pair into
+        // Z (which the transform then overwrites in place)
+        check(cudaMemcpyAsync(Z, in, size_t(batch * n_) * sizeof(T), cudaMemcpyDeviceToDevice, st), "align input");
+        in = Z;
+    }
     ceng_.execute(Z, in, batch, c_, c_, false, inner, st);
     ew_args e;
     e.in      = Z;
@@ -1456,7 +1543,7 @@ void real_engine<T>::forward(void* out, const void* in, long long batch, bool cc
     e.t1      = nullptr;
     e.n_src   = c_;
     e.flag    = ccs;
-    check(launch_elementwise<T>(EW_R2C, e, st), "launch r2c split");
+    check(launch_real_pairs<T>(e, false, st), "launch r2c split");
 }
 
 template <typename T>
@@ -1504,7 +1591,7 @@ void real_engine<T>::inverse(void* out, const void* in, long long batch, bool cc
         return;
     }
     char* Z     = static_cast<char*>(scratch);
-    char* inner = Z + batch * (c_ + 1) * 2 * sizeof(T);
+    char* inner = align_scratch(Z + batch * (c_ + 1) * 2 * sizeof(T));
     ew_args e;
     e.in      = in;
     e.out     = Z;
@@ -1516,7 +1603,14 @@ void real_engine<T>::inverse(void* out, const void* in, long long batch, bool cc
     e.t1      = nullptr;
     e.n_src   = c_;
     e.flag    = ccs;
-    check(launch_elementwise<T>(EW_C2R, e, st), "launch c2r merge");
+    check(launch_real_pairs<T>(e, true, st), "launch c2r merge");
+    if (reinterpret_cast<uintptr_t>(out) % (2 * sizeof(T)))
+    {
+        // the complex kernels write the reals in pairs: transform in place in Z, then copy out
+        ceng_.execute(Z, Z, batch, c_, c_, true, inner, st);
+        check(cudaMemcpyAsync(out, Z, size_t(batch * n_) * sizeof(T), cudaMemcpyDeviceToDevice, st), "copy output");
+        return;
+    }
     ceng_.execute(out, Z, batch, c_, c_, true, inner, st);
 }
 
@@ -1524,7 +1618,8 @@ template <typename T>
 std::string real_engine<T>::describe() const
 {
     std::ostringstream s;
-    s << "real n=" << n_ << (fused_ ? " fused split/merge" : " separate split/merge");
+    s << "real n=" << n_
+      << (fused_ ? " fused split/merge" : rfsp_ ? " split fused into the four-step row pass" : " separate split/merge");
     if (pipe_spc_)
         s << " pipelined spc=" << pipe_spc_;
     s << " complex{" << ceng_.describe() << "}";
@@ -1601,7 +1696,7 @@ long long dct_engine<T>::scratch_elems(long long batch) const
 {
     if (fused_)
         return 0;
-    return batch * n_ + ceng_.scratch_elems(batch);
+    return batch * n_ + kAlignSlack<T> + ceng_.scratch_elems(batch);
 }
 
 template <typename T>
@@ -1655,7 +1750,7 @@ void dct_engine<T>::execute(void* out, const void* in, long long batch, bool inv
         return;
     }
     char* V     = static_cast<char*>(scratch);
-    char* inner = V + batch * n_ * 2 * sizeof(T);
+    char* inner = align_scratch(V + batch * n_ * 2 * sizeof(T));
     ew_args e;
     e.batch = batch;
     e.n     = n_;

@@ -165,6 +165,20 @@ public:
     int launches(long long batch) const;
     // Throws if a kernel of this engine recorded a device-side error (a bounded wait that ran out).
     void check_device_error() const;
+    // The compile-time pair four-step's split and tables (false unless this engine runs one), for the real
+    // engine's kernels that run the two passes with the real split fused in.
+    struct pair_view
+    {
+        long long n1, n2;
+        const void* tw_cols;
+        const void* tw_rows;
+        const void* twA;
+        const void* twB;
+        int lbits;
+        fft_desc dcols, drows;
+        int* err;
+    };
+    bool pair_view_of(pair_view& v) const;
     // While set, in and out of execute() are host memory mapped into the device's address space (zero-copy
     // calls): the kernels that read or write through bulk and tensor copies give way to the plain-load ones.
     // The caller holds the plan's lock around the call.
@@ -231,6 +245,10 @@ private:
     bool fused_ = false;
     int pipe_spc_ = 0; // signals per tile of the pipelined forward / inverse kernels, 0 = not used
     dbuf err_;
+    // forward on the complex engine's pair kernels with the split fused into the row pass (16-byte-aligned
+    // input; launch_ct_fsp_r2c_f32), and its two-level table of W_n^k: W_n^k1 (k1 < n1), W_n^(n1 k2)
+    bool rfsp_ = false;
+    dbuf rtw2_;
 };
 
 // dct_plan<T>: DCT-II forward, DCT-III (X0 halved) inverse, unscaled.

@@ -371,6 +371,56 @@ def test_real_dft_batched_against_oracle(orc, n, batch, fmt):
     assert rel_rms(yd.cpu().numpy() / n, x) <= 2 * c32_tolerance(n), n
 
 
+@pytest.mark.parametrize("n", [44100, 48000])
+@pytest.mark.parametrize("fmt", ["CCs", "Perm"])
+def test_real_dft_split_fused_into_fourstep_rows(orc, n, fmt):
+    """Real lengths whose half-length complex DFT is a compile-time pair (22050 = 147 x 150, 24000 = 150 x 160):
+    the column pass writes each column with rows k1 and N1 - k1 side by side (and, for odd N1, one unused slot
+    so that the rows stay 16-byte aligned for the row pass's tensor copies), and the row pass applies the
+    real split to both rows of each pair, writing the spectrum directly.  Many tiles per CTA, an odd batch,
+    both formats; a 4-byte-misaligned input (staged into aligned scratch, then the separate split) gives the
+    same results, and so does the inverse into a 4-byte-misaligned output."""
+    batch = 61
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    ccs = fmt == "CCs"
+    plan = k.dft_plan_real(n, fmt, "f32")
+    xd = dev(x)
+    Xd = torch.empty((batch, plan.complex_size), dtype=torch.complex64, device="cuda")
+    plan.execute_batch(Xd, xd, batch)
+    pick = [0, 1, batch // 2, batch - 1]
+    ref = orc.dft_real(x[pick].astype(np.float64), ccs=ccs, threads=8)
+    assert rel_rms(Xd.cpu().numpy()[pick], ref) <= c32_tolerance(n)
+    buf = torch.empty(batch * n + 1, device="cuda")
+    buf[1:].copy_(xd.reshape(-1))
+    Xm = torch.empty_like(Xd)
+    plan.execute_batch(Xm, buf[1:], batch)
+    assert rel_rms(Xm.cpu().numpy(), Xd.cpu().numpy()) <= c32_tolerance(n)
+    # the inverse into a 4-byte-misaligned output (transformed in place in scratch, then copied)
+    back = torch.empty(batch * n + 1, device="cuda")
+    plan.execute_batch(back[1:], Xd, batch, inverse=True)
+    assert rel_rms(back[1:].reshape(batch, n).cpu().numpy() / n, x) <= 2 * c32_tolerance(n)
+
+
+@pytest.mark.parametrize("n,batch", [(1920, 33), (4096, 5), (2 * 8191, 3), (30, 7)])
+def test_real_dft_reals_aligned_to_one_element(orc, n, batch):
+    """Real input and output pointers aligned to one float only (a float array at an odd offset, which the
+    reference's float* interface allows): the per-tile kernels load and store such reals one by one, the
+    multi-kernel paths stage them through aligned scratch; same results as from aligned buffers."""
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    plan = k.dft_plan_real(n, "CCs", "f32")
+    buf = torch.zeros(batch * n + 1, device="cuda")
+    buf[1:].copy_(dev(x).reshape(-1))
+    X = torch.empty((batch, plan.complex_size), dtype=torch.complex64, device="cuda")
+    plan.execute_batch(X, buf[1:], batch)
+    ref = orc.dft_real(x.astype(np.float64), ccs=True, threads=8)
+    assert rel_rms(X.cpu().numpy(), ref) <= c32_tolerance(n)
+    back = torch.zeros(batch * n + 1, device="cuda")
+    plan.execute_batch(back[1:], X, batch, inverse=True)
+    assert rel_rms(back[1:].reshape(batch, n).cpu().numpy() / n, x) <= 2 * c32_tolerance(n)
+
+
 # ------------------------------------------------------------------------------------------------------
 # DCT
 # ------------------------------------------------------------------------------------------------------
