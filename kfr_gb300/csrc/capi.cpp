@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 #include <stdexcept>
 #include <string>
 
@@ -491,11 +492,13 @@ void run(plan_base& pl, void* out, size_t out_bytes, const void* in, size_t in_b
 }
 
 // Host buffers on both sides of a synchronous call of a batch-separable transform: the batch runs as a
-// pipeline of chunks (about 16 MiB of input each) over kPipeStreams streams, so that copying chunk c+1 in,
-// transforming chunk c and copying chunk c-1 out overlap (the two copy directions and the kernels run
-// concurrently).  exec(dout, din, nb, scratch, stream) transforms nb signals; scr_bytes(nb) is its scratch.
-// Returns false (nothing done) when the call does not qualify: device pointers, a caller stream, or a
-// batch too small to split.
+// pipeline of chunks (up to about 16 MiB of input each) over kPipeStreams streams, so that copying chunk c+1
+// in, transforming chunk c and copying chunk c-1 out overlap (the two copy directions and the kernels run
+// concurrently).  The first chunks grow from a quarter of that size and the last ones shrink back to it, so
+// that the copy-in before the first transform and the copy-out after the last one (when only one link
+// direction is busy) stay short.  exec(dout, din, nb, scratch, stream) transforms nb signals; scr_bytes(nb)
+// is its scratch.  Returns false (nothing done) when the call does not qualify: device pointers, a caller
+// stream, or a batch too small to split.
 template <typename Exec, typename Scr>
 bool run_chunked(plan_base& pl, void* out, size_t out_per, const void* in, size_t in_per, size_t batch, void* stream,
                  Scr&& scr_bytes, Exec&& exec)
@@ -504,9 +507,30 @@ bool run_chunked(plan_base& pl, void* out, size_t out_per, const void* in, size_
         return false;
     const size_t per   = std::max(in_per, out_per);
     const size_t chunk = std::max<size_t>(1, std::min<size_t>(batch, (size_t(16) << 20) / std::max<size_t>(per, 1)));
-    const size_t nchunks = (batch + chunk - 1) / chunk;
-    if (nchunks < 2)
+    if ((batch + chunk - 1) / chunk < 2)
         return false;
+    // chunk boundaries: sizes chunk/4, chunk/2, chunk, ..., chunk, chunk/2, chunk/4 (each at least one signal)
+    std::vector<size_t> bounds{ 0 };
+    {
+        const size_t q = std::max<size_t>(1, chunk / 4), h = std::max<size_t>(1, chunk / 2);
+        const size_t ramp = 2 * (q + h);
+        std::vector<size_t> sizes;
+        if (batch >= 2 * ramp + chunk)
+        {
+            sizes = { q, h };
+            size_t mid = batch - 2 * (q + h);
+            for (; mid > 0; mid -= std::min(mid, chunk))
+                sizes.push_back(std::min(mid, chunk));
+            sizes.push_back(h);
+            sizes.push_back(q);
+        }
+        else
+            for (size_t left = batch; left > 0; left -= std::min(left, chunk))
+                sizes.push_back(std::min(left, chunk));
+        for (size_t z : sizes)
+            bounds.push_back(bounds.back() + z);
+    }
+    const size_t nchunks = bounds.size() - 1;
     std::unique_lock<std::mutex> lock(pl.mu);
     if (!pl.pipes)
         pl.pipes.reset(new pipe_set());
@@ -524,8 +548,8 @@ bool run_chunked(plan_base& pl, void* out, size_t out_per, const void* in, size_
     for (size_t c = 0; c < nchunks; c++)
     {
         const int k       = int(c % kPipeStreams);
-        const size_t b0   = c * chunk;
-        const size_t nb   = std::min(chunk, batch - b0);
+        const size_t b0   = bounds[c];
+        const size_t nb   = bounds[c + 1] - bounds[c];
         cudaStream_t st   = P.s[k];
         check(cudaMemcpyAsync(P.in[k].get(), hin + b0 * in_per, nb * in_per, cudaMemcpyHostToDevice, st),
               "copy input to device");
