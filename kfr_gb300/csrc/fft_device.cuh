@@ -427,6 +427,25 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t x, const fast_div f)
 // threads lt in [0, ts) of a signal group own butterflies j = lt + b*ts.
 // --------------------------------------------------------------------------------------------------
 
+// v[r] *= W^{k r} from the one table value w1 = W^k by a binary powering tree, w_r = w_{r/2} w_{r - r/2}
+// (at most ceil(log2 r) products deep): one load per butterfly instead of R - 1.  Both factors have index
+// <= R/2 for every r < R, so only those powers stay live.
+template <typename T, int R>
+__device__ __forceinline__ void twiddle_powers(cpx<T> (&v)[R], const cpx<T> w1)
+{
+    cpx<T> w[R / 2 + 1];
+    w[1] = w1;
+    v[1] = v[1] * w1;
+#pragma unroll
+    for (int r = 2; r < R; r++)
+    {
+        const cpx<T> wr = w[r / 2] * w[r - r / 2];
+        if (r <= R / 2)
+            w[r] = wr;
+        v[r] = v[r] * wr;
+    }
+}
+
 template <typename T, int R, int EPT>
 __device__ __forceinline__ void pass_load(cpx<T> (&v)[EPT], const cpx<T>* buf, const int n, const pass_desc& p,
                                           const cpx<T>* __restrict__ tw, const int lt, const int ts)
@@ -445,11 +464,9 @@ __device__ __forceinline__ void pass_load(cpx<T> (&v)[EPT], const cpx<T>* buf, c
                 v[b * R + r] = buf[pidx<T>(j + r * nbf)];
             if (ns > 1)
             {
-                const int k     = j - int(fdiv(uint32_t(j), p.div_ns)) * ns;
-                const cpx<T>* t = tw + p.tw_off + k;
-#pragma unroll
-                for (int r = 1; r < R; r++)
-                    v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * ns);
+                // W^{k r} from the one table value W^k (the r = 1 entry) by the powering tree
+                const int k = j - int(fdiv(uint32_t(j), p.div_ns)) * ns;
+                twiddle_powers<T, R>(reinterpret_cast<cpx<T>(&)[R]>(v[b * R]), ldg(tw + p.tw_off + k));
             }
             dft_codelet<T, R>(&v[b * R]);
         }
@@ -676,30 +693,6 @@ __device__ __forceinline__ void ct_block_fft(cpx<T>* buf, const cpx<T>* __restri
     ct_passes<T, N, TS, EPT, 1, 0, Rs...>(v, buf, tw, lta);
 }
 
-// Ping-pong compile-time block FFT: pass i reads buffer A (i even) or B (i odd) and writes the other, so a
-// pass needs one barrier and each butterfly's outputs are stored as soon as they are computed (no register
-// array spans the pass).  ld(p) fetches input p of the first pass, st(q, x) stores output q of the last
-// pass (which writes A when the number of passes is even, else B); the passes in between use the padded
-// layouts of A and B.  hook() runs once, after the first pass's closing barrier.  Ends with a barrier.
-// v[r] *= W^{k r} from the one table value w1 = W^k by a binary powering tree, w_r = w_{r/2} w_{r - r/2}
-// (at most ceil(log2 r) products deep): one load per butterfly instead of R - 1.  Both factors have index
-// <= R/2 for every r < R, so only those powers stay live.
-template <typename T, int R>
-__device__ __forceinline__ void twiddle_powers(cpx<T> (&v)[R], const cpx<T> w1)
-{
-    cpx<T> w[R / 2 + 1];
-    w[1] = w1;
-    v[1] = v[1] * w1;
-#pragma unroll
-    for (int r = 2; r < R; r++)
-    {
-        const cpx<T> wr = w[r / 2] * w[r - r / 2];
-        if (r <= R / 2)
-            w[r] = wr;
-        v[r] = v[r] * wr;
-    }
-}
-
 // no-op post(j, o): the last pass stores its outputs as computed
 struct no_post
 {
@@ -709,6 +702,11 @@ struct no_post
     }
 };
 
+// Ping-pong compile-time block FFT: pass i reads buffer A (i even) or B (i odd) and writes the other, so a
+// pass needs one barrier and each butterfly's outputs are stored as soon as they are computed (no register
+// array spans the pass).  ld(p) fetches input p of the first pass, st(q, x) stores output q of the last
+// pass (which writes A when the number of passes is even, else B); the passes in between use the padded
+// layouts of A and B.  hook() runs once, after the first pass's closing barrier.  Ends with a barrier.
 // post(j, o) sees butterfly j's outputs o[r] (output j + r NS in the last pass) before they are stored
 template <typename T, int N, int TS, int R, int NS, int TWOFF, class LD, class ST, class PO = no_post>
 __device__ __forceinline__ void pp_pass(const LD& ld, const ST& st, const cpx<T>* __restrict__ tw, const int lt,
