@@ -464,9 +464,20 @@ __device__ __forceinline__ void pass_load(cpx<T> (&v)[EPT], const cpx<T>* buf, c
                 v[b * R + r] = buf[pidx<T>(j + r * nbf)];
             if (ns > 1)
             {
-                // W^{k r} from the one table value W^k (the r = 1 entry) by the powering tree
                 const int k = j - int(fdiv(uint32_t(j), p.div_ns)) * ns;
-                twiddle_powers<T, R>(reinterpret_cast<cpx<T>(&)[R]>(v[b * R]), ldg(tw + p.tw_off + k));
+                if constexpr (sizeof(T) == 4)
+                {
+                    // W^{k r} from the one table value W^k (the r = 1 entry) by the powering tree
+                    twiddle_powers<T, R>(reinterpret_cast<cpx<T>(&)[R]>(v[b * R]), ldg(tw + p.tw_off + k));
+                }
+                else
+                {
+                    // double precision: table loads (FP64 products are slow on this part)
+                    const cpx<T>* t = tw + p.tw_off + k;
+#pragma unroll
+                    for (int r = 1; r < R; r++)
+                        v[b * R + r] = v[b * R + r] * ldg(t + (r - 1) * ns);
+                }
             }
             dft_codelet<T, R>(&v[b * R]);
         }
