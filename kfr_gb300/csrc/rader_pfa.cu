@@ -25,9 +25,11 @@
 // middle axes run in place; the last axis of the first DFT and the same axis of the second are fused around
 // the multiplication by bphys; the second DFT's axis-0 pass reads into registers, a barrier, then scatters X
 // in natural order into the buffer, which one bulk copy stores (the tile's edge elements beyond the 16-byte
-// interior by plain stores).  Measured on 256 MiB batches (N=8191: 640 threads, one CTA per SM; N=127: 24
-// signals per tile, four CTAs per SM), two buffers beat one by 16% to 20%, and an earlier tiled ping-pong kernel
-// (three buffers, twiddled passes) by 12% (8191) and 22% (127).
+// interior by plain stores).  The three tables (bphys, and tin / tout as 16-bit indices) are copied into
+// shared memory once per CTA.  Measured on 256 MiB batches (N=8191: 640 threads, one CTA per SM; N=127: 24
+// signals per tile, four CTAs per SM), two buffers beat one by 16% to 20%, an earlier tiled ping-pong kernel
+// (three buffers, twiddled passes) by 12% (8191) and 22% (127), and the shared-memory tables the same tables
+// read through L1 by 6.5% (8191: 96 KB of tables beside 128 KB of tile buffers) and 4.5% (127).
 #include "kernels.cuh"
 
 namespace kfr_gpu
@@ -136,6 +138,18 @@ __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_arg
     cpx<T>* x0s        = bufs + NBUF * pfa_buflen<N, SPC>();
     cpx<T>* a0s        = x0s + SPC;
     uint64_t* bars     = reinterpret_cast<uint64_t*>(a0s + SPC);
+    // the kernel-spectrum and index tables, copied once per CTA into shared memory (for N = 8191 they are
+    // 96 KB, which the L1 left beside the tile buffers does not hold)
+    static_assert(N <= 65536, "16-bit index tables");
+    cpx<T>* const sbph    = reinterpret_cast<cpx<T>*>(bars + NBUF);
+    uint16_t* const stin  = reinterpret_cast<uint16_t*>(sbph + L);
+    uint16_t* const stout = stin + L;
+    for (int i = threadIdx.x; i < L; i += THREADS)
+    {
+        sbph[i]  = ldg(reinterpret_cast<const cpx<T>*>(a.bphys) + i);
+        stin[i]  = uint16_t(__ldg(a.tin + i));
+        stout[i] = uint16_t(__ldg(a.tout + i));
+    }
     // kernel parameters are read where they are used (from the parameter bank), and the tile's byte range is
     // recomputed after the passes, so that little stays live across the passes' register-heavy codelets
     constexpr long long tile_bytes = (long long)SPC * N * ESZ;
@@ -214,7 +228,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_arg
         {
 #pragma unroll
             for (int q = 0; q < R0; q++)
-                v[q] = conj_if(buf[off + gs * N + __ldg(a.tin + gb + q * S0)], inv);
+                v[q] = conj_if(buf[off + gs * N + stin[gb + q * S0]], inv);
             dft_codelet<T, R0>(v);
         }
         __syncthreads(); // every gather is done before the array overwrites the input
@@ -234,7 +248,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_arg
             {
                 if (pos == 0)
                     a0s[s] = x; // A[0]: the sum of x[1..N-1]
-                return conj(x * ldg(reinterpret_cast<const cpx<T>*>(a.bphys) + pos));
+                return conj(x * sbph[pos]);
             };
             axis_pass<T, RF, SF, L, THREADS, true>(buf, ns, mul);
         }
@@ -255,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_arg
             const cpx<T> x0 = x0s[gs];
 #pragma unroll
             for (int q = 0; q < R0; q++)
-                buf[off + gs * N + __ldg(a.tout + gb + q * S0)] = conj_if(x0 + conj(v[codelet_out<R0>(q)]), a.inverse != 0);
+                buf[off + gs * N + stout[gb + q * S0]] = conj_if(x0 + conj(v[codelet_out<R0>(q)]), a.inverse != 0);
         }
         if (int(threadIdx.x) < ns)
             buf[off + threadIdx.x * N] = conj_if(x0s[threadIdx.x] + a0s[threadIdx.x], a.inverse != 0);
@@ -296,7 +310,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_rader_pfa(const rader_pfa_arg
 template <int N, int SPC, int NBUF>
 constexpr int pfa_smem()
 {
-    return (NBUF * pfa_buflen<N, SPC>() + 2 * SPC) * 8 + 16;
+    // tile buffers, x[0] and A[0] per signal, mbarriers, the spectrum table and the two 16-bit index tables
+    return (NBUF * pfa_buflen<N, SPC>() + 2 * SPC) * 8 + NBUF * 8 + (N - 1) * (8 + 2 + 2);
 }
 
 template <class K>
