@@ -50,8 +50,8 @@ NCU_TRAFFIC_BYTES_PER_SIGNAL: dict[int, float] = {
     1536: (268_477_440 + 213_674_240) / 21845,
     2187: (268_476_672 + 216_896_512) / 15342,
     30720: (268_411_904 + 216_671_488 + 268_498_176 + 213_238_528) / 1092,
-    127: (268_488_960 + 213_872_128) / 264208,
-    8191: (268_600_064 + 213_764_096) / 4096,
+    127: (268_486_912 + 210_538_752) / 264208,
+    8191: (268_598_272 + 214_211_072) / 4096,
 }
 
 
@@ -450,6 +450,20 @@ def run_case(spec: str) -> int:
         torch.cuda.synchronize()
         print(json.dumps({"case": spec, "elements": int(sum(lengths)), "plan": up.describe()}))
         return 0
+    if parts[0] == "dct":
+        # DCT-II of `MiB` of f32 signals of length n, three calls back to back on a stream
+        n = int(parts[1])
+        mib = int(parts[2]) if len(parts) > 2 else 16
+        b = max(1, (mib << 20) // (4 * n))
+        plan = k.dct_plan(n)
+        x = torch.rand(b, n, device="cuda") * 2 - 1
+        y = torch.empty_like(x)
+        st = torch.cuda.Stream()
+        for _ in range(3):
+            plan.execute_batch(y, x, b, stream=st.cuda_stream)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": spec, "batch": b}))
+        return 0
     if parts[0] == "real":
         # the forward real DFT (CCs) of `MiB` of f32 signals of length n
         n = int(parts[1])
@@ -497,7 +511,7 @@ def main():
     ap.add_argument("--batch-mib", type=int, default=None, help="MiB per length instead of 256 (profiling)")
     ap.add_argument("--case", type=str, default=None,
                     help="profiling: run one plan `form:n[:MiB]` three times and exit (form: plain, fp16, bf16, "
-                         "real; or uneven:count[:fixed], fixed = no autotuning)")
+                         "real, dct; or uneven:count[:fixed], fixed = no autotuning)")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case)
