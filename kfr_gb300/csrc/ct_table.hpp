@@ -56,7 +56,7 @@
 
 // half lengths c = N/2 of the fused real DFT (dft_plan_real<float>): N = 1920, 2048, 4096, 8192
 #define KFR_CT_REAL_F32(X)                                                                                  \
-    X(960, 64, 16, 4, 3, 5)                                                                                  \
+    X(960, 96, 16, 6, 10)                                                                                    \
     X(1024, 64, 16, 16, 4)                                                                                   \
     X(2048, 128, 16, 16, 8)                                                                                  \
     X(4096, 256, 16, 16, 16)
