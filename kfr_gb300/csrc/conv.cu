@@ -208,7 +208,9 @@ conv_filter<T>::conv_filter(const T* taps, size_t ntaps, size_t block_size, int 
     while (block_program<T>::feasible((long long)(cmax * 2)))
         cmax *= 2;
     const size_t fmax = 2 * cmax;
-    size_t f          = std::max(next_pow2(4 * m1), 2 * next_pow2(block_size ? block_size : 1024));
+    // the FFT is at least 8x the taps (at most 1/8 of each block re-reads the overlap; measured 0.390 ->
+    // 0.374 ms against 4x for 64 channels of 2^20 samples and 1023 taps) and twice the block
+    size_t f          = std::max(next_pow2(8 * m1), 2 * next_pow2(block_size ? block_size : 1024));
     f                 = std::max<size_t>(f, 64);
     if (f > fmax)
         f = fmax;
