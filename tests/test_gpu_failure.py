@@ -70,6 +70,25 @@ def test_real_pipelined_wait_reported(restore_limit, orc, inverse):
     assert rel_rms(X[:4].cpu().numpy(), ref) <= c32_tolerance(n)
 
 
+@pytest.mark.parametrize("n", [44100, 48000])
+def test_real_fourstep_with_fused_split_wait_reported(restore_limit, orc, n):
+    """The real DFT whose split is fused into the four-step row pass (k_fspt_cols over the mirror-paired
+    layout, then k_fspt_rows_r2c): a copy wait that runs out is reported, and the plan recovers."""
+    batch = 40
+    plan = k.dft_plan_real(n)
+    g = torch.Generator(device="cuda").manual_seed(n)
+    x = torch.randn(batch, n, device="cuda", generator=g)
+    X = torch.empty(batch, n // 2 + 1, dtype=torch.complex64, device="cuda")
+    L = k.lib()
+    L.kfr_set_wait_limit(0)
+    with pytest.raises(k.KfrError, match="gave up waiting"):
+        plan.execute_batch(X, x, batch)
+    L.kfr_set_wait_limit(DEFAULT)
+    plan.execute_batch(X, x, batch)
+    ref = orc.dft_real(x[:3].cpu().numpy().astype(np.float64))
+    assert rel_rms(X[:3].cpu().numpy(), ref) <= c32_tolerance(n)
+
+
 def test_uneven_stage_wait_runs_out_within_a_second(restore_limit, orc):
     """An uneven batch with a four-step signal (65536 = COL tiles, then ROW tiles that wait on the COL
     stage's counter) and one-CTA signals.  With the stage target made unreachable and a limit of 4096 polls
