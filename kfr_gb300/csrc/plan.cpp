@@ -138,6 +138,43 @@ void host_fft_pow2(std::vector<std::complex<double>>& b)
             }
 }
 
+// Forward DFT of a[0..n) in place by decimation in time over the smallest prime factor, the roots W_n^k
+// read from w (W_N^k, k < N) at stride N / n.
+static void host_dft_rec(std::complex<double>* a, long long n, const std::vector<std::complex<double>>& w, long long N)
+{
+    if (n <= 1)
+        return;
+    long long p = 2;
+    while (p * p <= n && n % p)
+        p++;
+    if (n % p)
+        p = n;
+    const long long m = n / p, st = N / n;
+    std::vector<std::complex<double>> sub(n);
+    for (long long r = 0; r < p; r++)
+        for (long long j = 0; j < m; j++)
+            sub[r * m + j] = a[j * p + r];
+    if (m > 1)
+        for (long long r = 0; r < p; r++)
+            host_dft_rec(&sub[r * m], m, w, N);
+    for (long long k = 0; k < n; k++)
+    {
+        std::complex<double> acc = 0;
+        for (long long r = 0; r < p; r++)
+            acc += sub[r * m + k % m] * w[((r * k) % n) * st];
+        a[k] = acc;
+    }
+}
+
+void host_dft_smooth(std::vector<std::complex<double>>& a)
+{
+    const long long n = (long long)a.size();
+    std::vector<std::complex<double>> w(std::max<long long>(n, 1));
+    for (long long k = 0; k < n; k++)
+        w[k] = twiddle(k, n);
+    host_dft_rec(a.data(), n, w, n);
+}
+
 void host_dft(std::vector<std::complex<double>>& a)
 {
     const long long n = (long long)a.size();
@@ -804,8 +841,9 @@ void bluestein_tables(long long n, long long m, dbuf& chirp_out, dbuf& bhat_out)
         chirp[k]   = std::complex<T>(T(chirp64[k].real()), T(chirp64[k].imag()));
     }
     chirp_out.upload(chirp.data(), chirp.size() * sizeof(std::complex<T>));
-    // bhat = conj(FFT_M(b)) / M with b[k] = b[M-k] = chirp[k]: evaluated in double on the host by a plain
-    // radix-2 FFT so the table is exact to double rounding before it is stored as T.
+    // bhat = conj(FFT_M(b)) / M with b[k] = b[M-k] = chirp[k]: evaluated in double on the host (mixed-radix
+    // decimation in time over one table of roots) so the table is exact to double rounding before it is
+    // stored as T.
     std::vector<std::complex<double>> b(m, { 0.0, 0.0 });
     for (long long k = 0; k < n; k++)
     {
@@ -813,7 +851,7 @@ void bluestein_tables(long long n, long long m, dbuf& chirp_out, dbuf& bhat_out)
         if (k)
             b[m - k] = chirp64[k];
     }
-    host_fft_pow2(b);
+    host_dft_smooth(b);
     std::vector<std::complex<T>> bh(m);
     const double inv_m = 1.0 / double(m);
     for (long long k = 0; k < m; k++)

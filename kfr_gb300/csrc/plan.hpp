@@ -65,6 +65,8 @@ std::complex<double> twiddle(long long k, long long n);
 void host_fft_pow2(std::vector<std::complex<double>>& a);
 // Forward DFT of any length in double precision (host; recursive mixed radix, O(N * sum of prime factors)).
 void host_dft(std::vector<std::complex<double>>& a);
+// The same for lengths with small prime factors, over one table of roots (fast for long smooth lengths).
+void host_dft_smooth(std::vector<std::complex<double>>& a);
 
 // Radix sequence for a one-CTA length; empty if a prime factor exceeds kGenericMax.
 std::vector<int> factor_radices(long long n);
