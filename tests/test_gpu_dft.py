@@ -220,6 +220,32 @@ def test_page_locked_host_buffers(orc, n, batch):
     assert rel_rms(hz.numpy()[pick], ref) <= tol(n, "f32")
 
 
+@pytest.mark.parametrize("n,batch", [(1000, 600), (8191, 40)])
+def test_kfr_allocate_buffers(orc, n, batch):
+    """Buffers from kfr_allocate (host memory registered with the driver): a zero-copy length (1000) and a
+    chunk-pipeline length (8191) give the device call's results."""
+    import ctypes
+    nbytes = batch * n * 8
+    pin, pout = k.allocate(nbytes), k.allocate(nbytes)
+    try:
+        hin = np.ctypeslib.as_array((ctypes.c_float * (2 * batch * n)).from_address(pin)).view(np.complex64)
+        hout = np.ctypeslib.as_array((ctypes.c_float * (2 * batch * n)).from_address(pout)).view(np.complex64)
+        rng = np.random.default_rng(n)
+        hin[:] = (rng.standard_normal(batch * n) + 1j * rng.standard_normal(batch * n)).astype(np.complex64)
+        plan = k.dft_plan(n, "f32")
+        plan.execute_batch(pout, pin, batch)
+        xd = dev(hin.reshape(batch, n))
+        yd = torch.empty_like(xd)
+        plan.execute_batch(yd, xd, batch)
+        assert rel_rms(hout.reshape(batch, n), yd.cpu().numpy()) <= tol(n, "f32") / 4
+        pick = [0, batch - 1]
+        ref = orc.dft(hin.reshape(batch, n)[pick].astype(np.complex128))
+        assert rel_rms(hout.reshape(batch, n)[pick], ref) <= tol(n, "f32")
+    finally:
+        k.deallocate(pin)
+        k.deallocate(pout)
+
+
 def plan_forward(plan, hx, batch):
     hy = torch.empty_like(hx).pin_memory()
     plan.execute_batch(hy, hx, batch)
