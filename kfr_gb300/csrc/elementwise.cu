@@ -37,50 +37,6 @@ __global__ void __launch_bounds__(256) k_elementwise(const int op, const ew_args
         case EW_BS_POST:
             out[s * a.ostride + e] = conj_if(conj(in[s * a.istride + e]) * ldg(t0 + e), a.flag != 0);
             break;
-        case EW_R2C:
-        {
-            const long long c = a.n_src;
-            const cpx<T>* z   = in + s * a.istride;
-            cpx<T> v;
-            if (e == 0)
-            {
-                const cpx<T> z0 = z[0];
-                v = a.flag ? mk<T>(z0.x + z0.y, 0) : mk<T>(z0.x + z0.y, z0.x - z0.y);
-            }
-            else if (e == c)
-            {
-                const cpx<T> z0 = z[0];
-                v               = mk<T>(z0.x - z0.y, 0);
-            }
-            else
-            {
-                const cpx<T> zk  = z[e];
-                const cpx<T> znk = conj(z[c - e]);
-                v = scale(zk + znk, T(0.5)) + ldg(t0 + e) * scale(mul_mi(zk - znk), T(0.5));
-            }
-            out[s * a.ostride + e] = v;
-            break;
-        }
-        case EW_C2R:
-        {
-            const long long c = a.n_src;
-            const cpx<T>* X   = in + s * a.istride;
-            cpx<T> z;
-            if (e == 0)
-            {
-                const T x0 = X[0].x;
-                const T xn = a.flag ? X[c].x : X[0].y;
-                z          = mk<T>(x0 + xn, x0 - xn);
-            }
-            else
-            {
-                const cpx<T> xk  = X[e];
-                const cpx<T> xnk = conj(X[c - e]);
-                z                = (xk + xnk) + mul_pi(conj(ldg(t0 + e)) * (xk - xnk));
-            }
-            out[s * a.ostride + e] = z;
-            break;
-        }
         case EW_DCT2_PRE:
         {
             // e is the source index; write its mirrored position

@@ -205,8 +205,6 @@ enum ew_op
     EW_BS_PRE    = 0, // out[e] = e < n_src ? conj_if(in[e], flag) * chirp[e] : 0   (n = M)
     EW_BS_MID    = 1, // out[e] = conj(in[e] * bhat[e])                               (n = M)
     EW_BS_POST   = 2, // out[k] = conj_if(conj(in[k]) * chirp[k], flag)               (n = N)
-    EW_R2C       = 3, // real forward split of a c-point spectrum Z; n = c+1 (CCs) or c (Perm)
-    EW_C2R       = 4, // real inverse merge into conj of a c-point spectrum (n = c)
     EW_DCT2_PRE  = 5, // mirrored complex input (n = N)
     EW_DCT2_POST = 6, // Re*cos + Im*sin (n = N)
     EW_DCT3_PRE  = 7, // x * e^{-i pi k / 2N}, X0 halved (n = N)
@@ -215,9 +213,11 @@ enum ew_op
 
 template <typename T>
 cudaError_t launch_elementwise(int op, const ew_args& a, cudaStream_t st);
-// The real-DFT split (forward, EW_R2C's arithmetic) or merge (inverse, EW_C2R's) with one thread per mirror
-// pair (e, c - e) of each c-point spectrum, so that every spectrum element is read once: a.n_src = c,
-// a.flag = CCs, strides as for launch_elementwise.
+// The real-DFT split (forward: X[k] = (Z[k] + conj Z[c-k]) / 2 - i W_2c^k (Z[k] - conj Z[c-k]) / 2 from the
+// c-point spectrum Z of the reals taken in pairs; n = c + 1 bins for CCs, c for Perm) or merge (inverse: the
+// c-point spectrum whose inverse gives the reals) with one thread per mirror pair (e, c - e) of each
+// spectrum, so that every spectrum element is read once: a.n_src = c, a.flag = CCs, strides as for
+// launch_elementwise, a.t0 = W_2c^k for k = 0..c.
 template <typename T>
 cudaError_t launch_real_pairs(const ew_args& a, bool inverse, cudaStream_t st);
 

@@ -1486,7 +1486,7 @@ void real_engine<T>::forward(void* out, const void* in, long long batch, bool cc
         e.t1      = nullptr;
         e.n_src   = 1;
         e.flag    = ccs;
-        check(launch_elementwise<T>(EW_R2C, e, st), "launch r2c split");
+        check(launch_real_pairs<T>(e, false, st), "launch r2c split");
         return;
     }
     if (fused_)
