@@ -314,9 +314,12 @@ def test_complex_dft_c64_large(orc):
     assert rel_rms(yd.cpu().numpy(), ref) <= c64_tolerance(n)
 
 
-def test_complex_dft_linearity_and_parseval_full_batch():
-    """Size-independent properties at a full parity-config batch (N=1000, 256 MiB of c32)."""
-    n, batch = 1000, (256 << 20) // (8 * 1000)
+@pytest.mark.parametrize("n", [1000, 1536, 2187, 30720, 127, 8191])
+def test_complex_dft_linearity_and_parseval_full_batch(orc, n):
+    """Size-independent properties at the benchmark's full batch of each mixed-radix length (256 MiB of
+    c32): linearity, Parseval per signal, the inverse of the forward (x N) over the whole batch, and the
+    oracle on the first and last signals."""
+    batch = (256 << 20) // (8 * n)
     g = torch.Generator(device="cuda").manual_seed(5)
     a = torch.randn(batch, n, dtype=torch.complex64, device="cuda", generator=g)
     b = torch.randn(batch, n, dtype=torch.complex64, device="cuda", generator=g)
@@ -332,6 +335,38 @@ def test_complex_dft_linearity_and_parseval_full_batch():
     ea = (a.abs() ** 2).double().sum(dim=1) * n
     eA = (fa.abs() ** 2).double().sum(dim=1)
     assert torch.max(torch.abs(eA / ea - 1)).item() < 1e-5
+    # the inverse of the forward gives x N back for every signal of the batch
+    back = torch.empty_like(a)
+    plan.execute_batch(back, fa, batch, inverse=True)
+    err = torch.linalg.vector_norm(back / n - a) / torch.linalg.vector_norm(a)
+    assert err.item() <= 2 * c32_tolerance(n)
+    pick = [0, batch - 1]
+    ref = orc.dft(a[pick].cpu().numpy().astype(np.complex128))
+    assert rel_rms(fa[pick].cpu().numpy(), ref) <= c32_tolerance(n)
+
+
+@pytest.mark.parametrize("n", [1920, 44100, 48000])
+def test_real_dft_round_trip_and_parseval_full_batch(orc, n):
+    """The real lengths of the mixed-radix set at the benchmark's full batch (256 MiB of f32): Parseval per
+    signal (|X_0|^2 + 2 sum |X_k|^2 + |X_N/2|^2 = N sum x^2), the inverse of the forward (x N) over the whole
+    batch, and the oracle on the first and last signals."""
+    batch = (256 << 20) // (4 * n)
+    g = torch.Generator(device="cuda").manual_seed(6)
+    x = torch.randn(batch, n, device="cuda", generator=g)
+    plan = k.dft_plan_real(n)
+    X = torch.empty(batch, n // 2 + 1, dtype=torch.complex64, device="cuda")
+    plan.execute_batch(X, x, batch)
+    p = (X.abs() ** 2).double()
+    eX = p[:, 0] + p[:, -1] + 2 * p[:, 1:-1].sum(dim=1)
+    ex = (x.double() ** 2).sum(dim=1) * n
+    assert torch.max(torch.abs(eX / ex - 1)).item() < 1e-5
+    back = torch.empty_like(x)
+    plan.execute_batch(back, X, batch, inverse=True)
+    err = torch.linalg.vector_norm(back / n - x) / torch.linalg.vector_norm(x)
+    assert err.item() <= 2 * c32_tolerance(n)
+    pick = [0, batch - 1]
+    ref = orc.dft_real(x[pick].cpu().numpy().astype(np.float64))
+    assert rel_rms(X[pick].cpu().numpy(), ref) <= c32_tolerance(n)
 
 
 def test_plan_queries_and_errors():
